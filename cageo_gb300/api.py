@@ -1,0 +1,312 @@
+"""Python binding of the C ABI in include/cageo.h (ctypes; no torch types cross it).
+
+Each stage function mirrors one reference stage algorithm's ``execute``
+(see include/cageo.h for the reference interface each replaces) on CUDA
+tensors: grids are ``torch.float32`` tensors of shape (H, W) on the current
+CUDA device, directions ``int8`` (H, W, 2) holding (dx, dy), labels
+``int32`` (H, W).  Calls run on torch's current stream.  A non-zero status
+raises :class:`CageoError` with the library's message; a missing library
+raises ``FileNotFoundError`` -- there is no fallback implementation.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import _build
+
+FILTER_EXPONENTIAL = 0
+FILTER_GAUSSIAN = 1
+FILL_CPU_COMPAT = 0
+OUTSIDE = -9999
+LAKE = -9998
+
+
+class CageoError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("cageo status %d: %s" % (status, message))
+        self.status = status
+
+
+class PipelineConfig(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int), ("height", ctypes.c_int),
+                ("cell_size", ctypes.c_float), ("filter_model", ctypes.c_int),
+                ("practical_range", ctypes.c_float), ("error_mean", ctypes.c_float),
+                ("error_stddev", ctypes.c_float), ("bevel_radius", ctypes.c_int),
+                ("nodata_dem", ctypes.c_float), ("nodata_stream", ctypes.c_float),
+                ("seed", ctypes.c_uint64), ("use_graphs", ctypes.c_int)]
+
+
+class RasterInfo(ctypes.Structure):
+    _fields_ = [("ncols", ctypes.c_int), ("nrows", ctypes.c_int),
+                ("xllcorner", ctypes.c_double), ("yllcorner", ctypes.c_double),
+                ("cellsize", ctypes.c_float), ("nodata_value", ctypes.c_float),
+                ("byteorder_msb", ctypes.c_int)]
+
+
+_vp, _i, _f, _sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_size_t
+_SIGS = {
+    "cageo_version": ([], ctypes.c_char_p),
+    "cageo_last_error_string": ([], ctypes.c_char_p),
+    "cageo_noise_philox": ([_vp, _i, _i, ctypes.c_uint64, ctypes.c_uint32, _f, _f, _vp], _i),
+    "cageo_filter_radius": ([_f, _f], _i),
+    "cageo_filter_build": ([_i, _f, _f, _i, _vp], _i),
+    "cageo_convolve": ([_vp, _vp, _i, _i, _i, _vp, _i, _vp], _i),
+    "cageo_realistic_dem": ([_vp, _vp, _i, _i, _f, _vp], _i),
+    "cageo_stream_burn": ([_vp, _vp, _i, _i, _i, _f, _f, _vp], _i),
+    "cageo_pitfill_workspace_size": ([_i, _i], _sz),
+    "cageo_pitfill": ([_vp, _vp, _i, _i, _f, _i, _vp, _sz, _vp], _i),
+    "cageo_route_workspace_size": ([_i, _i], _sz),
+    "cageo_route_d8": ([_vp, _vp, _vp, _i, _i, _vp, _sz, _vp], _i),
+    "cageo_trace_workspace_size": ([_i, _i], _sz),
+    "cageo_trace": ([_vp, _vp, _vp, _i, _i, _vp, _sz, _vp], _i),
+    "cageo_border_accumulate": ([_vp, _vp, _i, _i, _vp], _i),
+    "cageo_pipeline_create": ([ctypes.POINTER(_vp), ctypes.POINTER(PipelineConfig), _vp, _vp], _i),
+    "cageo_pipeline_create_device": ([ctypes.POINTER(_vp), ctypes.POINTER(PipelineConfig), _vp,
+                                      _vp], _i),
+    "cageo_pipeline_run": ([_vp, ctypes.c_uint32, _i], _i),
+    "cageo_pipeline_counts": ([_vp, _vp], _i),
+    "cageo_pipeline_counts_device": ([_vp, _vp], _i),
+    "cageo_pipeline_last_stages": ([_vp, _vp, _vp, _vp], _i),
+    "cageo_pipeline_reset_counts": ([_vp], _i),
+    "cageo_pipeline_stream": ([_vp], _vp),
+    "cageo_pipeline_stats": ([_vp, _vp, _i], _i),
+    "cageo_pipeline_destroy": ([_vp], None),
+    "cageo_read_header": ([ctypes.c_char_p, ctypes.POINTER(RasterInfo)], _i),
+    "cageo_write_header": ([ctypes.c_char_p, ctypes.POINTER(RasterInfo)], _i),
+    "cageo_read_raster": ([ctypes.c_char_p, _vp, _sz], _i),
+    "cageo_write_raster": ([ctypes.c_char_p, _vp, _sz], _i),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded libcageo with typed signatures (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        L = _build.load()
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def _check(status):
+    if status != 0:
+        raise CageoError(status, lib().cageo_last_error_string().decode())
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream():
+    import torch
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _grid(t, dtype, name):
+    import torch
+    if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == dtype and t.is_contiguous()):
+        raise TypeError("%s must be a contiguous CUDA %s tensor" % (name, dtype))
+    return t
+
+
+def version():
+    return lib().cageo_version().decode()
+
+
+# ---- A1 ---------------------------------------------------------------------
+def noise_philox(field, seed, realization, mean=0.0, stddev=1.0):
+    import torch
+    _grid(field, torch.float32, "field")
+    H, W = field.shape
+    _check(lib().cageo_noise_philox(_ptr(field), W, H, seed, realization, mean, stddev, _stream()))
+    return field
+
+
+# ---- A2 ---------------------------------------------------------------------
+def filter_radius(practical_range, cell_size):
+    return lib().cageo_filter_radius(practical_range, cell_size)
+
+
+def filter_build(model, practical_range, cell_size, radius=None):
+    if radius is None:
+        radius = filter_radius(practical_range, cell_size)
+    n = 2 * radius + 1
+    out = np.zeros(n if model == FILTER_GAUSSIAN else n * n, np.float32)
+    _check(lib().cageo_filter_build(model, practical_range, cell_size, radius,
+                                    out.ctypes.data_as(ctypes.c_void_p)))
+    return out
+
+
+# ---- A3..A9 -------------------------------------------------------------------
+def convolve(field, model, taps, radius):
+    import torch
+    _grid(field, torch.float32, "field")
+    H, W = field.shape
+    t = torch.as_tensor(np.asarray(taps, np.float32)).to(field.device)
+    out = torch.empty_like(field)
+    _check(lib().cageo_convolve(_ptr(field), _ptr(out), W, H, model, _ptr(t), radius, _stream()))
+    return out
+
+
+def realistic_dem(dem, field, nodata_dem=-9999.0):
+    import torch
+    _grid(dem, torch.float32, "dem")
+    _grid(field, torch.float32, "field")
+    H, W = field.shape
+    _check(lib().cageo_realistic_dem(_ptr(dem), _ptr(field), W, H, nodata_dem, _stream()))
+    return field
+
+
+def stream_burn(dem, streams, bevel_radius=2, nodata_dem=-9999.0, nodata_stream=-9999.0):
+    import torch
+    _grid(dem, torch.float32, "dem")
+    _grid(streams, torch.float32, "streams")
+    H, W = dem.shape
+    _check(lib().cageo_stream_burn(_ptr(dem), _ptr(streams), W, H, bevel_radius, nodata_dem,
+                                   nodata_stream, _stream()))
+    return dem
+
+
+def pitfill(dem, nodata_dem=-9999.0, workspace=None):
+    """Quantizes `dem` in place (as the reference does) and returns the filled grid."""
+    import torch
+    _grid(dem, torch.float32, "dem")
+    H, W = dem.shape
+    filled = torch.empty_like(dem)
+    ws, wsb = (None, 0) if workspace is None else (_ptr(workspace), workspace.numel())
+    _check(lib().cageo_pitfill(_ptr(dem), _ptr(filled), W, H, nodata_dem, FILL_CPU_COMPAT, ws, wsb,
+                               _stream()))
+    return filled
+
+
+def route_d8(filled, with_flatdist=False):
+    import torch
+    _grid(filled, torch.float32, "filled")
+    H, W = filled.shape
+    d = torch.empty((H, W, 2), dtype=torch.int8, device=filled.device)
+    fd = torch.empty((H, W), dtype=torch.int32, device=filled.device) if with_flatdist else None
+    _check(lib().cageo_route_d8(_ptr(filled), _ptr(d), _ptr(fd) if fd is not None else None, W, H,
+                                None, 0, _stream()))
+    return (d, fd) if with_flatdist else d
+
+
+def trace(dirs, streams):
+    import torch
+    _grid(dirs, torch.int8, "dirs")
+    _grid(streams, torch.float32, "streams")
+    H, W = streams.shape
+    lab = torch.empty((H, W), dtype=torch.int32, device=streams.device)
+    _check(lib().cageo_trace(_ptr(dirs), _ptr(streams), _ptr(lab), W, H, None, 0, _stream()))
+    return lab
+
+
+def border_accumulate(labels, counts):
+    import torch
+    _grid(labels, torch.int32, "labels")
+    _grid(counts, torch.float32, "counts")
+    H, W = labels.shape
+    _check(lib().cageo_border_accumulate(_ptr(labels), _ptr(counts), W, H, _stream()))
+    return counts
+
+
+# ---- pipeline -------------------------------------------------------------------
+class Pipeline:
+    """The Monte Carlo loop (src/main.cpp:180-283) on device-resident grids.
+
+    ``dem`` and ``streams`` are float32 (H, W) numpy arrays (host) or CUDA
+    tensors (device).  ``run(first, count)`` accumulates border counts of
+    realizations first..first+count-1; ``counts()`` returns them as float32.
+    """
+
+    def __init__(self, dem, streams, cell_size=10.0, filter_model=FILTER_GAUSSIAN,
+                 practical_range=60.0, error_mean=0.0, error_stddev=1.0, bevel_radius=2,
+                 nodata_dem=-9999.0, nodata_stream=-9999.0, seed=0, use_graphs=True):
+        H, W = dem.shape
+        self.shape = (H, W)
+        cfg = PipelineConfig(W, H, cell_size, filter_model, practical_range, error_mean,
+                             error_stddev, bevel_radius, nodata_dem, nodata_stream, seed,
+                             1 if use_graphs else 0)
+        self._p = ctypes.c_void_p()
+        if isinstance(dem, np.ndarray):
+            d = np.ascontiguousarray(dem, np.float32)
+            s = np.ascontiguousarray(streams, np.float32)
+            _check(lib().cageo_pipeline_create(ctypes.byref(self._p), ctypes.byref(cfg),
+                                               d.ctypes.data_as(_vp), s.ctypes.data_as(_vp)))
+        else:
+            _check(lib().cageo_pipeline_create_device(ctypes.byref(self._p), ctypes.byref(cfg),
+                                                      _ptr(dem.contiguous()),
+                                                      _ptr(streams.contiguous())))
+
+    def run(self, first, count):
+        _check(lib().cageo_pipeline_run(self._p, first, count))
+
+    def counts(self, out=None):
+        """Float counts: into a host numpy array by default, or a CUDA tensor `out`."""
+        if out is not None:
+            _check(lib().cageo_pipeline_counts_device(self._p, _ptr(out)))
+            return out
+        h = np.empty(self.shape, np.float32)
+        _check(lib().cageo_pipeline_counts(self._p, h.ctypes.data_as(_vp)))
+        return h
+
+    def last_stages(self):
+        H, W = self.shape
+        f = np.empty((H, W), np.float32)
+        d = np.empty((H, W, 2), np.int8)
+        lab = np.empty((H, W), np.int32)
+        _check(lib().cageo_pipeline_last_stages(self._p, f.ctypes.data_as(_vp),
+                                                d.ctypes.data_as(_vp), lab.ctypes.data_as(_vp)))
+        return f, d, lab
+
+    def reset_counts(self):
+        _check(lib().cageo_pipeline_reset_counts(self._p))
+
+    def stats(self):
+        s = np.zeros(5, np.int64)
+        _check(lib().cageo_pipeline_stats(self._p, s.ctypes.data_as(_vp), 5))
+        return dict(fill_passes=int(s[0]), fill_phases=int(s[1]), flat_layers=int(s[2]),
+                    trace_jumps=int(s[3]), burn_reruns=int(s[4]))
+
+    @property
+    def stream(self):
+        return lib().cageo_pipeline_stream(self._p)
+
+    def close(self):
+        if self._p:
+            lib().cageo_pipeline_destroy(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---- A10 --------------------------------------------------------------------------
+def read_header(path):
+    info = RasterInfo()
+    _check(lib().cageo_read_header(os.fsencode(path), ctypes.byref(info)))
+    return info
+
+
+def write_header(path, ncols, nrows, cellsize, nodata, xll=0.0, yll=0.0):
+    info = RasterInfo(ncols, nrows, xll, yll, cellsize, nodata, 0)
+    _check(lib().cageo_write_header(os.fsencode(path), ctypes.byref(info)))
+
+
+def read_raster(path, shape):
+    out = np.empty(shape, np.float32)
+    _check(lib().cageo_read_raster(os.fsencode(path), out.ctypes.data_as(_vp), out.size))
+    return out
+
+
+def write_raster(path, data):
+    d = np.ascontiguousarray(data, np.float32)
+    _check(lib().cageo_write_raster(os.fsencode(path), d.ctypes.data_as(_vp), d.size))

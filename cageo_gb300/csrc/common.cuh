@@ -1,0 +1,107 @@
+// common.cuh -- shared device/host helpers for the cageo kernels.
+#pragma once
+#include <cstdint>
+#include <cstdio>
+#include <cuda_runtime.h>
+#include "cageo.h"
+
+namespace cageo {
+
+// ---- error reporting (thread-local last error; see cageo_last_error_string)
+void set_error(const char* fmt, ...);
+cageo_status cuda_fail(cudaError_t e, const char* what);
+
+#define CAGEO_CUDA(call)                                        \
+  do {                                                          \
+    cudaError_t e_ = (call);                                    \
+    if (e_ != cudaSuccess) return ::cageo::cuda_fail(e_, #call); \
+  } while (0)
+
+#define CAGEO_CHECK_ARG(cond, msg)                      \
+  do {                                                  \
+    if (!(cond)) {                                      \
+      ::cageo::set_error("invalid argument: %s", msg);  \
+      return CAGEO_ERR_ARGUMENT;                        \
+    }                                                   \
+  } while (0)
+
+// Grids larger than this are refused (int32 cell indices in the kernels).
+constexpr int64_t kMaxCells = (int64_t)1 << 31;
+
+inline bool valid_dims(int W, int H) {
+  return W > 0 && H > 0 && (int64_t)W * H < kMaxCells;
+}
+
+// Stream-ordered scratch: the caller's workspace when given, else
+// cudaMallocAsync / cudaFreeAsync on the stream.
+struct Scratch {
+  void* ptr = nullptr;
+  bool owned = false;
+  cudaStream_t stream = 0;
+  cageo_status acquire(void* given, size_t given_bytes, size_t need,
+                       cudaStream_t s);
+  ~Scratch();
+};
+
+inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// ---- device helpers --------------------------------------------------------
+constexpr float kInf = __builtin_huge_valf();
+
+// Monotone map float -> uint32 so that unsigned order equals float order
+// (for non-NaN values); used for atomicMin/atomicMax on floats.
+__host__ __device__ inline uint32_t float_to_ordered(float f) {
+  uint32_t u;
+  memcpy(&u, &f, 4);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__host__ __device__ inline float ordered_to_float(uint32_t u) {
+  uint32_t v = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+  float f;
+  memcpy(&f, &v, 4);
+  return f;
+}
+
+// Grid-wide barrier for persistent kernels launched cooperatively (all
+// blocks co-resident).  Sense is a generation counter.  Every wait is
+// bounded: after `limit` polls the block records an error in *err and
+// returns false; callers then leave their loops.
+struct GridSync {
+  unsigned int* count;
+  unsigned int* generation;
+  int* err;
+};
+
+__device__ inline bool grid_barrier(const GridSync& g, unsigned int nblocks) {
+  __syncthreads();
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    volatile unsigned int* gen = g.generation;
+    unsigned int my = *gen;
+    __threadfence();
+    unsigned int arrived = atomicAdd(g.count, 1u);
+    if (arrived == nblocks - 1) {
+      atomicExch(g.count, 0u);
+      __threadfence();
+      atomicAdd(g.generation, 1u);
+      ok = 1;
+    } else {
+      ok = 1;
+      long long polls = 0;
+      while (*gen == my) {
+        if (++polls > 40000000LL) {  // a few seconds at most
+          atomicExch(g.err, 1);
+          ok = 0;
+          break;
+        }
+        if (*((volatile int*)g.err)) { ok = 0; break; }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+}  // namespace cageo

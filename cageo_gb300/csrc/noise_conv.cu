@@ -1,0 +1,256 @@
+// noise_conv.cu -- A1 Philox Gaussian noise and A3 process convolution.
+//
+// Convolution kernels stage a (tile + 2r halo) block of the input in shared
+// memory with periodic wrap and compute every output with the reference's
+// summation order (ascending taps, sum starting at 0, unfused multiply and
+// add), so they equal ConvolutionAlgorithm_CPU_OpenMP bit for bit.  The
+// same kernels, instantiated with the FrontEpilogue, fuse the realistic-DEM,
+// burning and quantization steps of a realization into their store.
+#include "common.cuh"
+#include "front.cuh"
+#include "stage_math.cuh"
+
+namespace cageo {
+
+// ---- A1 ------------------------------------------------------------------
+// One thread per group of 4 consecutive cells: one Philox call gives four
+// uniforms -> two Box-Muller pairs -> four N(0,1) deviates.
+__global__ void noise_kernel(float* __restrict__ out, int64_t n, uint32_t k0,
+                             uint32_t k1, uint32_t realization,
+                             const uint32_t* __restrict__ dreal, float mean,
+                             float sd) {
+  int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t base = g * 4;
+  if (base >= n) return;
+  if (dreal) realization = *dreal;
+  U4 ctr = {(uint32_t)g, realization, kNoiseTag, (uint32_t)(g >> 32)};
+  U4 r = philox4x32_10(ctr, k0, k1);
+  float z[4];
+  {
+    float rad = sqrtf(-2.0f * logf(u01_open(r.x)));
+    float s, c;
+    sincospif(2.0f * u01_open(r.y), &s, &c);
+    z[0] = rad * c;
+    z[1] = rad * s;
+  }
+  {
+    float rad = sqrtf(-2.0f * logf(u01_open(r.z)));
+    float s, c;
+    sincospif(2.0f * u01_open(r.w), &s, &c);
+    z[2] = rad * c;
+    z[3] = rad * s;
+  }
+  float v[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) v[j] = __fadd_rn(mean, __fmul_rn(z[j], sd));
+  if (base + 4 <= n) {
+    *reinterpret_cast<float4*>(out + base) = make_float4(v[0], v[1], v[2], v[3]);
+  } else {
+    for (int j = 0; base + j < n; j++) out[base + j] = v[j];
+  }
+}
+
+// ---- A3 separable (Gaussian) ----------------------------------------------
+constexpr int kSepTW = 64, kSepTH = 32, kSepThreads = 256;
+
+__device__ inline int wrap_idx(int v, int n) {
+  v %= n;
+  return v < 0 ? v + n : v;
+}
+
+struct StoreEpilogue {
+  float* out;
+  __device__ inline float operator()(int64_t i, float v) const {
+    out[i] = v;
+    return v;
+  }
+};
+
+struct FrontEpilogue {
+  FrontParams p;
+  __device__ inline float operator()(int64_t i, float v) const {
+    return front_epilogue(p, i, v);
+  }
+};
+
+template <class Epi>
+__device__ inline void block_min_out(float local_min, const Epi&) {}
+
+__device__ inline void block_min_out(float local_min, const FrontEpilogue& e) {
+  // Block-wide min of q, then one ordered atomicMin.
+  __shared__ float red[32];
+  for (int o = 16; o > 0; o >>= 1)
+    local_min = fminf(local_min, __shfl_xor_sync(0xffffffffu, local_min, o));
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = local_min;
+  __syncthreads();
+  if (wid == 0) {
+    int nw = blockDim.x >> 5;
+    float m = lane < nw ? red[lane] : kInf;
+    for (int o = 16; o > 0; o >>= 1)
+      m = fminf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0 && m < kInf) atomicMin(e.p.min_ord, float_to_ordered(m));
+  }
+}
+
+template <class Epi>
+__global__ void __launch_bounds__(kSepThreads)
+conv_sep_kernel(const float* __restrict__ in, int W, int H,
+                const float* __restrict__ taps, int r, Epi epi) {
+  extern __shared__ float sm[];
+  const int L = 2 * r + 1;
+  const int IW = kSepTW + 2 * r, IH = kSepTH + 2 * r;
+  float* s_taps = sm;
+  float* s_in = sm + ((L + 3) & ~3);
+  float* s_tmp = s_in + IW * IH;
+  const int x0 = blockIdx.x * kSepTW, y0 = blockIdx.y * kSepTH;
+  for (int t = threadIdx.x; t < L; t += blockDim.x) s_taps[t] = taps[t];
+  for (int idx = threadIdx.x; idx < IW * IH; idx += blockDim.x) {
+    int iy = idx / IW, ix = idx - iy * IW;
+    int gy = wrap_idx(y0 - r + iy, H), gx = wrap_idx(x0 - r + ix, W);
+    s_in[idx] = in[(int64_t)gy * W + gx];
+  }
+  __syncthreads();
+  // Column pass: tmp[y][ix] = sum_t in[y+t][ix] * taps[t].
+  for (int idx = threadIdx.x; idx < IW * kSepTH; idx += blockDim.x) {
+    int y = idx / IW, ix = idx - y * IW;
+    float sum = 0.0f;
+    const float* col = s_in + y * IW + ix;
+    for (int t = 0; t < L; t++) sum = __fadd_rn(sum, __fmul_rn(col[t * IW], s_taps[t]));
+    s_tmp[idx] = sum;
+  }
+  __syncthreads();
+  // Row pass and store.
+  float local_min = kInf;
+  for (int idx = threadIdx.x; idx < kSepTW * kSepTH; idx += blockDim.x) {
+    int y = idx / kSepTW, x = idx - y * kSepTW;
+    int gy = y0 + y, gx = x0 + x;
+    if (gy >= H || gx >= W) continue;
+    const float* row = s_tmp + y * IW + x;
+    float sum = 0.0f;
+    for (int t = 0; t < L; t++) sum = __fadd_rn(sum, __fmul_rn(row[t], s_taps[t]));
+    float q = epi((int64_t)gy * W + gx, sum);
+    local_min = fminf(local_min, q);
+  }
+  block_min_out(local_min, epi);
+}
+
+// ---- A3 full 2D (exponential) -----------------------------------------------
+constexpr int kTwoDT = 32, kTwoDThreads = 256;
+
+template <class Epi>
+__global__ void __launch_bounds__(kTwoDThreads)
+conv_2d_kernel(const float* __restrict__ in, int W, int H,
+               const float* __restrict__ filt, int r, Epi epi) {
+  extern __shared__ float sm[];
+  const int L = 2 * r + 1;
+  const int IW = kTwoDT + 2 * r;
+  float* s_f = sm;
+  float* s_in = sm + ((L * L + 3) & ~3);
+  const int x0 = blockIdx.x * kTwoDT, y0 = blockIdx.y * kTwoDT;
+  for (int t = threadIdx.x; t < L * L; t += blockDim.x) s_f[t] = filt[t];
+  for (int idx = threadIdx.x; idx < IW * IW; idx += blockDim.x) {
+    int iy = idx / IW, ix = idx - iy * IW;
+    int gy = wrap_idx(y0 - r + iy, H), gx = wrap_idx(x0 - r + ix, W);
+    s_in[idx] = in[(int64_t)gy * W + gx];
+  }
+  __syncthreads();
+  // Each thread: column tx, rows ty, ty+8, ty+16, ty+24 (4 independent sums).
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  float sum[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  for (int fy = 0; fy < L; fy++) {
+    const float* frow = s_f + fy * L;
+    for (int fx = 0; fx < L; fx++) {
+      float f = frow[fx];
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        sum[k] = __fadd_rn(sum[k], __fmul_rn(s_in[(ty + 8 * k + fy) * IW + tx + fx], f));
+    }
+  }
+  float local_min = kInf;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    int gy = y0 + ty + 8 * k, gx = x0 + tx;
+    if (gy < H && gx < W) local_min = fminf(local_min, epi((int64_t)gy * W + gx, sum[k]));
+  }
+  block_min_out(local_min, epi);
+}
+
+size_t conv_smem_bytes(int model, int r) {
+  int L = 2 * r + 1;
+  if (model == CAGEO_FILTER_GAUSSIAN) {
+    int IW = kSepTW + 2 * r, IH = kSepTH + 2 * r;
+    return sizeof(float) * (((L + 3) & ~3) + (size_t)IW * IH + (size_t)IW * kSepTH);
+  }
+  int IW = kTwoDT + 2 * r;
+  return sizeof(float) * (((L * L + 3) & ~3) + (size_t)IW * IW);
+}
+
+template <class Epi>
+cageo_status launch_conv(const float* in, int W, int H, int model,
+                         const float* filt, int r, const Epi& epi,
+                         cudaStream_t s) {
+  size_t smem = conv_smem_bytes(model, r);
+  if (smem > 227 * 1024) {
+    set_error("filter radius %d needs %zu bytes of shared memory", r, smem);
+    return CAGEO_ERR_ARGUMENT;
+  }
+  if (model == CAGEO_FILTER_GAUSSIAN) {
+    CAGEO_CUDA(cudaFuncSetAttribute(conv_sep_kernel<Epi>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((W + kSepTW - 1) / kSepTW, (H + kSepTH - 1) / kSepTH);
+    conv_sep_kernel<Epi><<<grid, kSepThreads, smem, s>>>(in, W, H, filt, r, epi);
+  } else {
+    CAGEO_CUDA(cudaFuncSetAttribute(conv_2d_kernel<Epi>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((W + kTwoDT - 1) / kTwoDT, (H + kTwoDT - 1) / kTwoDT);
+    conv_2d_kernel<Epi><<<grid, kTwoDThreads, smem, s>>>(in, W, H, filt, r, epi);
+  }
+  CAGEO_CUDA(cudaGetLastError());
+  return CAGEO_OK;
+}
+
+cageo_status launch_noise(float* d, int64_t n, uint64_t seed, uint32_t realization,
+                          const uint32_t* dreal, float mean, float sd, cudaStream_t s) {
+  int64_t groups = (n + 3) / 4;
+  int threads = 256;
+  int64_t blocks = (groups + threads - 1) / threads;
+  noise_kernel<<<(unsigned)blocks, threads, 0, s>>>(d, n, (uint32_t)seed,
+                                                    (uint32_t)(seed >> 32), realization,
+                                                    dreal, mean, sd);
+  CAGEO_CUDA(cudaGetLastError());
+  return CAGEO_OK;
+}
+
+cageo_status launch_front(const float* noise, int W, int H, int model,
+                          const float* filt, int r, const FrontParams& fp,
+                          cudaStream_t s) {
+  FrontEpilogue e{fp};
+  return launch_conv(noise, W, H, model, filt, r, e, s);
+}
+
+}  // namespace cageo
+
+using namespace cageo;
+
+extern "C" cageo_status cageo_noise_philox(float* d_field, int W, int H,
+                                           uint64_t seed, uint32_t realization,
+                                           float mean, float stddev,
+                                           cudaStream_t stream) {
+  CAGEO_CHECK_ARG(d_field && valid_dims(W, H), "field pointer and size");
+  return launch_noise(d_field, (int64_t)W * H, seed, realization, nullptr, mean, stddev,
+                      stream);
+}
+
+extern "C" cageo_status cageo_convolve(const float* d_in, float* d_out, int W,
+                                       int H, int model, const float* d_filter,
+                                       int radius, cudaStream_t stream) {
+  CAGEO_CHECK_ARG(d_in && d_out && d_filter && valid_dims(W, H), "pointers and size");
+  CAGEO_CHECK_ARG(d_in != d_out, "convolution cannot run in place");
+  CAGEO_CHECK_ARG(model == CAGEO_FILTER_GAUSSIAN || model == CAGEO_FILTER_EXPONENTIAL,
+                  "filter model");
+  CAGEO_CHECK_ARG(radius >= 0 && radius < W && radius < H,
+                  "filter radius must be below the grid width and height");
+  StoreEpilogue e{d_out};
+  return launch_conv(d_in, W, H, model, d_filter, radius, e, stream);
+}

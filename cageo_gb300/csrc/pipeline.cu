@@ -1,0 +1,380 @@
+// pipeline.cu -- the Monte Carlo loop of src/main.cpp:180-283 as one object
+// that owns its device buffers.
+//
+// A realization is: noise (Philox) -> fused convolution + realistic DEM +
+// burning + quantization (front) -> pit fill -> routing -> tracing ->
+// border counts.  The launch sequence of one realization reads the
+// realization number from device memory, so it is captured once in a CUDA
+// graph and replayed; the data-dependent loops (fill passes, flat BFS
+// layers, pointer jumps) run inside persistent kernels and need no host
+// round trip.  Counts accumulate in uint32.
+//
+// The fused front uses a burn code precomputed from the stream raster.  It
+// flags a realization where that code may differ from the reference's
+// in-place burning (a stream cell whose realistic elevation equals NODATA);
+// such a realization is not counted by the fast path and is recomputed with
+// the stage kernels, which follow the reference step by step.  With a
+// NODATA of 0 every realization takes the stage path.
+#include <cmath>
+#include <vector>
+#include "common.cuh"
+#include "front.cuh"
+#include "pitfill.cuh"
+#include "routing.cuh"
+
+namespace cageo {
+cageo_status launch_noise(float* d, int64_t n, uint64_t seed, uint32_t realization,
+                          const uint32_t* dreal, float mean, float sd, cudaStream_t s);
+cageo_status launch_front(const float* noise, int W, int H, int model, const float* filt,
+                          int r, const FrontParams& fp, cudaStream_t s);
+cageo_status launch_burn_code(const float* streams, uint8_t* code, int W, int H,
+                              float nodata_stream, int bevel, float* factor_out,
+                              cudaStream_t s);
+cageo_status launch_realistic(const float* dem, float* field, int64_t n, float nodata,
+                              cudaStream_t s);
+cageo_status launch_burn_stage(const float* src, float* dst, const float* streams, int W,
+                               int H, int bevel, float nodata_dem, float nodata_stream,
+                               cudaStream_t s);
+
+// Accumulate the border mask unless the realization was flagged; a flagged
+// realization index is appended to the redo list.
+__global__ void border_gated_kernel(const int* __restrict__ label, uint32_t* __restrict__ count,
+                                    int W, int H, const int* __restrict__ anomaly) {
+  if (*anomaly) return;
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= W || y >= H) return;
+  int64_t i = (int64_t)y * W + x;
+  const int c = label[i];
+  if (c == kLake) return;
+#pragma unroll
+  for (int n = 0; n < 8; n++) {
+    int nx = x + d8_dx(n), ny = y + d8_dy(n);
+    if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+    int v = label[(int64_t)ny * W + nx];
+    if (c < v && v != kLake) { count[i] += 1u; return; }
+  }
+}
+
+// End of a realization: record a flagged realization, clear the flag and
+// advance the device realization counter.
+__global__ void realization_end_kernel(uint32_t* real, int* anomaly, uint32_t* redo,
+                                       unsigned int* nredo) {
+  if (threadIdx.x == 0) {
+    if (*anomaly) {
+      unsigned int k = atomicAdd(nredo, 1u);
+      if (k < 4096) redo[k] = *real;
+      *anomaly = 0;
+    }
+    *real += 1u;
+  }
+}
+
+__global__ void counts_to_float_kernel(const uint32_t* __restrict__ c, float* __restrict__ f,
+                                       int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) f[i] = (float)c[i];
+}
+
+}  // namespace cageo
+
+using namespace cageo;
+
+struct cageo_pipeline {
+  cageo_pipeline_config cfg{};
+  int W = 0, H = 0;
+  int64_t N = 0;
+  int radius = 0;
+  cudaStream_t stream = nullptr;
+  float *dem = nullptr, *streams = nullptr, *noise = nullptr, *q = nullptr, *filled = nullptr,
+        *filter = nullptr, *tmp = nullptr;
+  uint8_t* code = nullptr;
+  int8_t* dir = nullptr;
+  int *flatdist = nullptr, *label = nullptr;
+  uint32_t* counts = nullptr;
+  void *fill_ws = nullptr, *route_ws = nullptr, *trace_ws = nullptr;
+  FillWork fw;
+  RouteWork rw;
+  TraceWork tw;
+  // device scalars: [0] realization counter, [1] anomaly, [2] nredo, [3..] redo list
+  uint32_t* dscal = nullptr;
+  FrontParams fp{};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool graph_ok = false;
+  int64_t stats[5] = {0, 0, 0, 0, 0};
+};
+
+namespace {
+
+void free_all(cageo_pipeline* p) {
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  void* bufs[] = {p->dem, p->streams, p->noise, p->q, p->filled, p->filter, p->tmp, p->code,
+                  p->dir, p->flatdist, p->label, p->counts, p->fill_ws, p->route_ws,
+                  p->trace_ws, p->dscal};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  if (p->stream) cudaStreamDestroy(p->stream);
+}
+
+// Launch sequence of one realization on the fast path.  The realization
+// number is read from dscal[0] by the noise kernel.
+cageo_status enqueue_fast(cageo_pipeline* p) {
+  cudaStream_t s = p->stream;
+  const cageo_pipeline_config& c = p->cfg;
+  cageo_status st;
+  if ((st = fill_reset_scalars(p->fw, s))) return st;
+  if ((st = launch_noise(p->noise, p->N, c.seed, 0, p->dscal, c.error_mean, c.error_stddev, s)))
+    return st;
+  if ((st = launch_front(p->noise, p->W, p->H, c.filter_model, p->filter, p->radius, p->fp, s)))
+    return st;
+  if ((st = fill_run(p->q, p->filled, p->fw, c.nodata_dem, s))) return st;
+  if ((st = route_run(p->filled, p->dir, p->flatdist, p->rw, s))) return st;
+  if ((st = trace_run(p->dir, p->streams, p->label, p->tw, s))) return st;
+  dim3 b(32, 8), g((p->W + 31) / 32, (p->H + 7) / 8);
+  border_gated_kernel<<<g, b, 0, s>>>(p->label, p->counts, p->W, p->H, (const int*)p->dscal + 1);
+  realization_end_kernel<<<1, 32, 0, s>>>(p->dscal, (int*)p->dscal + 1, p->dscal + 3,
+                                          p->dscal + 2);
+  CAGEO_CUDA(cudaGetLastError());
+  return CAGEO_OK;
+}
+
+// Reference-order stage sequence for one realization (exact burning).
+cageo_status run_stage_path(cageo_pipeline* p, uint32_t r) {
+  cudaStream_t s = p->stream;
+  const cageo_pipeline_config& c = p->cfg;
+  cageo_status st;
+  if ((st = fill_reset_scalars(p->fw, s))) return st;
+  if ((st = launch_noise(p->noise, p->N, c.seed, r, nullptr, c.error_mean, c.error_stddev, s)))
+    return st;
+  if ((st = cageo_convolve(p->noise, p->tmp, p->W, p->H, c.filter_model, p->filter, p->radius, s)))
+    return st;
+  if ((st = launch_realistic(p->dem, p->tmp, p->N, c.nodata_dem, s))) return st;
+  if ((st = launch_burn_stage(p->tmp, p->q, p->streams, p->W, p->H, c.bevel_radius, c.nodata_dem,
+                              c.nodata_stream, s)))
+    return st;
+  if ((st = fill_quantize_min(p->q, p->fw, c.nodata_dem, s))) return st;
+  if ((st = fill_run(p->q, p->filled, p->fw, c.nodata_dem, s))) return st;
+  if ((st = route_run(p->filled, p->dir, p->flatdist, p->rw, s))) return st;
+  if ((st = trace_run(p->dir, p->streams, p->label, p->tw, s))) return st;
+  if ((st = border_u32(p->label, p->counts, p->W, p->H, s))) return st;
+  return CAGEO_OK;
+}
+
+template <typename T>
+cageo_status dalloc(T** ptr, size_t bytes) {
+  CAGEO_CUDA(cudaMalloc((void**)ptr, bytes ? bytes : 16));
+  return CAGEO_OK;
+}
+
+cageo_status create_common(cageo_pipeline** out, const cageo_pipeline_config* cfg,
+                           const float* dem, const float* streams, cudaMemcpyKind kind) {
+  CAGEO_CHECK_ARG(out && cfg && dem && streams, "null argument");
+  const int W = cfg->width, H = cfg->height;
+  CAGEO_CHECK_ARG(valid_dims(W, H) && W >= 2 && H >= 2, "grid size");
+  CAGEO_CHECK_ARG(W <= 65535 && H <= 65535, "width and height must be <= 65535");
+  CAGEO_CHECK_ARG(cfg->filter_model == CAGEO_FILTER_GAUSSIAN ||
+                      cfg->filter_model == CAGEO_FILTER_EXPONENTIAL,
+                  "filter model");
+  CAGEO_CHECK_ARG(cfg->bevel_radius >= 1 && cfg->bevel_radius <= 5, "bevel radius must be 1..5");
+  CAGEO_CHECK_ARG(cfg->cell_size > 0 && cfg->practical_range > 0, "range and cell size");
+  const int r = cageo_filter_radius(cfg->practical_range, cfg->cell_size);
+  CAGEO_CHECK_ARG(r >= 0 && r < W && r < H, "filter radius must be below the grid size");
+  auto* p = new cageo_pipeline();
+  p->cfg = *cfg;
+  p->W = W;
+  p->H = H;
+  p->N = (int64_t)W * H;
+  p->radius = r;
+  cageo_status st = CAGEO_OK;
+  auto fail = [&](cageo_status s) {
+    free_all(p);
+    delete p;
+    return s;
+  };
+  if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(cuda_fail(cudaGetLastError(), "cudaStreamCreate"));
+  const size_t fb = sizeof(float) * p->N;
+  const int L = 2 * r + 1;
+  const int taps = cfg->filter_model == CAGEO_FILTER_GAUSSIAN ? L : L * L;
+  if ((st = dalloc(&p->dem, fb)) || (st = dalloc(&p->streams, fb)) ||
+      (st = dalloc(&p->noise, fb)) || (st = dalloc(&p->q, fb)) || (st = dalloc(&p->filled, fb)) ||
+      (st = dalloc(&p->tmp, fb)) || (st = dalloc(&p->filter, sizeof(float) * taps)) ||
+      (st = dalloc(&p->code, (size_t)p->N)) || (st = dalloc(&p->dir, 2 * (size_t)p->N)) ||
+      (st = dalloc(&p->flatdist, 4 * (size_t)p->N)) || (st = dalloc(&p->label, 4 * (size_t)p->N)) ||
+      (st = dalloc(&p->counts, 4 * (size_t)p->N)) ||
+      (st = dalloc(&p->fill_ws, fill_workspace_bytes(W, H))) ||
+      (st = dalloc(&p->route_ws, route_workspace_bytes(W, H))) ||
+      (st = dalloc(&p->trace_ws, trace_workspace_bytes(W, H))) ||
+      (st = dalloc(&p->dscal, sizeof(uint32_t) * (3 + 4096))))
+    return fail(st);
+  p->fw = fill_carve(p->fill_ws, W, H);
+  p->rw = route_carve(p->route_ws, W, H);
+  p->tw = trace_carve(p->trace_ws, W, H);
+  std::vector<float> hf(taps);
+  if ((st = cageo_filter_build(cfg->filter_model, cfg->practical_range, cfg->cell_size, r,
+                               hf.data())))
+    return fail(st);
+  cudaStream_t s = p->stream;
+#define PCUDA(call)                                          \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return fail(cuda_fail(e_, #call)); \
+  } while (0)
+  PCUDA(cudaMemcpyAsync(p->filter, hf.data(), sizeof(float) * taps, cudaMemcpyHostToDevice, s));
+  PCUDA(cudaMemcpyAsync(p->dem, dem, fb, kind, s));
+  PCUDA(cudaMemcpyAsync(p->streams, streams, fb, kind, s));
+  PCUDA(cudaMemsetAsync(p->counts, 0, 4 * (size_t)p->N, s));
+  PCUDA(cudaMemsetAsync(p->dscal, 0, sizeof(uint32_t) * 3, s));
+  if ((st = launch_burn_code(p->streams, p->code, W, H, cfg->nodata_stream, cfg->bevel_radius,
+                             p->fp.factor, s)))
+    return fail(st);
+  p->fp.dem = p->dem;
+  p->fp.code = p->code;
+  p->fp.q = p->q;
+  p->fp.min_ord = fill_min_slot(p->fw);
+  p->fp.anomaly = (int*)p->dscal + 1;
+  p->fp.nodata_dem = cfg->nodata_dem;
+  PCUDA(cudaStreamSynchronize(s));
+#undef PCUDA
+  *out = p;
+  return CAGEO_OK;
+}
+
+}  // namespace
+
+extern "C" cageo_status cageo_pipeline_create(cageo_pipeline** out,
+                                              const cageo_pipeline_config* cfg,
+                                              const float* h_dem, const float* h_streams) {
+  return create_common(out, cfg, h_dem, h_streams, cudaMemcpyHostToDevice);
+}
+
+extern "C" cageo_status cageo_pipeline_create_device(cageo_pipeline** out,
+                                                     const cageo_pipeline_config* cfg,
+                                                     const float* d_dem,
+                                                     const float* d_streams) {
+  return create_common(out, cfg, d_dem, d_streams, cudaMemcpyDeviceToDevice);
+}
+
+extern "C" cageo_status cageo_pipeline_run(cageo_pipeline* p, uint32_t first, int count) {
+  CAGEO_CHECK_ARG(p && count >= 0, "pipeline and count");
+  cudaStream_t s = p->stream;
+  cageo_status st;
+  CAGEO_CUDA(cudaMemcpyAsync(p->dscal, &first, sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+  CAGEO_CUDA(cudaMemsetAsync(p->dscal + 1, 0, 2 * sizeof(uint32_t), s));
+  const bool stage_only = p->cfg.nodata_dem == 0.0f;
+  int done = 0;
+  if (!stage_only && count > 0 && p->cfg.use_graphs && !p->graph_ok && !p->exec) {
+    // Warm-up outside capture (kernel attributes, occupancy caches), then
+    // capture one realization.
+    if ((st = enqueue_fast(p))) return st;
+    done = 1;
+    CAGEO_CUDA(cudaStreamSynchronize(s));
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      cageo_status cst = enqueue_fast(p);
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamEndCapture(s, &g);
+      if (cst == CAGEO_OK && e == cudaSuccess &&
+          cudaGraphInstantiate(&p->exec, g, 0) == cudaSuccess) {
+        p->graph = g;
+        p->graph_ok = true;
+      } else {
+        if (g) cudaGraphDestroy(g);
+        p->exec = nullptr;
+      }
+      cudaGetLastError();
+    }
+    // A failed capture leaves the flag off: the launches run directly.
+    if (!p->graph_ok) p->cfg.use_graphs = 0;
+  }
+  for (int i = done; i < count; i++) {
+    if (stage_only) {
+      if ((st = run_stage_path(p, first + (uint32_t)i))) return st;
+    } else if (p->graph_ok) {
+      CAGEO_CUDA(cudaGraphLaunch(p->exec, s));
+    } else {
+      if ((st = enqueue_fast(p))) return st;
+    }
+  }
+  CAGEO_CUDA(cudaStreamSynchronize(s));
+  int64_t fs[2] = {0, 0}, layers = 0, jumps = 0;
+  if ((st = fill_check_status(p->fw, fs))) return st;
+  if ((st = route_check_status(p->rw, &layers))) return st;
+  if ((st = trace_check_status(p->tw, &jumps))) return st;
+  uint32_t nredo = 0;
+  CAGEO_CUDA(cudaMemcpy(&nredo, p->dscal + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  if (nredo) {
+    if (nredo > 4096) {
+      set_error("more than 4096 realizations need the exact burning path in one run");
+      return CAGEO_ERR_NO_CONVERGENCE;
+    }
+    std::vector<uint32_t> redo(nredo);
+    CAGEO_CUDA(cudaMemcpy(redo.data(), p->dscal + 3, sizeof(uint32_t) * nredo,
+                          cudaMemcpyDeviceToHost));
+    for (uint32_t r : redo)
+      if ((st = run_stage_path(p, r))) return st;
+    CAGEO_CUDA(cudaStreamSynchronize(s));
+    if ((st = fill_check_status(p->fw, fs))) return st;
+  }
+  p->stats[0] = fs[0];
+  p->stats[1] = fs[1];
+  p->stats[2] = layers;
+  p->stats[3] = jumps;
+  p->stats[4] = nredo;
+  return CAGEO_OK;
+}
+
+extern "C" cageo_status cageo_pipeline_counts_device(cageo_pipeline* p, float* d_out) {
+  CAGEO_CHECK_ARG(p && d_out, "null argument");
+  counts_to_float_kernel<<<(unsigned)((p->N + 255) / 256), 256, 0, p->stream>>>(p->counts, d_out,
+                                                                                 p->N);
+  CAGEO_CUDA(cudaGetLastError());
+  CAGEO_CUDA(cudaStreamSynchronize(p->stream));
+  return CAGEO_OK;
+}
+
+extern "C" cageo_status cageo_pipeline_counts(cageo_pipeline* p, float* h_out) {
+  CAGEO_CHECK_ARG(p && h_out, "null argument");
+  counts_to_float_kernel<<<(unsigned)((p->N + 255) / 256), 256, 0, p->stream>>>(p->counts, p->tmp,
+                                                                                 p->N);
+  CAGEO_CUDA(cudaGetLastError());
+  CAGEO_CUDA(cudaMemcpyAsync(h_out, p->tmp, sizeof(float) * p->N, cudaMemcpyDeviceToHost,
+                             p->stream));
+  CAGEO_CUDA(cudaStreamSynchronize(p->stream));
+  return CAGEO_OK;
+}
+
+extern "C" cageo_status cageo_pipeline_last_stages(cageo_pipeline* p, float* h_filled,
+                                                   int8_t* h_dir, int* h_label) {
+  CAGEO_CHECK_ARG(p, "null pipeline");
+  cudaStream_t s = p->stream;
+  if (h_filled)
+    CAGEO_CUDA(cudaMemcpyAsync(h_filled, p->filled, 4 * p->N, cudaMemcpyDeviceToHost, s));
+  if (h_dir) CAGEO_CUDA(cudaMemcpyAsync(h_dir, p->dir, 2 * p->N, cudaMemcpyDeviceToHost, s));
+  if (h_label) CAGEO_CUDA(cudaMemcpyAsync(h_label, p->label, 4 * p->N, cudaMemcpyDeviceToHost, s));
+  CAGEO_CUDA(cudaStreamSynchronize(s));
+  return CAGEO_OK;
+}
+
+extern "C" cageo_status cageo_pipeline_reset_counts(cageo_pipeline* p) {
+  CAGEO_CHECK_ARG(p, "null pipeline");
+  CAGEO_CUDA(cudaMemsetAsync(p->counts, 0, 4 * (size_t)p->N, p->stream));
+  CAGEO_CUDA(cudaStreamSynchronize(p->stream));
+  return CAGEO_OK;
+}
+
+extern "C" cudaStream_t cageo_pipeline_stream(cageo_pipeline* p) { return p ? p->stream : nullptr; }
+
+extern "C" cageo_status cageo_pipeline_stats(cageo_pipeline* p, int64_t* h_stats, int n) {
+  CAGEO_CHECK_ARG(p && h_stats, "null argument");
+  for (int i = 0; i < n && i < 5; i++) h_stats[i] = p->stats[i];
+  return CAGEO_OK;
+}
+
+extern "C" void cageo_pipeline_destroy(cageo_pipeline* p) {
+  if (!p) return;
+  cudaStreamSynchronize(p->stream);
+  free_all(p);
+  delete p;
+}

@@ -1,0 +1,451 @@
+// pitfill.cu -- A6 pit filling with the semantics of the reference's CPU
+// path (src/pitfilling/PitFillingAlgorithmCPUOpenMP.h:68-242).
+//
+// The CPU fill is a bucket priority-flood over 1 mm levels in which a
+// popped cell expands its neighbours only if its value v survives
+// toElev(toIndex(v)) == v ("passable").  The result is: outlets (border
+// cells and cells equal to 0) keep q; every other reached cell gets
+// W = max(q, L) where L is the lowest value among neighbours that expand;
+// a non-passable cell expands only when it was reached at a level L >= q;
+// unreached cells keep q.  Whether a non-passable cell expands depends only
+// on cells with a strictly lower q, so the solution is unique, and it is
+// computed here by monotone relaxations:
+//
+//   1. flood A: every reached cell relays (non-passable outlets do not):
+//      gives L_A <= L everywhere (a lower bound);
+//   2. non-passable cells with L_A >= q are certainly expanding ("confirmed");
+//      the other non-passable cells are walls for now;
+//   3. flood B from +inf with walls: an upper bound L_B >= L;
+//   4. phases: M = min L_B over unconfirmed non-passable cells with
+//      L_B >= q; every such cell with q <= M is confirmed (no later change
+//      can take its level below M >= q); relax again; repeat until none.
+//
+// Each flood is a persistent cooperative kernel.  One warp owns a 32x32
+// tile at a time, stages W, q, flags and the relay values of a one-cell
+// halo in shared memory and sweeps it down, up, right and left (Gauss-Seidel)
+// until it stops changing; a tile whose border changed queues the
+// neighbouring tiles for the next pass.  Passes end when no tile is queued.
+// Every grid-wide wait and every loop is bounded; exceeding a bound sets an
+// error flag that the host turns into CAGEO_ERR_NO_CONVERGENCE.
+#include <algorithm>
+#include "common.cuh"
+#include "pitfill.cuh"
+#include "stage_math.cuh"
+
+namespace cageo {
+
+// Per-cell flag bits.
+constexpr uint8_t FNODATA = 0x01, FOUTLET = 0x02, FNONPASS = 0x04, FCONF = 0x08,
+                  FBELOW = 0x10, FDIRTY = 0x40;
+
+// Scalar block layout (unsigned ints).
+enum : int {
+  S_MIN = 0,       // ordered min of q (minE)
+  S_BAR_COUNT = 1,
+  S_BAR_GEN = 2,
+  S_ERR = 3,       // 0 ok, 1 barrier wait limit, 2 pass limit
+  S_LIST = 4,      // 3 slots: worklist counts
+  S_M = 7,         // 3 slots: ordered phase minima
+  S_CAND = 10,     // candidate count
+  S_PASS = 11,     // last pass number
+  S_PHASES = 12,
+  S_SIZE = 16
+};
+
+constexpr int kTile = 32;
+constexpr int kWarps = 4;
+constexpr int kRS = 35;           // relay row stride (34 used)
+constexpr int kWS = 33;           // W/q row stride
+constexpr int kFS = 36;           // flag row stride (bytes)
+constexpr int kMaxRounds = 64;
+constexpr int kMaxPasses = 1000000;
+
+struct WarpSmem {
+  float R[34 * kRS];
+  float Wv[kTile * kWS];
+  float Qv[kTile * kWS];
+  uint8_t F[kTile * kFS];
+};
+
+size_t fill_workspace_bytes(int W, int H) {
+  size_t n = (size_t)W * H;
+  size_t nt = (size_t)((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile);
+  return align_up(n, 256) + align_up(nt * 4, 256) + align_up(2 * nt * 4, 256) +
+         align_up(n * 4, 256) + 256;
+}
+
+FillWork fill_carve(void* base, int W, int H) {
+  FillWork w;
+  w.W = W;
+  w.H = H;
+  w.tiles_x = (W + kTile - 1) / kTile;
+  w.tiles_y = (H + kTile - 1) / kTile;
+  size_t n = (size_t)W * H, nt = (size_t)w.tiles_x * w.tiles_y;
+  char* p = (char*)base;
+  w.flags = (uint8_t*)p;
+  p += align_up(n, 256);
+  w.queued = (int*)p;
+  p += align_up(nt * 4, 256);
+  w.lists = (int*)p;
+  p += align_up(2 * nt * 4, 256);
+  w.cand = (uint32_t*)p;
+  p += align_up(n * 4, 256);
+  w.scal = (unsigned int*)p;
+  return w;
+}
+
+unsigned int* fill_min_slot(const FillWork& w) { return w.scal + S_MIN; }
+
+template <int MODE>
+__device__ __forceinline__ float relay(float w, uint8_t f, float q) {
+  if (f & FNODATA) return kInf;
+  if (f & FOUTLET) return (f & FNONPASS) ? kInf : q;
+  if (MODE == 0 || !(f & FNONPASS)) return w;
+  return ((f & FCONF) && !(f & FBELOW)) ? w : kInf;
+}
+
+struct FloodArgs {
+  const float* q;
+  float* Wg;
+  FillWork w;
+};
+
+__device__ __forceinline__ void enqueue(const FillWork& w, int t, int k) {
+  if (atomicMax(&w.queued[t], k) < k) {
+    unsigned int pos = atomicAdd(&w.scal[S_LIST + k % 3], 1u);
+    w.lists[(k & 1) * (w.tiles_x * w.tiles_y) + pos] = t;
+  }
+}
+
+// Relax cell (x, y) of the staged tile; returns true if it changed.
+template <int MODE>
+__device__ __forceinline__ bool relax(WarpSmem& s, int x, int y) {
+  uint8_t f = s.F[y * kFS + x];
+  if (f & (FNODATA | FOUTLET)) return false;
+  const float* r = &s.R[(y + 1) * kRS + (x + 1)];
+  float m = fminf(fminf(fminf(r[-kRS - 1], r[-kRS]), fminf(r[-kRS + 1], r[-1])),
+                  fminf(fminf(r[1], r[kRS - 1]), fminf(r[kRS], r[kRS + 1])));
+  float w = s.Wv[y * kWS + x];
+  float qv = s.Qv[y * kWS + x];
+  float nw = fminf(w, fmaxf(qv, m));
+  uint8_t nf = f | ((m < qv) ? FBELOW : 0);
+  if (nw != w || nf != f) {
+    s.Wv[y * kWS + x] = nw;
+    s.F[y * kFS + x] = nf | FDIRTY;
+    s.R[(y + 1) * kRS + (x + 1)] = relay<MODE>(nw, nf, qv);
+    return true;
+  }
+  return false;
+}
+
+template <int MODE>
+__device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
+                             int lane) {
+  const FillWork& w = a.w;
+  const int W = w.W, H = w.H;
+  const int tx = t % w.tiles_x, ty = t / w.tiles_x;
+  const int x0 = tx * kTile, y0 = ty * kTile;
+  for (int idx = lane; idx < 34 * 34; idx += 32) {
+    int hy = idx / 34, hx = idx - hy * 34;
+    int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
+    float wv = kInf, qv = 0.0f;
+    uint8_t fv = FNODATA;
+    if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+      int64_t i = (int64_t)gy * W + gx;
+      wv = a.Wg[i];
+      qv = a.q[i];
+      fv = w.flags[i];
+    }
+    s.R[hy * kRS + hx] = relay<MODE>(wv, fv, qv);
+    if (hx >= 1 && hx <= kTile && hy >= 1 && hy <= kTile) {
+      s.Wv[(hy - 1) * kWS + hx - 1] = wv;
+      s.Qv[(hy - 1) * kWS + hx - 1] = qv;
+      s.F[(hy - 1) * kFS + hx - 1] = fv;
+    }
+  }
+  __syncwarp();
+  bool capped = true;
+  for (int round = 0; round < kMaxRounds; round++) {
+    bool any = false;
+    for (int y = 0; y < kTile; y++) { any |= relax<MODE>(s, lane, y); __syncwarp(); }
+    for (int y = kTile - 1; y >= 0; y--) { any |= relax<MODE>(s, lane, y); __syncwarp(); }
+    for (int x = 0; x < kTile; x++) { any |= relax<MODE>(s, x, lane); __syncwarp(); }
+    for (int x = kTile - 1; x >= 0; x--) { any |= relax<MODE>(s, x, lane); __syncwarp(); }
+    if (!__any_sync(0xffffffffu, any)) { capped = false; break; }
+  }
+  // Write back changed cells; note which borders changed.
+  unsigned int sides = 0;  // 1 L, 2 R, 4 T, 8 B, 16 TL, 32 TR, 64 BL, 128 BR
+  for (int idx = lane; idx < kTile * kTile; idx += 32) {
+    int y = idx >> 5, x = idx & 31;
+    uint8_t f = s.F[y * kFS + x];
+    if (f & FDIRTY) {
+      int64_t i = (int64_t)(y0 + y) * W + (x0 + x);
+      a.Wg[i] = s.Wv[y * kWS + x];
+      w.flags[i] = f & (uint8_t)~FDIRTY;
+      if (x == 0) sides |= 1;
+      if (x == kTile - 1) sides |= 2;
+      if (y == 0) sides |= 4;
+      if (y == kTile - 1) sides |= 8;
+      if (x == 0 && y == 0) sides |= 16;
+      if (x == kTile - 1 && y == 0) sides |= 32;
+      if (x == 0 && y == kTile - 1) sides |= 64;
+      if (x == kTile - 1 && y == kTile - 1) sides |= 128;
+    }
+  }
+  sides = __reduce_or_sync(0xffffffffu, sides);
+  const int k = p + 1;
+  // Lanes 0..8 queue self (if capped) and the 8 neighbours whose halo changed.
+  if (lane < 9) {
+    int dx = 0, dy = 0;
+    bool want = false;
+    switch (lane) {
+      case 0: want = capped; break;
+      case 1: dx = -1; want = sides & 1; break;
+      case 2: dx = 1; want = sides & 2; break;
+      case 3: dy = -1; want = sides & 4; break;
+      case 4: dy = 1; want = sides & 8; break;
+      case 5: dx = -1; dy = -1; want = sides & 16; break;
+      case 6: dx = 1; dy = -1; want = sides & 32; break;
+      case 7: dx = -1; dy = 1; want = sides & 64; break;
+      case 8: dx = 1; dy = 1; want = sides & 128; break;
+    }
+    int nx = tx + dx, ny = ty + dy;
+    if (want && nx >= 0 && ny >= 0 && nx < w.tiles_x && ny < w.tiles_y)
+      enqueue(w, ny * w.tiles_x + nx, k);
+  }
+  __syncwarp();
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kWarps * 32)
+fill_flood_kernel(FloodArgs a) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  WarpSmem& s = reinterpret_cast<WarpSmem*>(smraw)[warp];
+  const FillWork& w = a.w;
+  const unsigned int nblocks = gridDim.x;
+  const int gwarp = blockIdx.x * kWarps + warp, nwarps = gridDim.x * kWarps;
+  const int ntiles = w.tiles_x * w.tiles_y;
+  const int64_t ncell = (int64_t)w.W * w.H;
+  GridSync gs{w.scal + S_BAR_COUNT, w.scal + S_BAR_GEN, (int*)(w.scal + S_ERR)};
+  volatile unsigned int* vs = w.scal;
+  const int p0 = (int)vs[S_PASS] + 2;
+  int p = p0;
+  bool full = true, cand_built = false;
+  int ph = 0;
+  while (true) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) vs[S_LIST + (p + 2) % 3] = 0u;
+    int n = full ? ntiles : (int)vs[S_LIST + p % 3];
+    const int* list = w.lists + (p & 1) * ntiles;
+    for (int i = gwarp; i < n; i += nwarps) process_tile<MODE>(s, a, full ? i : list[i], p, lane);
+    if (!grid_barrier(gs, nblocks)) break;
+    if (p - p0 > kMaxPasses) {
+      if (threadIdx.x == 0) atomicCAS((int*)(w.scal + S_ERR), 0, 2);
+      break;
+    }
+    if (vs[S_LIST + (p + 1) % 3] == 0u) {
+      if (MODE == 0) break;
+      // ---- confirmation phase ----
+      if (!cand_built) {
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ncell;
+             i += (int64_t)gridDim.x * blockDim.x) {
+          uint8_t f = w.flags[i];
+          if ((f & FNONPASS) && !(f & (FNODATA | FOUTLET | FCONF | FBELOW))) {
+            unsigned int pos = atomicAdd(&w.scal[S_CAND], 1u);
+            w.cand[pos] = (uint32_t)i;
+          }
+        }
+        cand_built = true;
+        if (!grid_barrier(gs, nblocks)) break;
+      }
+      if (blockIdx.x == 0 && threadIdx.x == 0) vs[S_M + (ph + 1) % 3] = 0xffffffffu;
+      const unsigned int nc = vs[S_CAND];
+      unsigned int local = 0xffffffffu;
+      for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < nc;
+           j += gridDim.x * blockDim.x) {
+        uint32_t c = w.cand[j];
+        uint8_t f = w.flags[c];
+        float wv = a.Wg[c];
+        if (!(f & (FCONF | FBELOW)) && wv < kInf) local = min(local, float_to_ordered(wv));
+      }
+      local = __reduce_min_sync(0xffffffffu, local);
+      if (lane == 0 && local != 0xffffffffu) atomicMin(&w.scal[S_M + ph % 3], local);
+      if (!grid_barrier(gs, nblocks)) break;
+      const unsigned int mo = vs[S_M + ph % 3];
+      if (mo == 0xffffffffu) break;
+      const float M = ordered_to_float(mo);
+      for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < nc;
+           j += gridDim.x * blockDim.x) {
+        uint32_t c = w.cand[j];
+        uint8_t f = w.flags[c];
+        if (!(f & (FCONF | FBELOW)) && a.q[c] <= M) {
+          w.flags[c] = f | FCONF;
+          if (a.Wg[c] < kInf) {
+            int cx = (int)(c % (uint32_t)w.W), cy = (int)(c / (uint32_t)w.W);
+            enqueue(w, (cy / kTile) * w.tiles_x + cx / kTile, p + 1);
+          }
+        }
+      }
+      ph++;
+      if (!grid_barrier(gs, nblocks)) break;
+    }
+    full = false;
+    p++;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    vs[S_PASS] = (unsigned int)p;
+    if (MODE == 1) vs[S_PHASES] = (unsigned int)ph;
+  }
+}
+
+__global__ void fill_init_kernel(const float* __restrict__ q, float* __restrict__ Wg,
+                                 uint8_t* __restrict__ F, const unsigned int* minslot,
+                                 int W, int H, float nodata) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)W * H) return;
+  const float minE = ordered_to_float(*minslot);
+  int x = (int)(i % W), y = (int)(i / W);
+  float qv = q[i];
+  uint8_t f = 0;
+  if (qv == nodata) {
+    f = FNODATA;
+  } else {
+    if (!fill_passable(qv, minE)) f |= FNONPASS;
+    if (x == 0 || y == 0 || x == W - 1 || y == H - 1 || qv == 0.0f) f |= FOUTLET;
+  }
+  F[i] = f;
+  Wg[i] = (f & (FNODATA | FOUTLET)) ? qv : kInf;
+}
+
+__global__ void fill_classify_kernel(float* __restrict__ Wg, uint8_t* __restrict__ F,
+                                     int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint8_t f = F[i];
+  if (f & (FNODATA | FOUTLET)) return;
+  if ((f & FNONPASS) && !(f & FBELOW) && Wg[i] < kInf) f |= FCONF;
+  F[i] = f & (uint8_t)~FBELOW;
+  Wg[i] = kInf;
+}
+
+__global__ void fill_final_kernel(const float* __restrict__ q, float* __restrict__ Wg,
+                                  int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (Wg[i] == kInf) Wg[i] = q[i];
+}
+
+__global__ void quantize_min_kernel(float* __restrict__ d, int64_t n, float nodata,
+                                    unsigned int* minslot) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float m = kInf;
+  if (i < n) {
+    float q = fill_quantize(d[i], nodata);
+    d[i] = q;
+    m = q;
+  }
+  unsigned int o = float_to_ordered(m);
+  o = __reduce_min_sync(0xffffffffu, o);
+  if ((threadIdx.x & 31) == 0) atomicMin(minslot, o);
+}
+
+__global__ void fill_scalars_kernel(unsigned int* s) {
+  int i = threadIdx.x;
+  if (i < S_SIZE) s[i] = (i == S_MIN || (i >= S_M && i < S_M + 3)) ? 0xffffffffu : 0u;
+}
+
+static int coop_blocks(const void* fn, size_t smem) {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kWarps * 32, smem);
+  return std::max(1, per) * sms;
+}
+
+template <int MODE>
+static cageo_status launch_flood(const FloodArgs& a, cudaStream_t s) {
+  const size_t smem = sizeof(WarpSmem) * kWarps;
+  auto fn = fill_flood_kernel<MODE>;
+  CAGEO_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  static int blocks[2] = {0, 0};
+  if (!blocks[MODE]) blocks[MODE] = coop_blocks((const void*)fn, smem);
+  FloodArgs args = a;
+  void* params[] = {&args};
+  CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(blocks[MODE]),
+                                         dim3(kWarps * 32), params, smem, s));
+  return CAGEO_OK;
+}
+
+cageo_status fill_reset_scalars(const FillWork& w, cudaStream_t s) {
+  fill_scalars_kernel<<<1, 32, 0, s>>>(w.scal);
+  CAGEO_CUDA(cudaGetLastError());
+  CAGEO_CUDA(cudaMemsetAsync(w.queued, 0, sizeof(int) * w.tiles_x * w.tiles_y, s));
+  return CAGEO_OK;
+}
+
+cageo_status fill_run(const float* q, float* filled, const FillWork& w, float nodata,
+                      cudaStream_t s) {
+  const int64_t n = (int64_t)w.W * w.H;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  fill_init_kernel<<<blocks, 256, 0, s>>>(q, filled, w.flags, w.scal + S_MIN, w.W, w.H, nodata);
+  CAGEO_CUDA(cudaGetLastError());
+  FloodArgs a{q, filled, w};
+  cageo_status st = launch_flood<0>(a, s);
+  if (st) return st;
+  fill_classify_kernel<<<blocks, 256, 0, s>>>(filled, w.flags, n);
+  CAGEO_CUDA(cudaGetLastError());
+  st = launch_flood<1>(a, s);
+  if (st) return st;
+  fill_final_kernel<<<blocks, 256, 0, s>>>(q, filled, n);
+  CAGEO_CUDA(cudaGetLastError());
+  return CAGEO_OK;
+}
+
+cageo_status fill_quantize_min(float* d, const FillWork& w, float nodata, cudaStream_t s) {
+  const int64_t n = (int64_t)w.W * w.H;
+  quantize_min_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, n, nodata, w.scal + S_MIN);
+  CAGEO_CUDA(cudaGetLastError());
+  return CAGEO_OK;
+}
+
+cageo_status fill_check_status(const FillWork& w, int64_t* stats) {
+  unsigned int h[S_SIZE];
+  CAGEO_CUDA(cudaMemcpy(h, w.scal, sizeof(h), cudaMemcpyDeviceToHost));
+  if (stats) {
+    stats[0] = h[S_PASS];
+    stats[1] = h[S_PHASES];
+  }
+  if (h[S_ERR]) {
+    set_error(h[S_ERR] == 1 ? "pit filling: a grid-wide wait hit its limit"
+                            : "pit filling: pass limit reached without convergence");
+    return CAGEO_ERR_NO_CONVERGENCE;
+  }
+  return CAGEO_OK;
+}
+
+}  // namespace cageo
+
+using namespace cageo;
+
+extern "C" size_t cageo_pitfill_workspace_size(int W, int H) {
+  if (!valid_dims(W, H)) return 0;
+  return fill_workspace_bytes(W, H);
+}
+
+extern "C" cageo_status cageo_pitfill(float* d_dem, float* d_filled, int W, int H,
+                                      float nodata_dem, int mode, void* d_workspace,
+                                      size_t workspace_bytes, cudaStream_t stream) {
+  CAGEO_CHECK_ARG(d_dem && d_filled && valid_dims(W, H), "pointers and size");
+  CAGEO_CHECK_ARG(W <= 65535 && H <= 65535, "width and height must be <= 65535");
+  CAGEO_CHECK_ARG(d_dem != d_filled, "the filled grid must not alias the DEM");
+  CAGEO_CHECK_ARG(mode == CAGEO_FILL_CPU_COMPAT, "fill mode");
+  Scratch ws;
+  cageo_status st = ws.acquire(d_workspace, workspace_bytes, fill_workspace_bytes(W, H), stream);
+  if (st) return st;
+  FillWork w = fill_carve(ws.ptr, W, H);
+  if ((st = fill_reset_scalars(w, stream))) return st;
+  if ((st = fill_quantize_min(d_dem, w, nodata_dem, stream))) return st;
+  if ((st = fill_run(d_dem, d_filled, w, nodata_dem, stream))) return st;
+  CAGEO_CUDA(cudaStreamSynchronize(stream));
+  return fill_check_status(w, nullptr);
+}

@@ -1,0 +1,41 @@
+// pitfill.cuh -- CPU-path-compatible pit filling on the GPU (shared with
+// pipeline.cu).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "cageo.h"
+
+namespace cageo {
+
+// Workspace of one fill: per-cell flags, per-tile worklists, counters and
+// the candidate list of the confirmation phases.
+struct FillWork {
+  int W = 0, H = 0;
+  int tiles_x = 0, tiles_y = 0;
+  uint8_t* flags = nullptr;      // W*H
+  int* queued = nullptr;         // ntiles: last pass a tile was queued for
+  int* lists = nullptr;          // 2 * ntiles: tile worklists (double buffer)
+  uint32_t* cand = nullptr;      // W*H: candidate cells of the phases
+  unsigned int* scal = nullptr;  // scalar block (see pitfill.cu)
+};
+
+size_t fill_workspace_bytes(int W, int H);
+FillWork fill_carve(void* base, int W, int H);
+
+// Fill q (already quantized, min already in scal) into `filled`.  Runs on
+// `s`; does not synchronize.  Errors found on the device are reported by
+// fill_check_status after the stream has drained.
+cageo_status fill_run(const float* q, float* filled, const FillWork& w,
+                      float nodata, cudaStream_t s);
+// Quantize d in place (the reference's step (i)) and reduce its minimum
+// into the scalar block.
+cageo_status fill_quantize_min(float* d, const FillWork& w, float nodata,
+                               cudaStream_t s);
+// Launch-time setup of the scalar block and the ordered minimum of q.
+cageo_status fill_reset_scalars(const FillWork& w, cudaStream_t s);
+unsigned int* fill_min_slot(const FillWork& w);
+// Copies the device status (0 ok) and stats into host memory; the stream
+// must have been synchronized.  stats: passes, phases.
+cageo_status fill_check_status(const FillWork& w, int64_t* stats);
+
+}  // namespace cageo

@@ -1,0 +1,41 @@
+// routing.cuh -- A7 flow routing and A8/A9 tracing and border internals,
+// shared with pipeline.cu.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "cageo.h"
+
+namespace cageo {
+
+struct RouteWork {
+  int W = 0, H = 0;
+  uint32_t* flats = nullptr;     // W*H: flat cells
+  uint32_t* front = nullptr;     // 2 * W*H: BFS frontiers
+  unsigned int* scal = nullptr;  // counters, barrier, error
+};
+size_t route_workspace_bytes(int W, int H);
+RouteWork route_carve(void* base, int W, int H);
+cageo_status route_run(const float* filled, int8_t* dir, int* flatdist,
+                       const RouteWork& w, cudaStream_t s);
+cageo_status route_check_status(const RouteWork& w, int64_t* bfs_layers);
+
+struct TraceWork {
+  int W = 0, H = 0;
+  long long* state = nullptr;    // W*H: packed pointer / label
+  unsigned int* scal = nullptr;
+};
+size_t trace_workspace_bytes(int W, int H);
+TraceWork trace_carve(void* base, int W, int H);
+// is_stream(c) = streams[c] >= 0; the label of a stream terminal is
+// (int)(-streams[c]).
+cageo_status trace_run(const int8_t* dir, const float* streams, int* label,
+                       const TraceWork& w, cudaStream_t s);
+cageo_status trace_check_status(const TraceWork& w, int64_t* jumps);
+
+// count[i] += border(label) for float (stage API) or uint32 (pipeline) counts.
+cageo_status border_float(const int* label, float* count, int W, int H,
+                          cudaStream_t s);
+cageo_status border_u32(const int* label, uint32_t* count, int W, int H,
+                        cudaStream_t s);
+
+}  // namespace cageo

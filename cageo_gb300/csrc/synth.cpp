@@ -1,0 +1,99 @@
+// synth.cpp -- host helper for the synthetic inputs used by the tests and the
+// benchmark: a stream raster derived from a DEM by priority-flood routing and
+// D8 flow accumulation.
+//
+// Not part of the drainage pipeline itself.  The reference ships no sample
+// data (its DEM/*.bin are missing), so seeded synthetic DEMs stand in for it.
+//
+// Method: priority-flood (Barnes, Lehman & Mulla 2014) from the grid border;
+// each cell drains to the cell that first reached it, which gives every cell
+// (pits and flats included) a receiver; flow accumulation then runs in
+// reverse pop order.  Cells whose accumulation exceeds `threshold` become
+// stream cells, numbered per 8-connected stream component (1, 2, ...) or all
+// 1.0; the rest get `nodata`.
+#include <cstdint>
+#include <queue>
+#include <vector>
+
+extern "C" int cageo_synth_streams(const float* dem, int W, int H,
+                                   int threshold, int per_component_ids,
+                                   float nodata, float* streams_out,
+                                   int* accum_out) {
+  if (W < 3 || H < 3) return 1;
+  const int64_t N = (int64_t)W * H;
+  struct Item {
+    float z;
+    int64_t order;
+    uint32_t i;
+  };
+  struct Cmp {
+    bool operator()(const Item& a, const Item& b) const {
+      if (a.z != b.z) return a.z > b.z;
+      return a.order > b.order;  // FIFO among equal elevations
+    }
+  };
+  std::priority_queue<Item, std::vector<Item>, Cmp> pq;
+  std::vector<uint8_t> seen(N, 0);
+  std::vector<uint32_t> recv(N, 0xffffffffu), pop_order;
+  pop_order.reserve(N);
+  int64_t order = 0;
+  for (int y = 0; y < H; y++)
+    for (int x = 0; x < W; x++)
+      if (x == 0 || y == 0 || x == W - 1 || y == H - 1) {
+        uint32_t i = (uint32_t)((int64_t)y * W + x);
+        pq.push({dem[i], order++, i});
+        seen[i] = 1;
+      }
+  static const int dx[8] = {0, 1, 1, 1, 0, -1, -1, -1};
+  static const int dy[8] = {-1, -1, 0, 1, 1, 1, 0, -1};
+  while (!pq.empty()) {
+    Item c = pq.top();
+    pq.pop();
+    pop_order.push_back(c.i);
+    int cx = (int)(c.i % (uint32_t)W), cy = (int)(c.i / (uint32_t)W);
+    for (int n = 0; n < 8; n++) {
+      int nx = cx + dx[n], ny = cy + dy[n];
+      if (nx < 0 || ny < 0 || nx >= W || ny >= H) continue;
+      uint32_t ni = (uint32_t)((int64_t)ny * W + nx);
+      if (seen[ni]) continue;
+      seen[ni] = 1;
+      recv[ni] = c.i;
+      float z = dem[ni] < c.z ? c.z : dem[ni];
+      pq.push({z, order++, ni});
+    }
+  }
+  std::vector<int> acc(N, 1);
+  for (int64_t k = N - 1; k >= 0; k--) {
+    uint32_t i = pop_order[k];
+    if (recv[i] != 0xffffffffu) acc[recv[i]] += acc[i];
+  }
+  for (int64_t i = 0; i < N; i++) streams_out[i] = acc[i] > threshold ? 1.0f : nodata;
+  if (per_component_ids) {
+    std::vector<int> comp(N, 0);
+    int next = 0;
+    std::vector<uint32_t> stack;
+    for (int64_t s = 0; s < N; s++) {
+      if (streams_out[s] == nodata || comp[s]) continue;
+      comp[s] = ++next;
+      stack.assign(1, (uint32_t)s);
+      while (!stack.empty()) {
+        uint32_t c = stack.back();
+        stack.pop_back();
+        int cx = (int)(c % (uint32_t)W), cy = (int)(c / (uint32_t)W);
+        for (int n = 0; n < 8; n++) {
+          int nx = cx + dx[n], ny = cy + dy[n];
+          if (nx < 0 || ny < 0 || nx >= W || ny >= H) continue;
+          uint32_t ni = (uint32_t)((int64_t)ny * W + nx);
+          if (streams_out[ni] == nodata || comp[ni]) continue;
+          comp[ni] = next;
+          stack.push_back(ni);
+        }
+      }
+    }
+    for (int64_t i = 0; i < N; i++)
+      if (comp[i]) streams_out[i] = (float)comp[i];
+  }
+  if (accum_out)
+    for (int64_t i = 0; i < N; i++) accum_out[i] = acc[i];
+  return 0;
+}

@@ -1,0 +1,213 @@
+// trace_border.cu -- A8 flow tracing by pointer jumping and A9 catchment
+// border extraction + Monte Carlo accumulation.
+//
+// Tracing (src/flowtracing/FlowTracingAlgorithmCPUOpenMP.h:34-134): a stream
+// cell (streams >= 0) is LAKE; every other cell follows its direction until
+// it leaves the grid (OUTSIDE) or steps onto a stream cell s (label
+// (int)(-streams[s])).  The reference walks each path serially with caching;
+// the label of a cell depends only on where its path ends, so here every
+// cell holds a packed state -- "points to cell p" or "resolved to label l"
+// -- and repeatedly jumps p <- state[p] (pointer doubling) until all are
+// resolved: O(log path length) grid passes.  A cell without a direction
+// (0,0) is a dead end: the reference's walk never terminates there, leaves
+// the path at 0 and its connect pass then copies the label of cell 0; such
+// cells and label-0 terminals take the label of cell 0 here too.  (The
+// reference also abandons walks longer than 100000 steps; paths of that
+// length do not occur in these grids and are not modelled.)
+//
+// Border (src/catchmentborder/CatchmentBorderAlgorithmCPUOpenMP.h:30-82):
+// border = 1 where the label is not LAKE and some N8 neighbour has a larger
+// label that is not LAKE; the count grid adds it
+// (src/catchmentborder/CatchmentBorderAlgorithm.h:53-74).
+#include <algorithm>
+#include "common.cuh"
+#include "routing.cuh"
+#include "stage_math.cuh"
+
+namespace cageo {
+
+constexpr long long kResolved = 1LL << 32;
+constexpr int kStuck = (int)0x80000000;  // dead end marker, never a real label
+enum : int { T_BAR_COUNT = 0, T_BAR_GEN = 1, T_ERR = 2, T_ACTIVE = 3, T_JUMPS = 6, T_SIZE = 8 };
+
+size_t trace_workspace_bytes(int W, int H) {
+  return align_up((size_t)W * H * 8, 256) + 256;
+}
+
+TraceWork trace_carve(void* base, int W, int H) {
+  TraceWork w;
+  w.W = W;
+  w.H = H;
+  w.state = (long long*)base;
+  w.scal = (unsigned int*)((char*)base + align_up((size_t)W * H * 8, 256));
+  return w;
+}
+
+__device__ inline long long resolved(int label) {
+  return kResolved | (long long)(unsigned int)label;
+}
+
+__global__ void trace_init_kernel(const char2* __restrict__ dir,
+                                  const float* __restrict__ streams,
+                                  long long* __restrict__ st, int W, int H) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)W * H) return;
+  if (streams[i] >= 0.0f) { st[i] = resolved(kLake); return; }
+  int x = (int)(i % W), y = (int)(i / W);
+  char2 d = dir[i];
+  int nx = x + d.x, ny = y + d.y;
+  if (nx < 0 || nx >= W || ny < 0 || ny >= H) { st[i] = resolved(kOutside); return; }
+  if (d.x == 0 && d.y == 0) { st[i] = resolved(kStuck); return; }
+  int64_t n = (int64_t)ny * W + nx;
+  float s = streams[n];
+  if (s >= 0.0f) { st[i] = resolved((int)(-s)); return; }
+  st[i] = n;
+}
+
+// Pointer doubling in place (reading a neighbour's newer state only speeds
+// convergence).  Persistent; one bounded grid barrier per pass.
+__global__ void trace_jump_kernel(long long* st, TraceWork w) {
+  const int64_t N = (int64_t)w.W * w.H;
+  GridSync gs{w.scal + T_BAR_COUNT, w.scal + T_BAR_GEN, (int*)(w.scal + T_ERR)};
+  volatile unsigned int* vs = w.scal;
+  int pass = 0;
+  while (true) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) vs[T_ACTIVE + (pass + 2) % 3] = 0u;
+    unsigned int active = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+         i += (int64_t)gridDim.x * blockDim.x) {
+      long long s = st[i];
+      if (s & kResolved) continue;
+      long long t = ((volatile long long*)st)[s];
+      st[i] = t;
+      if (!(t & kResolved)) active = 1;
+    }
+    active = __reduce_or_sync(0xffffffffu, active);
+    if ((threadIdx.x & 31) == 0 && active) atomicOr(&w.scal[T_ACTIVE + pass % 3], 1u);
+    if (!grid_barrier(gs, gridDim.x)) break;
+    if (vs[T_ACTIVE + pass % 3] == 0u) break;
+    if (++pass > 64) {  // 2^64 exceeds any path length: a cycle
+      if (threadIdx.x == 0) atomicCAS((int*)(w.scal + T_ERR), 0, 2);
+      break;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) vs[T_JUMPS] = (unsigned int)(pass + 1);
+}
+
+// Labels; dead ends and label-0 terminals take cell 0's label.
+__global__ void trace_final_kernel(const long long* __restrict__ st, int* __restrict__ label,
+                                   int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int l = (int)(unsigned int)st[i];
+  if (l >= 0 || l == kStuck) {
+    int l0 = (int)(unsigned int)st[0];
+    l = (l0 == kStuck || l0 >= 0) ? 0 : l0;
+  }
+  label[i] = l;
+}
+
+__global__ void trace_scalars_kernel(unsigned int* s) {
+  if (threadIdx.x < T_SIZE) s[threadIdx.x] = 0u;
+}
+
+cageo_status trace_run(const int8_t* dir, const float* streams, int* label,
+                       const TraceWork& w, cudaStream_t s) {
+  const int64_t n = (int64_t)w.W * w.H;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  trace_scalars_kernel<<<1, 32, 0, s>>>(w.scal);
+  trace_init_kernel<<<blocks, 256, 0, s>>>((const char2*)dir, streams, w.state, w.W, w.H);
+  CAGEO_CUDA(cudaGetLastError());
+  static int coop = 0;
+  if (!coop) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trace_jump_kernel, 256, 0);
+    coop = std::max(1, per) * sms;
+  }
+  long long* stp = w.state;
+  TraceWork wc = w;
+  void* params[] = {(void*)&stp, (void*)&wc};
+  CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)trace_jump_kernel, dim3(coop), dim3(256),
+                                         params, 0, s));
+  trace_final_kernel<<<blocks, 256, 0, s>>>(w.state, label, n);
+  CAGEO_CUDA(cudaGetLastError());
+  return CAGEO_OK;
+}
+
+cageo_status trace_check_status(const TraceWork& w, int64_t* jumps) {
+  unsigned int h[T_SIZE];
+  CAGEO_CUDA(cudaMemcpy(h, w.scal, sizeof(h), cudaMemcpyDeviceToHost));
+  if (jumps) *jumps = h[T_JUMPS];
+  if (h[T_ERR]) {
+    set_error("flow tracing: pointer jumping hit a wait or pass limit");
+    return CAGEO_ERR_NO_CONVERGENCE;
+  }
+  return CAGEO_OK;
+}
+
+// ---- A9 -------------------------------------------------------------------
+template <typename T>
+__global__ void border_kernel(const int* __restrict__ label, T* __restrict__ count, int W,
+                              int H) {
+  int x = blockIdx.x * blockDim.x + threadIdx.x;
+  int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= W || y >= H) return;
+  int64_t i = (int64_t)y * W + x;
+  const int c = label[i];
+  bool border = false;
+  if (c != kLake) {
+#pragma unroll
+    for (int n = 0; n < 8; n++) {
+      int nx = x + d8_dx(n), ny = y + d8_dy(n);
+      if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+      int v = label[(int64_t)ny * W + nx];
+      if (c < v && v != kLake) { border = true; break; }
+    }
+  }
+  if (border) count[i] = count[i] + (T)1;
+}
+
+template <typename T>
+static cageo_status launch_border(const int* label, T* count, int W, int H, cudaStream_t s) {
+  dim3 b(32, 8), g((W + 31) / 32, (H + 7) / 8);
+  border_kernel<T><<<g, b, 0, s>>>(label, count, W, H);
+  CAGEO_CUDA(cudaGetLastError());
+  return CAGEO_OK;
+}
+
+cageo_status border_float(const int* label, float* count, int W, int H, cudaStream_t s) {
+  return launch_border(label, count, W, H, s);
+}
+cageo_status border_u32(const int* label, uint32_t* count, int W, int H, cudaStream_t s) {
+  return launch_border(label, count, W, H, s);
+}
+
+}  // namespace cageo
+
+using namespace cageo;
+
+extern "C" size_t cageo_trace_workspace_size(int W, int H) {
+  if (!valid_dims(W, H)) return 0;
+  return trace_workspace_bytes(W, H);
+}
+
+extern "C" cageo_status cageo_trace(const int8_t* d_dir, const float* d_streams,
+                                    int* d_label, int W, int H, void* d_workspace,
+                                    size_t workspace_bytes, cudaStream_t stream) {
+  CAGEO_CHECK_ARG(d_dir && d_streams && d_label && valid_dims(W, H), "pointers and size");
+  Scratch ws;
+  cageo_status st = ws.acquire(d_workspace, workspace_bytes, trace_workspace_bytes(W, H), stream);
+  if (st) return st;
+  TraceWork w = trace_carve(ws.ptr, W, H);
+  if ((st = trace_run(d_dir, d_streams, d_label, w, stream))) return st;
+  CAGEO_CUDA(cudaStreamSynchronize(stream));
+  return trace_check_status(w, nullptr);
+}
+
+extern "C" cageo_status cageo_border_accumulate(const int* d_label, float* d_count, int W,
+                                                int H, cudaStream_t stream) {
+  CAGEO_CHECK_ARG(d_label && d_count && valid_dims(W, H), "pointers and size");
+  return border_float(d_label, d_count, W, H, stream);
+}

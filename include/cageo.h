@@ -1,0 +1,219 @@
+/* cageo.h -- C ABI of the GB300 (sm_103a) Monte Carlo drainage-basin pipeline.
+ *
+ * Drop-in for the per-realization stage algorithms of the drainage program
+ * (jsoksane/cageo).  Each stage entry point replaces one reference
+ * interface, cited beside it.  The semantics are those of the reference's
+ * CPU path (`drainage --cpu`), which these kernels reproduce bit-for-bit on
+ * the same inputs.
+ *
+ * Conventions
+ *  - Grids are row-major, index y*W + x, no padding (the reference's
+ *    CellGrid layout, src/framework/CellGrid.h:491-500).
+ *  - Every grid pointer named d_* is a caller-owned DEVICE pointer on the
+ *    current CUDA device; h_* pointers are host memory.
+ *  - Every call is asynchronous on `stream` (0 = the legacy default stream)
+ *    unless it says otherwise.  Calls return a cageo_status; on failure
+ *    cageo_last_error_string() describes the error.  Nothing calls exit().
+ *  - Flow directions are 2 signed bytes per cell (dx, dy), the reference's
+ *    char2 FlowDirDataType (src/flowrouting/FlowDirClass.h:44).
+ *  - Basin labels are int32: -(int)streams[terminal stream cell],
+ *    CAGEO_OUTSIDE or CAGEO_LAKE (src/flowtracing/FlowTracingCommon.h:18-21).
+ *  - Stages that need scratch memory take (d_workspace, workspace_bytes);
+ *    query the size with the matching *_workspace_size().  Passing NULL lets
+ *    the call allocate and free it stream-ordered (cudaMallocAsync).
+ */
+#ifndef CAGEO_H_
+#define CAGEO_H_
+
+#include <stddef.h>
+#include <stdint.h>
+#include <cuda_runtime_api.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int cageo_status;
+#define CAGEO_OK 0
+#define CAGEO_ERR_ARGUMENT 1   /* a size, pointer or option is invalid */
+#define CAGEO_ERR_CUDA 2       /* a CUDA runtime call failed */
+#define CAGEO_ERR_NO_CONVERGENCE 3 /* an iterative stage hit its iteration or wait limit */
+#define CAGEO_ERR_IO 4         /* a raster or header file could not be read or written */
+#define CAGEO_ERR_FORMAT 5     /* a header tag or value is not understood */
+
+/* Filter models, src/convolution/ConvolutionCommon.h:21-24. */
+#define CAGEO_FILTER_EXPONENTIAL 0
+#define CAGEO_FILTER_GAUSSIAN 1
+
+/* Basin label codes, src/flowtracing/FlowTracingCommon.h:18-19. */
+#define CAGEO_OUTSIDE (-9999)
+#define CAGEO_LAKE (-9998)
+
+/* Pit-filling modes.  CPU_COMPAT reproduces the reference CPU path
+ * (src/pitfilling/PitFillingAlgorithmCPUOpenMP.h:68-242). */
+#define CAGEO_FILL_CPU_COMPAT 0
+
+const char* cageo_version(void);
+/* Text of the last error raised on the calling host thread. */
+const char* cageo_last_error_string(void);
+
+/* ---- A1 random field ----------------------------------------------------
+ * Replaces RandomFieldAlgorithm<T>::execute(field, seed)
+ * (src/randomfield/RandomFieldAlgorithm.h:82-93; CPU
+ * src/randomfield/RandomFieldAlgorithmCPUOpenMP.h:47-76).
+ * d_field[i] = mean + stddev * N(0,1), where the normal deviates come from
+ * Philox4x32-10 (key = seed, counter = (cell/4, realization)) and the
+ * Box-Muller transform.  Deterministic for a given (seed, realization). */
+cageo_status cageo_noise_philox(float* d_field, int W, int H, uint64_t seed,
+                                uint32_t realization, float mean, float stddev,
+                                cudaStream_t stream);
+
+/* ---- A2 filter ----------------------------------------------------------
+ * Radius used by the driver: ceil(range/cell*2.5) (src/main.cpp:110). */
+int cageo_filter_radius(float practical_range, float cell_size);
+/* Replaces ConvolutionAlgorithm::createFilter(range, cell)
+ * (src/convolution/ConvolutionAlgorithm.cpp:18-172), host FP64:
+ * correlogram -> 2D DFT -> sqrt|F| -> inverse DFT / n^2 -> fftshift; the
+ * Gaussian model keeps the rank-1 factor u0*sqrt(s0).  h_filter receives
+ * 2r+1 taps (Gaussian) or (2r+1)^2 row-major taps (exponential).
+ * Synchronous, host only. */
+cageo_status cageo_filter_build(int model, float practical_range,
+                                float cell_size, int radius, float* h_filter);
+
+/* ---- A3 convolution -----------------------------------------------------
+ * Replaces ConvolutionAlgorithm::execute -> performConvolution
+ * (src/convolution/ConvolutionAlgorithm.h:124-140; CPU
+ * src/convolution/ConvolutionAlgorithmCPUOpenMP.h:70-248).  Periodic wrap;
+ * Gaussian = column pass then row pass; ascending tap order, unfused
+ * multiply and add, so results equal the CPU path bit-for-bit.
+ * d_filter holds the taps on the device.  d_in != d_out.  Needs r < W, r < H. */
+cageo_status cageo_convolve(const float* d_in, float* d_out, int W, int H,
+                            int model, const float* d_filter, int radius,
+                            cudaStream_t stream);
+
+/* ---- A4 realistic DEM ---------------------------------------------------
+ * Replaces RealisticDemAlgorithm::execute(dem, rand, rDem) with rDem
+ * aliasing rand (src/realisticdem/RealisticDemAlgorithm.h:49-70,
+ * src/main.cpp:200-204): d_field = dem + field where dem != nodata_dem, then
+ * values <= 0 that are not nodata_dem become 1.0.  In place on d_field. */
+cageo_status cageo_realistic_dem(const float* d_dem, float* d_field, int W,
+                                 int H, float nodata_dem, cudaStream_t stream);
+
+/* ---- A5 stream burning --------------------------------------------------
+ * Replaces StreamBurningAlgorithm::execute(rDem, streams)
+ * (src/streamburning/StreamBurningAlgorithm.h:116-134; CPU
+ * src/streamburning/StreamBurningAlgorithmCPUOpenMP.h:32-82).  In place on
+ * d_dem; bevel radius 1..5 (MAX_BEVEL_RADIUS). */
+cageo_status cageo_stream_burn(float* d_dem, const float* d_streams, int W,
+                               int H, int bevel_radius, float nodata_dem,
+                               float nodata_stream, cudaStream_t stream);
+
+/* ---- A6 pit filling -----------------------------------------------------
+ * Replaces PitFillingAlgorithm::execute(filled, rDem)
+ * (src/pitfilling/PitFillingAlgorithm.h:88-98; CPU
+ * src/pitfilling/PitFillingAlgorithmCPUOpenMP.h:68-242).  Like the
+ * reference, d_dem is quantized to 1/1000 m in place and d_filled receives
+ * the filled surface.  W, H <= 65535 (the reference's Cell coordinates). */
+size_t cageo_pitfill_workspace_size(int W, int H);
+cageo_status cageo_pitfill(float* d_dem, float* d_filled, int W, int H,
+                           float nodata_dem, int mode, void* d_workspace,
+                           size_t workspace_bytes, cudaStream_t stream);
+
+/* ---- A7 flow routing ----------------------------------------------------
+ * Replaces FlowRoutingAlgorithm::execute(flowDir, filled)
+ * (src/flowrouting/FlowRoutingAlgorithm.h:69-94; CPU
+ * src/flowrouting/FlowRoutingAlgorithmCPUOpenMP.h:53-249): D8 steepest
+ * descent, border cells point outward, flat cells by layered BFS.
+ * d_dir: 2*W*H int8 (dx,dy).  d_flatdist (optional, may be NULL): the
+ * reference's flat-distance grid (-1 has a direction, -2 stream, k >= 1
+ * flat layer, 0 unresolved). */
+size_t cageo_route_workspace_size(int W, int H);
+cageo_status cageo_route_d8(const float* d_filled, int8_t* d_dir,
+                            int* d_flatdist, int W, int H, void* d_workspace,
+                            size_t workspace_bytes, cudaStream_t stream);
+
+/* ---- A8 flow tracing ----------------------------------------------------
+ * Replaces FlowTracingAlgorithm::execute(trace, flowDir, streams)
+ * (src/flowtracing/FlowTracingAlgorithm.h:52-69; CPU
+ * src/flowtracing/FlowTracingAlgorithmCPUOpenMP.h:34-134), by pointer
+ * jumping.  d_label: W*H int32. */
+size_t cageo_trace_workspace_size(int W, int H);
+cageo_status cageo_trace(const int8_t* d_dir, const float* d_streams,
+                         int* d_label, int W, int H, void* d_workspace,
+                         size_t workspace_bytes, cudaStream_t stream);
+
+/* ---- A9 catchment border ------------------------------------------------
+ * Replaces CatchmentBorderAlgorithm::execute(mc, trace)
+ * (src/catchmentborder/CatchmentBorderAlgorithm.h:53-74; CPU
+ * src/catchmentborder/CatchmentBorderAlgorithmCPUOpenMP.h:30-82):
+ * d_count += border mask (float counts, like the reference's grid). */
+cageo_status cageo_border_accumulate(const int* d_label, float* d_count, int W,
+                                     int H, cudaStream_t stream);
+
+/* ---- Pipeline: the whole Monte Carlo loop of src/main.cpp:180-283 -------
+ * Owns its device buffers; runs realizations [first, first+count) with
+ * noise Philox(seed, realization) and accumulates the border counts
+ * internally (uint32).  The per-realization stage sequence runs as fused
+ * kernels; outputs are bit-identical to calling the stage functions above
+ * in the reference order. */
+typedef struct cageo_pipeline cageo_pipeline;
+typedef struct {
+  int width, height;
+  float cell_size;
+  int filter_model;        /* CAGEO_FILTER_* */
+  float practical_range;
+  float error_mean, error_stddev;
+  int bevel_radius;        /* reference default 2 */
+  float nodata_dem, nodata_stream;
+  uint64_t seed;
+  int use_graphs;          /* capture the per-realization launches in a CUDA graph */
+} cageo_pipeline_config;
+
+/* h_dem, h_streams: host grids (W*H floats).  The filter is built with
+ * cageo_filter_build().  Synchronous. */
+cageo_status cageo_pipeline_create(cageo_pipeline** out,
+                                   const cageo_pipeline_config* cfg,
+                                   const float* h_dem, const float* h_streams);
+/* Same, from device grids (copied). */
+cageo_status cageo_pipeline_create_device(cageo_pipeline** out,
+                                          const cageo_pipeline_config* cfg,
+                                          const float* d_dem,
+                                          const float* d_streams);
+cageo_status cageo_pipeline_run(cageo_pipeline* p, uint32_t first_realization,
+                                int count);
+/* Border counts so far as float (the reference's CatchmentBorderType). */
+cageo_status cageo_pipeline_counts(cageo_pipeline* p, float* h_out);
+cageo_status cageo_pipeline_counts_device(cageo_pipeline* p, float* d_out);
+/* Stage outputs of the most recent realization (any pointer may be NULL):
+ * filled surface (float), dir (2 int8 per cell), labels (int32).  Host. */
+cageo_status cageo_pipeline_last_stages(cageo_pipeline* p, float* h_filled,
+                                        int8_t* h_dir, int* h_label);
+cageo_status cageo_pipeline_reset_counts(cageo_pipeline* p);
+cudaStream_t cageo_pipeline_stream(cageo_pipeline* p);
+/* Counters of the last run: [0] fill passes, [1] confirmation phases,
+ * [2] flat-BFS passes, [3] trace jumps, [4] burn re-runs. */
+cageo_status cageo_pipeline_stats(cageo_pipeline* p, int64_t* h_stats, int n);
+void cageo_pipeline_destroy(cageo_pipeline* p);
+
+/* ---- A10 raster I/O -----------------------------------------------------
+ * Header: ESRI-style tags ncols nrows xllcorner yllcorner cellsize
+ * NODATA_value byteorder (src/utils/utils.cpp:58-112); an unknown tag is an
+ * error.  Rasters: raw native-endian float32 (src/utils/SystemUtils.h:53-86);
+ * the read fails unless the file holds exactly `count` floats. */
+typedef struct {
+  int ncols, nrows;
+  double xllcorner, yllcorner;
+  float cellsize;
+  float nodata_value;
+  int byteorder_msb;  /* 1 for MSBFIRST; the reference parses but ignores it */
+} cageo_raster_info;
+cageo_status cageo_read_header(const char* path, cageo_raster_info* info);
+cageo_status cageo_write_header(const char* path, const cageo_raster_info* info);
+cageo_status cageo_read_raster(const char* path, float* h_out, size_t count);
+cageo_status cageo_write_raster(const char* path, const float* h_data,
+                                size_t count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CAGEO_H_ */

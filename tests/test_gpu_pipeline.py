@@ -1,0 +1,74 @@
+"""The fused, graph-captured pipeline equals the oracle's realization loop
+(border counts bit-exact) on the same Philox noise."""
+import numpy as np
+import pytest
+
+from cases import bits, make_case
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_counts(oracle, dem, streams, seed, reals, model, rng_m, sigma, mean=0.0):
+    import torch
+    from cageo_gb300 import api
+    H, W = dem.shape
+    r = api.filter_radius(rng_m, 10.0)
+    taps = api.filter_build(model, rng_m, 10.0, r)
+    mc = np.zeros((H, W), np.float32)
+    noise = torch.empty((H, W), dtype=torch.float32, device="cuda")
+    last = None
+    for k in reals:
+        api.noise_philox(noise, seed, k, mean, sigma)
+        mc, filled, dirs, lab = oracle.realization(dem, streams, noise.cpu().numpy(), taps, r,
+                                                   model, mc)
+        last = (filled, dirs, lab)
+    return mc, last
+
+
+@pytest.mark.parametrize("W,H,model,graphs", [(128, 96, 1, True), (257, 131, 1, False),
+                                             (200, 150, 0, True), (512, 512, 1, True)])
+def test_pipeline_counts(cuda, oracle, W, H, model, graphs):
+    from cageo_gb300 import api
+    dem, streams = make_case(W, H, seed=W)
+    rng_m = 60.0 if model == 1 else 30.0
+    p = api.Pipeline(dem, streams, filter_model=model, practical_range=rng_m, error_stddev=1.5,
+                     seed=77, use_graphs=graphs)
+    p.run(0, 3)
+    p.run(3, 2)
+    got = p.counts()
+    f, d, lab = p.last_stages()
+    ref, (rf, rd, rl) = _oracle_counts(oracle, dem, streams, 77, range(5), model, rng_m, 1.5)
+    assert np.array_equal(got, ref)
+    assert np.array_equal(bits(f), bits(rf))
+    assert np.array_equal(d, rd)
+    assert np.array_equal(lab, rl)
+    p.close()
+
+
+def test_pipeline_nodata_zero_uses_stage_path(cuda, oracle):
+    from cageo_gb300 import api
+    dem, streams = make_case(96, 80, seed=5)
+    p = api.Pipeline(dem, streams, nodata_dem=0.0, error_stddev=1.0, seed=3)
+    p.run(0, 2)
+    got = p.counts()
+    import torch
+    r = api.filter_radius(60.0, 10.0)
+    taps = api.filter_build(1, 60.0, 10.0, r)
+    mc = np.zeros_like(dem)
+    noise = torch.empty(dem.shape, dtype=torch.float32, device="cuda")
+    for k in range(2):
+        api.noise_philox(noise, 3, k, 0.0, 1.0)
+        mc, *_ = oracle.realization(dem, streams, noise.cpu().numpy(), taps, r, 1, mc,
+                                    nodata_dem=0.0)
+    assert np.array_equal(got, mc)
+
+
+def test_pipeline_graph_equals_direct(cuda):
+    from cageo_gb300 import api
+    dem, streams = make_case(300, 200, seed=12)
+    a = api.Pipeline(dem, streams, seed=5, use_graphs=True)
+    b = api.Pipeline(dem, streams, seed=5, use_graphs=False)
+    a.run(0, 6)
+    b.run(0, 6)
+    assert np.array_equal(a.counts(), b.counts())
+    assert a.counts().max() <= 6
