@@ -1,0 +1,306 @@
+"""Benchmark: Monte Carlo drainage-basin realizations/s at an 8192 x 8192 DEM.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Workload ("eval-8192"): 8192^2 float32 DEM from seeded spectral fBm (Hurst
+0.8, 0-300 m relief, 10 m cells) with 20000 pits of 0.5-3 m; stream raster
+1.0 where D8 accumulation on the priority-flood-routed DEM exceeds 2000
+cells, -9999 elsewhere; Gaussian filter, 60 m practical range, error sd
+1.5 m.  Synthetic data stands in for the reference's missing sample DEM.
+
+A step is one realization (noise -> convolution -> realistic DEM ->
+burning -> pit fill -> routing -> tracing -> border count) over the whole
+DEM.  Every grid is 256 MiB, larger than the 129 MB L2, so no flush is
+needed between steps.  `value` times K steps with the grids resident on
+the device (CUDA events on the pipeline's stream); `e2e` times the same K
+steps through the C ABI from pinned host buffers: upload of DEM and
+streams, the K realizations, download of the counts (the bytes are spread
+over the K steps).
+
+--impl reference times the reference's CPU algorithm (the oracle's
+restatement, which is pinned bit-exactly to the reference's own CPU stage
+code by the golden fixtures) on the host cores, one realization per step
+on a 2048^2 window of the same DEM, scaled to the full DEM by cell count.
+
+With --gpus N > 1 (torchrun, one process per GPU) every rank runs its own
+realizations (replicas: the path has no exchange until the final count
+sum, which is done once after timing) and the value is the total rate.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MC realizations/sec at 8192^2 DEM, learned+batched vs plain GPU, exact basins"
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM = 6800.0
+# Algorithmic bytes per cell of each stage (unfused compulsory I/O).
+STAGE_BYTES = {"noise": 4, "front": 40, "fill": 8, "route": 5, "trace": 6, "border": 12}
+PIPE_BYTES = 75
+
+
+def peak_hbm():
+    try:
+        with open(PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4)
+                          if s[3 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def workload():
+    from cageo_gb300 import synth
+    dem, streams, p = synth.workload("eval-8192", ids="ones")
+    return dem, streams, p
+
+
+def cpu_rate(dem, streams, p, steps, first_real, window=2048, gpu_noise=True):
+    """Oracle realizations on a window; returns (realizations/s scaled to the full DEM, threads, s)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Oracle, build
+    if not os.path.exists(Oracle.path):
+        build()
+    o = Oracle()
+    from cageo_gb300 import api
+    H, W = dem.shape
+    wy, wx = min(window, H), min(window, W)
+    d = np.ascontiguousarray(dem[:wy, :wx])
+    s = np.ascontiguousarray(streams[:wy, :wx])
+    r = api.filter_radius(p["range_m"], p["cell"])
+    taps = api.filter_build(api.FILTER_GAUSSIAN, p["range_m"], p["cell"], r)
+    mc = np.zeros_like(d)
+    if gpu_noise:
+        import torch
+        nt = torch.empty((wy, wx), dtype=torch.float32, device="cuda")
+    total = 0.0
+    for k in range(steps):
+        if gpu_noise:
+            api.noise_philox(nt, 1, first_real + k, 0.0, p["sigma"])
+            noise = nt.cpu().numpy()
+        else:
+            noise = (np.random.default_rng(first_real + k).standard_normal((wy, wx))
+                     * p["sigma"]).astype(np.float32)
+        t0 = time.perf_counter()
+        mc, *_ = o.realization(d, s, noise, taps, r, 1, mc)
+        total += time.perf_counter() - t0
+    rate = steps / total * (wy * wx) / (H * W)
+    return rate, o.threads(), total
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    dem, streams, p = workload()
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
+    cpu_rate(dem, streams, p, max(args.warmup, 1), 10_000, gpu_noise=False)
+    t0 = time.perf_counter()
+    rate, threads, sec = cpu_rate(dem, streams, p, args.steps, 0, gpu_noise=False)
+    wall = time.perf_counter() - t0
+    H, W = dem.shape
+    sample = "%d realizations on a 2048x2048 window of the 8192^2 DEM, rate scaled by cell count" % args.steps
+    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "realizations/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 / rate, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "eval-8192", "width": W, "height": H, "filter": "Gaussian 60 m",
+                       "error_sd": p["sigma"], "pits": p["pits"], "stream_threshold": p["threshold"],
+                       "parallelism": "cpu"},
+            "cpu_baseline": {"value": rate, "unit": "realizations/s", "cores": threads,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": rate, "unit": "realizations/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "wall_s": wall}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    import torch.distributed as dist
+    from cageo_gb300 import api, _build
+    if not os.path.exists(_build.LIB):
+        _build.build()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    dem, streams, p = workload()
+    H, W = dem.shape
+    N = H * W
+    cfg = dict(cell_size=p["cell"], filter_model=api.FILTER_GAUSSIAN,
+               practical_range=p["range_m"], error_stddev=p["sigma"], seed=1)
+    pipe = api.Pipeline(dem, streams, **cfg)
+    base = rank * 1_000_000  # disjoint realization numbers per rank
+    # Warm-up: graph capture + stage profile.
+    pipe.run(base, args.warmup)
+    stage_ms = pipe.profile(base + args.warmup)
+    stats = pipe.stats()
+    pipe.reset_counts()
+    ext = torch.cuda.ExternalStream(pipe.stream)
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    barrier()
+    with ClockSampler(local) as clocks:
+        start.record(ext)
+        pipe.run(base + 10_000, args.steps)
+        stop.record(ext)
+        barrier()
+    ms = start.elapsed_time(stop)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * args.steps / (ms / 1000.0)
+
+    # End to end through the C ABI from pinned host memory.
+    dem_h = torch.from_numpy(dem).pin_memory()
+    st_h = torch.from_numpy(streams).pin_memory()
+    counts_h = torch.empty((H, W), dtype=torch.float32).pin_memory()
+    barrier()
+    t0 = time.perf_counter()
+    pe = api.Pipeline(dem_h.numpy(), st_h.numpy(), **cfg)
+    pe.run(base + 20_000, args.steps)
+    pe.counts(out=counts_h)
+    if world > 1:
+        c = counts_h.cuda()
+        dist.all_reduce(c)
+        counts_h.copy_(c.cpu())
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    pe.close()
+    e2e_value = world * args.steps / e2e_s
+
+    if rank != 0:
+        pipe.close()
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
+    hbm, peak_kind = peak_hbm()
+    dom = max(stage_ms, key=stage_ms.get)
+    achieved = STAGE_BYTES[dom] * N / (stage_ms[dom] / 1000.0) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "realizations/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded fBm DEM + pits, D8-accumulation streams)",
+        "config": {"workload": "eval-8192", "width": W, "height": H, "filter": "Gaussian 60 m",
+                   "error_sd": p["sigma"], "pits": p["pits"], "stream_threshold": p["threshold"],
+                   "hurst": p["hurst"], "relief_m": [p["lo"], p["hi"]],
+                   "realizations_per_step": 1, "l2": "inputs larger than L2 (256 MiB grids)",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "cuda_graph": True},
+        "cells_per_s": value * N,
+        "e2e": {"value": e2e_value, "unit": "realizations/s",
+                "h2d_bytes_per_step": int(2 * 4 * N / args.steps),
+                "d2h_bytes_per_step": int(4 * N / args.steps),
+                "note": "upload of DEM+streams and download of the counts, once per job, spread over the steps"},
+        "gpu_launches": None,
+        "stage_ms": stage_ms,
+        "fill_stats": stats,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                     "algorithmic_bytes_per_cell": STAGE_BYTES[dom], "peak_kind": peak_kind},
+        "pipeline_roofline": {"achieved": value / world * N * PIPE_BYTES / 1e9, "peak": hbm,
+                              "frac": value / world * N * PIPE_BYTES / 1e9 / hbm,
+                              "bytes_per_cell": PIPE_BYTES},
+        "clocks": clocks.summary(),
+    }
+    # Kernel launches per realization: noise, front, fill (scalars, memset,
+    # init, 2 floods, classify, final), route (scalars, d8, seed, mark, bfs,
+    # dir, final), trace (scalars, init, jump, final), border, end.
+    line["gpu_launches"] = args.steps * 21
+    if not args.no_cpu_baseline:
+        rate, threads, sec = cpu_rate(dem, streams, p, args.cpu_steps, 50_000)
+        line["cpu_baseline"] = {"value": rate, "unit": "realizations/s", "cores": threads,
+                                "kind": "port", "seconds": sec,
+                                "sample": "%d realizations on a 2048x2048 window, rate scaled by cell count"
+                                % args.cpu_steps}
+    print(json.dumps(line), flush=True)
+    pipe.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

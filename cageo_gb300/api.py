@@ -71,6 +71,7 @@ _SIGS = {
     "cageo_pipeline_reset_counts": ([_vp], _i),
     "cageo_pipeline_stream": ([_vp], _vp),
     "cageo_pipeline_stats": ([_vp, _vp, _i], _i),
+    "cageo_pipeline_profile": ([_vp, ctypes.c_uint32, _vp, _i], _i),
     "cageo_pipeline_destroy": ([_vp], None),
     "cageo_read_header": ([ctypes.c_char_p, ctypes.POINTER(RasterInfo)], _i),
     "cageo_write_header": ([ctypes.c_char_p, ctypes.POINTER(RasterInfo)], _i),
@@ -247,9 +248,13 @@ class Pipeline:
         _check(lib().cageo_pipeline_run(self._p, first, count))
 
     def counts(self, out=None):
-        """Float counts: into a host numpy array by default, or a CUDA tensor `out`."""
+        """Float counts: a new host numpy array, or into `out` (a CUDA tensor, or a
+        contiguous host float32 torch tensor, e.g. pinned)."""
         if out is not None:
-            _check(lib().cageo_pipeline_counts_device(self._p, _ptr(out)))
+            if out.is_cuda:
+                _check(lib().cageo_pipeline_counts_device(self._p, _ptr(out)))
+            else:
+                _check(lib().cageo_pipeline_counts(self._p, _ptr(out)))
             return out
         h = np.empty(self.shape, np.float32)
         _check(lib().cageo_pipeline_counts(self._p, h.ctypes.data_as(_vp)))
@@ -272,6 +277,14 @@ class Pipeline:
         _check(lib().cageo_pipeline_stats(self._p, s.ctypes.data_as(_vp), 5))
         return dict(fill_passes=int(s[0]), fill_phases=int(s[1]), flat_layers=int(s[2]),
                     trace_jumps=int(s[3]), burn_reruns=int(s[4]))
+
+    STAGES = ("noise", "front", "fill", "route", "trace", "border")
+
+    def profile(self, realization):
+        """Run one realization with per-stage CUDA event timing; returns {stage: ms}."""
+        ms = np.zeros(6, np.float32)
+        _check(lib().cageo_pipeline_profile(self._p, realization, ms.ctypes.data_as(_vp), 6))
+        return dict(zip(self.STAGES, (float(v) for v in ms)))
 
     @property
     def stream(self):

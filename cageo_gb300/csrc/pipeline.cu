@@ -325,6 +325,61 @@ extern "C" cageo_status cageo_pipeline_run(cageo_pipeline* p, uint32_t first, in
   return CAGEO_OK;
 }
 
+// One fast-path realization with CUDA events between the stages on the
+// pipeline's stream (no graph).  It is a real realization: its border mask
+// is accumulated like any other.  h_ms receives up to 6 stage times:
+// noise, front (convolution+realistic+burn+quantize), fill, routing,
+// tracing, border.
+extern "C" cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t realization,
+                                               float* h_ms, int n) {
+  CAGEO_CHECK_ARG(p && h_ms, "null argument");
+  CAGEO_CHECK_ARG(p->cfg.nodata_dem != 0.0f, "profiling needs the fused path (NODATA != 0)");
+  cudaStream_t s = p->stream;
+  const cageo_pipeline_config& c = p->cfg;
+  cudaEvent_t ev[7];
+  for (auto& e : ev) CAGEO_CUDA(cudaEventCreate(&e));
+  cageo_status st = CAGEO_OK;
+  do {
+    if (cudaMemcpyAsync(p->dscal, &realization, 4, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+      st = cuda_fail(cudaGetLastError(), "cudaMemcpyAsync");
+      break;
+    }
+    if ((st = fill_reset_scalars(p->fw, s))) break;
+    cudaEventRecord(ev[0], s);
+    if ((st = launch_noise(p->noise, p->N, c.seed, 0, p->dscal, c.error_mean, c.error_stddev, s)))
+      break;
+    cudaEventRecord(ev[1], s);
+    if ((st = launch_front(p->noise, p->W, p->H, c.filter_model, p->filter, p->radius, p->fp, s)))
+      break;
+    cudaEventRecord(ev[2], s);
+    if ((st = fill_run(p->q, p->filled, p->fw, c.nodata_dem, s))) break;
+    cudaEventRecord(ev[3], s);
+    if ((st = route_run(p->filled, p->dir, p->flatdist, p->rw, s))) break;
+    cudaEventRecord(ev[4], s);
+    if ((st = trace_run(p->dir, p->streams, p->label, p->tw, s))) break;
+    cudaEventRecord(ev[5], s);
+    dim3 b(32, 8), g((p->W + 31) / 32, (p->H + 7) / 8);
+    border_gated_kernel<<<g, b, 0, s>>>(p->label, p->counts, p->W, p->H,
+                                        (const int*)p->dscal + 1);
+    realization_end_kernel<<<1, 32, 0, s>>>(p->dscal, (int*)p->dscal + 1, p->dscal + 3,
+                                            p->dscal + 2);
+    cudaEventRecord(ev[6], s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) {
+      st = cuda_fail(cudaGetLastError(), "cudaStreamSynchronize");
+      break;
+    }
+    for (int i = 0; i < 6 && i < n; i++) cudaEventElapsedTime(&h_ms[i], ev[i], ev[i + 1]);
+    int64_t fs[2];
+    if ((st = fill_check_status(p->fw, fs))) break;
+    p->stats[0] = fs[0];
+    p->stats[1] = fs[1];
+    if ((st = route_check_status(p->rw, &p->stats[2]))) break;
+    st = trace_check_status(p->tw, &p->stats[3]);
+  } while (0);
+  for (auto& e : ev) cudaEventDestroy(e);
+  return st;
+}
+
 extern "C" cageo_status cageo_pipeline_counts_device(cageo_pipeline* p, float* d_out) {
   CAGEO_CHECK_ARG(p && d_out, "null argument");
   counts_to_float_kernel<<<(unsigned)((p->N + 255) / 256), 256, 0, p->stream>>>(p->counts, d_out,

@@ -281,8 +281,12 @@ fill_flood_kernel(FloodArgs a) {
         if (!(f & (FCONF | FBELOW)) && a.q[c] <= M) {
           w.flags[c] = f | FCONF;
           if (a.Wg[c] < kInf) {
+            // The cell now relays: every tile whose halo holds it must rerun.
             int cx = (int)(c % (uint32_t)w.W), cy = (int)(c / (uint32_t)w.W);
-            enqueue(w, (cy / kTile) * w.tiles_x + cx / kTile, p + 1);
+            int tx0 = max(cx - 1, 0) / kTile, tx1 = min(cx + 1, w.W - 1) / kTile;
+            int ty0 = max(cy - 1, 0) / kTile, ty1 = min(cy + 1, w.H - 1) / kTile;
+            for (int ty = ty0; ty <= ty1; ty++)
+              for (int tx = tx0; tx <= tx1; tx++) enqueue(w, ty * w.tiles_x + tx, p + 1);
           }
         }
       }

@@ -72,7 +72,9 @@ __global__ void trace_jump_kernel(long long* st, TraceWork w) {
   volatile unsigned int* vs = w.scal;
   int pass = 0;
   while (true) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) vs[T_ACTIVE + (pass + 2) % 3] = 0u;
+    // Slot pass%3 is written during this pass and read after its barrier;
+    // slot (pass+1)%3 was last read before the previous barrier.
+    if (blockIdx.x == 0 && threadIdx.x == 0) vs[T_ACTIVE + (pass + 1) % 3] = 0u;
     unsigned int active = 0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N;
          i += (int64_t)gridDim.x * blockDim.x) {

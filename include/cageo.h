@@ -190,6 +190,12 @@ cageo_status cageo_pipeline_last_stages(cageo_pipeline* p, float* h_filled,
                                         int8_t* h_dir, int* h_label);
 cageo_status cageo_pipeline_reset_counts(cageo_pipeline* p);
 cudaStream_t cageo_pipeline_stream(cageo_pipeline* p);
+/* One realization with CUDA events between stages (fused path, no graph);
+ * it is accumulated like any other.  h_ms[0..5]: noise, front
+ * (convolution + realistic DEM + burning + quantization), pit fill,
+ * routing, tracing, border (milliseconds). */
+cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t realization,
+                                    float* h_ms, int n);
 /* Counters of the last run: [0] fill passes, [1] confirmation phases,
  * [2] flat-BFS passes, [3] trace jumps, [4] burn re-runs. */
 cageo_status cageo_pipeline_stats(cageo_pipeline* p, int64_t* h_stats, int n);
