@@ -56,6 +56,8 @@ _SIGS = {
     "cageo_stream_burn": ([_vp, _vp, _i, _i, _i, _f, _f, _vp], _i),
     "cageo_pitfill_workspace_size": ([_i, _i], _sz),
     "cageo_pitfill": ([_vp, _vp, _i, _i, _f, _i, _vp, _sz, _vp], _i),
+    "cageo_pitfill_static_max_bytes": ([], _sz),
+    "cageo_pitfill_static": ([_vp, _vp, _i, _i, _f, _i, _vp], _i),
     "cageo_route_workspace_size": ([_i, _i], _sz),
     "cageo_route_d8": ([_vp, _vp, _vp, _i, _i, _vp, _sz, _vp], _i),
     "cageo_trace_workspace_size": ([_i, _i], _sz),

@@ -119,6 +119,23 @@ cageo_status cageo_pitfill(float* d_dem, float* d_filled, int W, int H,
                            float nodata_dem, int mode, void* d_workspace,
                            size_t workspace_bytes, cudaStream_t stream);
 
+/* Pit filling that allocates no device memory.  No counterpart in the
+ * reference: it exists for callers that cannot allocate -- e.g. a host
+ * application that has reserved the GPU's memory for its own allocator and
+ * forbids plug-ins from calling cudaMalloc, or a loop that must not pay an
+ * allocation's latency or implicit synchronization.  Same semantics and
+ * result as cageo_pitfill; its scratch is a fixed array inside the library
+ * (cageo_pitfill_static_max_bytes(), 24 MiB, held on every GPU that loads
+ * the library until the process exits), enough for grids up to 2048 x 2048
+ * cells; larger grids are refused with CAGEO_ERR_ARGUMENT.  The first call
+ * on a device looks up the array's device address (make that first call
+ * before any stream capture).  All calls share the array: each call clears
+ * what must start at zero, and calls that overlap on the GPU race, so the
+ * caller must serialize them.  Synchronizes `stream` before returning. */
+size_t cageo_pitfill_static_max_bytes(void);
+cageo_status cageo_pitfill_static(float* d_dem, float* d_filled, int W, int H,
+                                  float nodata_dem, int mode, cudaStream_t stream);
+
 /* ---- A7 flow routing ----------------------------------------------------
  * Replaces FlowRoutingAlgorithm::execute(flowDir, filled)
  * (src/flowrouting/FlowRoutingAlgorithm.h:69-94; CPU
