@@ -105,9 +105,9 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
-def workload():
+def workload(name="eval-8192"):
     from cageo_gb300 import synth
-    dem, streams, p = synth.workload("eval-8192", ids="ones")
+    dem, streams, p = synth.workload(name, ids="ones")
     return dem, streams, p
 
 
@@ -147,7 +147,7 @@ def cpu_rate(dem, streams, p, steps, first_real, window=2048, gpu_noise=True):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    dem, streams, p = workload()
+    dem, streams, p = workload(args.workload)
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count()))
     cpu_rate(dem, streams, p, max(args.warmup, 1), 10_000, gpu_noise=False)
     t0 = time.perf_counter()
@@ -159,7 +159,7 @@ def run_reference(args, rank, world):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 / rate, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "eval-8192", "width": W, "height": H, "filter": "Gaussian 60 m",
+            "config": {"workload": args.workload, "width": W, "height": H, "filter": "Gaussian 60 m",
                        "error_sd": p["sigma"], "pits": p["pits"], "stream_threshold": p["threshold"],
                        "parallelism": "cpu"},
             "cpu_baseline": {"value": rate, "unit": "realizations/s", "cores": threads,
@@ -178,6 +178,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="eval-8192",
+                    help="eval-8192 (the benchmark) or a smaller case for profiling (plain-4096)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -195,7 +197,7 @@ def main():
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    dem, streams, p = workload()
+    dem, streams, p = workload(args.workload)
     H, W = dem.shape
     N = H * W
     cfg = dict(cell_size=p["cell"], filter_model=api.FILTER_GAUSSIAN,
@@ -264,7 +266,7 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded fBm DEM + pits, D8-accumulation streams)",
-        "config": {"workload": "eval-8192", "width": W, "height": H, "filter": "Gaussian 60 m",
+        "config": {"workload": args.workload, "width": W, "height": H, "filter": "Gaussian 60 m",
                    "error_sd": p["sigma"], "pits": p["pits"], "stream_threshold": p["threshold"],
                    "hurst": p["hurst"], "relief_m": [p["lo"], p["hi"]],
                    "realizations_per_step": 1, "l2": "inputs larger than L2 (256 MiB grids)",

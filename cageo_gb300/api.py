@@ -275,10 +275,11 @@ class Pipeline:
         _check(lib().cageo_pipeline_reset_counts(self._p))
 
     def stats(self):
-        s = np.zeros(5, np.int64)
-        _check(lib().cageo_pipeline_stats(self._p, s.ctypes.data_as(_vp), 5))
-        return dict(fill_passes=int(s[0]), fill_phases=int(s[1]), flat_layers=int(s[2]),
-                    trace_jumps=int(s[3]), burn_reruns=int(s[4]))
+        s = np.zeros(10, np.int64)
+        _check(lib().cageo_pipeline_stats(self._p, s.ctypes.data_as(_vp), 10))
+        keys = ("fill_passes", "fill_phases", "flat_layers", "trace_jumps", "burn_reruns",
+                "flood_a_passes", "flood_b_passes", "flood_a_us", "flood_b_us", "phases_us")
+        return {k: int(v) for k, v in zip(keys, s)}
 
     STAGES = ("noise", "front", "fill", "route", "trace", "border")
 

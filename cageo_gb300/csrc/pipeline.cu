@@ -102,7 +102,7 @@ struct cageo_pipeline {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool graph_ok = false;
-  int64_t stats[5] = {0, 0, 0, 0, 0};
+  int64_t stats[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -298,7 +298,7 @@ extern "C" cageo_status cageo_pipeline_run(cageo_pipeline* p, uint32_t first, in
     }
   }
   CAGEO_CUDA(cudaStreamSynchronize(s));
-  int64_t fs[2] = {0, 0}, layers = 0, jumps = 0;
+  int64_t fs[7] = {0, 0, 0, 0, 0, 0, 0}, layers = 0, jumps = 0;
   if ((st = fill_check_status(p->fw, fs))) return st;
   if ((st = route_check_status(p->rw, &layers))) return st;
   if ((st = trace_check_status(p->tw, &jumps))) return st;
@@ -322,6 +322,7 @@ extern "C" cageo_status cageo_pipeline_run(cageo_pipeline* p, uint32_t first, in
   p->stats[2] = layers;
   p->stats[3] = jumps;
   p->stats[4] = nredo;
+  for (int k = 0; k < 5; k++) p->stats[5 + k] = fs[2 + k];
   return CAGEO_OK;
 }
 
@@ -369,10 +370,11 @@ extern "C" cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t reali
       break;
     }
     for (int i = 0; i < 6 && i < n; i++) cudaEventElapsedTime(&h_ms[i], ev[i], ev[i + 1]);
-    int64_t fs[2];
+    int64_t fs[7];
     if ((st = fill_check_status(p->fw, fs))) break;
     p->stats[0] = fs[0];
     p->stats[1] = fs[1];
+    for (int k = 0; k < 5; k++) p->stats[5 + k] = fs[2 + k];
     if ((st = route_check_status(p->rw, &p->stats[2]))) break;
     st = trace_check_status(p->tw, &p->stats[3]);
   } while (0);
@@ -423,7 +425,7 @@ extern "C" cudaStream_t cageo_pipeline_stream(cageo_pipeline* p) { return p ? p-
 
 extern "C" cageo_status cageo_pipeline_stats(cageo_pipeline* p, int64_t* h_stats, int n) {
   CAGEO_CHECK_ARG(p && h_stats, "null argument");
-  for (int i = 0; i < n && i < 5; i++) h_stats[i] = p->stats[i];
+  for (int i = 0; i < n && i < 10; i++) h_stats[i] = p->stats[i];
   return CAGEO_OK;
 }
 

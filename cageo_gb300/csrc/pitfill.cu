@@ -49,8 +49,19 @@ enum : int {
   S_CAND = 10,     // candidate count
   S_PASS = 11,     // last pass number
   S_PHASES = 12,
-  S_SIZE = 16
+  S_PASSES_A = 13, // passes of flood A
+  S_PASSES_B = 14, // passes of flood B before the first phase
+  S_US_A = 15,     // microseconds of flood A
+  S_US_B = 16,     // microseconds of flood B up to its first convergence
+  S_US_P = 17,     // microseconds of the phase loop
+  S_SIZE = 32
 };
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 constexpr int kTile = 32;
 constexpr int kWarps = 4;
@@ -233,6 +244,8 @@ fill_flood_kernel(FloodArgs a) {
   int p = p0;
   bool full = true, cand_built = false;
   int ph = 0;
+  const unsigned long long t_start = global_ns();
+  unsigned long long t_conv = 0;
   while (true) {
     if (blockIdx.x == 0 && threadIdx.x == 0) vs[S_LIST + (p + 2) % 3] = 0u;
     int n = full ? ntiles : (int)vs[S_LIST + p % 3];
@@ -247,6 +260,8 @@ fill_flood_kernel(FloodArgs a) {
       if (MODE == 0) break;
       // ---- confirmation phase ----
       if (!cand_built) {
+        t_conv = global_ns();
+        if (blockIdx.x == 0 && threadIdx.x == 0) vs[S_PASSES_B] = (unsigned int)(p - p0 + 1);
         for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ncell;
              i += (int64_t)gridDim.x * blockDim.x) {
           uint8_t f = w.flags[i];
@@ -298,7 +313,16 @@ fill_flood_kernel(FloodArgs a) {
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     vs[S_PASS] = (unsigned int)p;
-    if (MODE == 1) vs[S_PHASES] = (unsigned int)ph;
+    const unsigned long long t_end = global_ns();
+    if (MODE == 0) {
+      vs[S_PASSES_A] = (unsigned int)(p - p0 + 1);
+      vs[S_US_A] = (unsigned int)((t_end - t_start) / 1000);
+    } else {
+      vs[S_PHASES] = (unsigned int)ph;
+      if (!t_conv) t_conv = t_end;
+      vs[S_US_B] = (unsigned int)((t_conv - t_start) / 1000);
+      vs[S_US_P] = (unsigned int)((t_end - t_conv) / 1000);
+    }
   }
 }
 
@@ -418,6 +442,11 @@ cageo_status fill_check_status(const FillWork& w, int64_t* stats) {
   if (stats) {
     stats[0] = h[S_PASS];
     stats[1] = h[S_PHASES];
+    stats[2] = h[S_PASSES_A];
+    stats[3] = h[S_PASSES_B];
+    stats[4] = h[S_US_A];
+    stats[5] = h[S_US_B];
+    stats[6] = h[S_US_P];
   }
   if (h[S_ERR]) {
     set_error(h[S_ERR] == 1 ? "pit filling: a grid-wide wait hit its limit"

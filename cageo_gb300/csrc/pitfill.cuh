@@ -35,7 +35,9 @@ cageo_status fill_quantize_min(float* d, const FillWork& w, float nodata,
 cageo_status fill_reset_scalars(const FillWork& w, cudaStream_t s);
 unsigned int* fill_min_slot(const FillWork& w);
 // Copies the device status (0 ok) and stats into host memory; the stream
-// must have been synchronized.  stats: passes, phases.
+// must have been synchronized.  stats (7 entries): last pass number,
+// phases, passes of flood A, passes of flood B before the first phase,
+// microseconds of flood A, of flood B to convergence, of the phase loop.
 cageo_status fill_check_status(const FillWork& w, int64_t* stats);
 
 }  // namespace cageo

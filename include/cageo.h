@@ -214,7 +214,10 @@ cudaStream_t cageo_pipeline_stream(cageo_pipeline* p);
 cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t realization,
                                     float* h_ms, int n);
 /* Counters of the last run: [0] fill passes, [1] confirmation phases,
- * [2] flat-BFS passes, [3] trace jumps, [4] burn re-runs. */
+ * [2] flat-BFS layers, [3] trace jumps, [4] burn re-runs, [5] passes of
+ * the lower-bound flood, [6] passes of the walled flood before the first
+ * phase, [7..9] microseconds of the lower-bound flood, of the walled flood
+ * to convergence and of the phase loop (last realization). */
 cageo_status cageo_pipeline_stats(cageo_pipeline* p, int64_t* h_stats, int n);
 void cageo_pipeline_destroy(cageo_pipeline* p);
 
