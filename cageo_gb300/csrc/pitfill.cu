@@ -36,7 +36,7 @@ namespace cageo {
 
 // Per-cell flag bits.
 constexpr uint8_t FNODATA = 0x01, FOUTLET = 0x02, FNONPASS = 0x04, FCONF = 0x08,
-                  FBELOW = 0x10, FDIRTY = 0x40;
+                  FBELOW = 0x10, FBELOWA = 0x20, FDIRTY = 0x40, FUNSURE = 0x80;
 
 // Scalar block layout (unsigned ints).
 enum : int {
@@ -46,7 +46,7 @@ enum : int {
   S_ERR = 3,       // 0 ok, 1 barrier wait limit, 2 pass limit
   S_LIST = 4,      // 3 slots: worklist counts
   S_M = 7,         // 3 slots: ordered phase minima
-  S_CAND = 10,     // candidate count
+  S_CAND = 10,     // number of undecided cells
   S_PASS = 11,     // last pass number
   S_PHASES = 12,
   S_PASSES_A = 13, // passes of flood A
@@ -54,6 +54,7 @@ enum : int {
   S_US_A = 15,     // microseconds of flood A
   S_US_B = 16,     // microseconds of flood B up to its first convergence
   S_US_P = 17,     // microseconds of the phase loop
+  S_PEND = 18,     // 3 slots: pending cells seen by a phase
   S_SIZE = 32
 };
 
@@ -82,7 +83,7 @@ size_t fill_workspace_bytes(int W, int H) {
   size_t n = (size_t)W * H;
   size_t nt = (size_t)((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile);
   return align_up(n, 256) + align_up(nt * 4, 256) + align_up(2 * nt * 4, 256) +
-         align_up(n * 4, 256) + 256;
+         3 * align_up(n * 4, 256) + 256;
 }
 
 FillWork fill_carve(void* base, int W, int H) {
@@ -100,6 +101,10 @@ FillWork fill_carve(void* base, int W, int H) {
   w.lists = (int*)p;
   p += align_up(2 * nt * 4, 256);
   w.cand = (uint32_t*)p;
+  p += align_up(n * 4, 256);
+  w.aux = (uint32_t*)p;
+  p += align_up(n * 4, 256);
+  w.cmin = (uint32_t*)p;
   p += align_up(n * 4, 256);
   w.scal = (unsigned int*)p;
   return w;
@@ -227,6 +232,30 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
   __syncwarp();
 }
 
+// Lock-free union-find over the undecided cells (labels in w.aux): links
+// always point to a smaller cell index, so no cycle can form; roots are
+// hooked with CAS, paths halved with plain stores.  Bounded loops.
+__device__ __forceinline__ uint32_t uf_find(uint32_t* lab, uint32_t x) {
+  for (int it = 0; it < (1 << 20); it++) {
+    uint32_t p = ((volatile uint32_t*)lab)[x];
+    if (p == x) return x;
+    uint32_t g = ((volatile uint32_t*)lab)[p];
+    if (g != p) lab[x] = g;
+    x = p;
+  }
+  return x;
+}
+
+__device__ __forceinline__ bool uf_unite(uint32_t* lab, uint32_t a, uint32_t b) {
+  for (int it = 0; it < (1 << 16); it++) {
+    uint32_t ra = uf_find(lab, a), rb = uf_find(lab, b);
+    if (ra == rb) return true;
+    if (ra > rb) { uint32_t t = ra; ra = rb; rb = t; }
+    if (atomicCAS(&lab[rb], rb, ra) == rb) return true;
+  }
+  return false;
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(kWarps * 32)
 fill_flood_kernel(FloodArgs a) {
@@ -258,51 +287,88 @@ fill_flood_kernel(FloodArgs a) {
     }
     if (vs[S_LIST + (p + 1) % 3] == 0u) {
       if (MODE == 0) break;
-      // ---- confirmation phase ----
+      // ---- confirmation phases ----
+      // Flood A gave a lower bound (W_A in aux, FBELOWA), flood B an upper
+      // bound (Wg, FBELOW).  Where they agree the cell is final; the
+      // undecided cells form 8-connected components that no later change
+      // can leave, so each component takes its own phase minimum.
+      const int64_t tid0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+      const int64_t tstride = (int64_t)gridDim.x * blockDim.x;
       if (!cand_built) {
         t_conv = global_ns();
         if (blockIdx.x == 0 && threadIdx.x == 0) vs[S_PASSES_B] = (unsigned int)(p - p0 + 1);
-        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ncell;
-             i += (int64_t)gridDim.x * blockDim.x) {
+        for (int64_t i = tid0; i < ncell; i += tstride) {
           uint8_t f = w.flags[i];
-          if ((f & FNONPASS) && !(f & (FNODATA | FOUTLET | FCONF | FBELOW))) {
+          if (f & (FNODATA | FOUTLET)) continue;
+          const float wa = __uint_as_float(w.aux[i]);
+          const bool unsure = wa != a.Wg[i] ||
+                              ((f & FNONPASS) && (((f & FBELOWA) != 0) != ((f & FBELOW) != 0)));
+          if (unsure) {
             unsigned int pos = atomicAdd(&w.scal[S_CAND], 1u);
             w.cand[pos] = (uint32_t)i;
+            w.flags[i] = f | FUNSURE;
+            w.aux[i] = (uint32_t)i;
           }
+        }
+        if (!grid_barrier(gs, nblocks)) break;
+        const unsigned int nu = vs[S_CAND];
+        bool ok = true;
+        for (int64_t j = tid0; j < nu; j += tstride) {
+          uint32_t c = w.cand[j];
+          int cx = (int)(c % (uint32_t)w.W), cy = (int)(c / (uint32_t)w.W);
+          for (int k = 0; k < 4; k++) {  // W, NW, N, NE: each pair once
+            int nx = cx + (k == 0 ? -1 : k - 2), ny = cy + (k == 0 ? 0 : -1);
+            if (nx < 0 || ny < 0 || nx >= w.W) continue;
+            uint32_t n = (uint32_t)ny * (uint32_t)w.W + (uint32_t)nx;
+            if (w.flags[n] & FUNSURE) ok &= uf_unite(w.aux, c, n);
+          }
+        }
+        if (!ok) atomicCAS((int*)(w.scal + S_ERR), 0, 2);
+        if (!grid_barrier(gs, nblocks)) break;
+        for (int64_t j = tid0; j < nu; j += tstride) {
+          uint32_t c = w.cand[j];
+          w.aux[c] = uf_find(w.aux, c);
         }
         cand_built = true;
         if (!grid_barrier(gs, nblocks)) break;
       }
-      if (blockIdx.x == 0 && threadIdx.x == 0) vs[S_M + (ph + 1) % 3] = 0xffffffffu;
-      const unsigned int nc = vs[S_CAND];
-      unsigned int local = 0xffffffffu;
-      for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < nc;
-           j += gridDim.x * blockDim.x) {
+      const unsigned int nu = vs[S_CAND];
+      if (blockIdx.x == 0 && threadIdx.x == 0) vs[S_PEND + (ph + 1) % 3] = 0u;
+      for (int64_t j = tid0; j < nu; j += tstride) {
         uint32_t c = w.cand[j];
-        uint8_t f = w.flags[c];
-        float wv = a.Wg[c];
-        if (!(f & (FCONF | FBELOW)) && wv < kInf) local = min(local, float_to_ordered(wv));
+        if (w.aux[c] == c) w.cmin[c] = 0xffffffffu;
       }
-      local = __reduce_min_sync(0xffffffffu, local);
-      if (lane == 0 && local != 0xffffffffu) atomicMin(&w.scal[S_M + ph % 3], local);
       if (!grid_barrier(gs, nblocks)) break;
-      const unsigned int mo = vs[S_M + ph % 3];
-      if (mo == 0xffffffffu) break;
-      const float M = ordered_to_float(mo);
-      for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < nc;
-           j += gridDim.x * blockDim.x) {
+      unsigned int pend = 0;
+      for (int64_t j = tid0; j < nu; j += tstride) {
         uint32_t c = w.cand[j];
         uint8_t f = w.flags[c];
-        if (!(f & (FCONF | FBELOW)) && a.q[c] <= M) {
-          w.flags[c] = f | FCONF;
-          if (a.Wg[c] < kInf) {
-            // The cell now relays: every tile whose halo holds it must rerun.
-            int cx = (int)(c % (uint32_t)w.W), cy = (int)(c / (uint32_t)w.W);
-            int tx0 = max(cx - 1, 0) / kTile, tx1 = min(cx + 1, w.W - 1) / kTile;
-            int ty0 = max(cy - 1, 0) / kTile, ty1 = min(cy + 1, w.H - 1) / kTile;
-            for (int ty = ty0; ty <= ty1; ty++)
-              for (int tx = tx0; tx <= tx1; tx++) enqueue(w, ty * w.tiles_x + tx, p + 1);
+        if ((f & FNONPASS) && !(f & (FCONF | FBELOW))) {
+          float wv = a.Wg[c];
+          if (wv < kInf) {
+            atomicMin(&w.cmin[w.aux[c]], float_to_ordered(wv));
+            pend = 1;
           }
+        }
+      }
+      pend = __reduce_or_sync(0xffffffffu, pend);
+      if (lane == 0 && pend) atomicOr(&w.scal[S_PEND + ph % 3], 1u);
+      if (!grid_barrier(gs, nblocks)) break;
+      if (vs[S_PEND + ph % 3] == 0u) break;
+      for (int64_t j = tid0; j < nu; j += tstride) {
+        uint32_t c = w.cand[j];
+        uint8_t f = w.flags[c];
+        if (!(f & FNONPASS) || (f & (FCONF | FBELOW))) continue;
+        const unsigned int mo = w.cmin[w.aux[c]];
+        if (mo == 0xffffffffu || !(a.q[c] <= ordered_to_float(mo))) continue;
+        w.flags[c] = f | FCONF;
+        if (a.Wg[c] < kInf) {
+          // The cell now relays: every tile whose halo holds it must rerun.
+          int cx = (int)(c % (uint32_t)w.W), cy = (int)(c / (uint32_t)w.W);
+          int tx0 = max(cx - 1, 0) / kTile, tx1 = min(cx + 1, w.W - 1) / kTile;
+          int ty0 = max(cy - 1, 0) / kTile, ty1 = min(cy + 1, w.H - 1) / kTile;
+          for (int ty = ty0; ty <= ty1; ty++)
+            for (int tx = tx0; tx <= tx1; tx++) enqueue(w, ty * w.tiles_x + tx, p + 1);
         }
       }
       ph++;
@@ -345,13 +411,18 @@ __global__ void fill_init_kernel(const float* __restrict__ q, float* __restrict_
   Wg[i] = (f & (FNODATA | FOUTLET)) ? qv : kInf;
 }
 
+// Between the floods: keep flood A's result (lower bound) in aux and
+// FBELOWA, confirm non-passable cells reached at a level >= q, reset W.
 __global__ void fill_classify_kernel(float* __restrict__ Wg, uint8_t* __restrict__ F,
-                                     int64_t n) {
+                                     uint32_t* __restrict__ aux, int64_t n) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   uint8_t f = F[i];
+  const float wa = Wg[i];
+  aux[i] = __float_as_uint(wa);
   if (f & (FNODATA | FOUTLET)) return;
-  if ((f & FNONPASS) && !(f & FBELOW) && Wg[i] < kInf) f |= FCONF;
+  if ((f & FNONPASS) && !(f & FBELOW) && wa < kInf) f |= FCONF;
+  if (f & FBELOW) f |= FBELOWA;
   F[i] = f & (uint8_t)~FBELOW;
   Wg[i] = kInf;
 }
@@ -420,7 +491,7 @@ cageo_status fill_run(const float* q, float* filled, const FillWork& w, float no
   FloodArgs a{q, filled, w};
   cageo_status st = launch_flood<0>(a, s);
   if (st) return st;
-  fill_classify_kernel<<<blocks, 256, 0, s>>>(filled, w.flags, n);
+  fill_classify_kernel<<<blocks, 256, 0, s>>>(filled, w.flags, w.aux, n);
   CAGEO_CUDA(cudaGetLastError());
   st = launch_flood<1>(a, s);
   if (st) return st;

@@ -15,7 +15,9 @@ struct FillWork {
   uint8_t* flags = nullptr;      // W*H
   int* queued = nullptr;         // ntiles: last pass a tile was queued for
   int* lists = nullptr;          // 2 * ntiles: tile worklists (double buffer)
-  uint32_t* cand = nullptr;      // W*H: candidate cells of the phases
+  uint32_t* cand = nullptr;      // W*H: list of undecided cells of the phases
+  uint32_t* aux = nullptr;       // W*H: flood A's result, then component labels
+  uint32_t* cmin = nullptr;      // W*H: per-component phase minima (at roots)
   unsigned int* scal = nullptr;  // scalar block (see pitfill.cu)
 };
 

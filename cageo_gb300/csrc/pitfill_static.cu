@@ -9,9 +9,9 @@
 // scratch array compiled into this library instead.
 //
 // The array is a file-scope __device__ variable of kStaticFillBytes
-// (24 MiB): every GPU that loads the library holds it until the process
+// (64 MiB): every GPU that loads the library holds it until the process
 // exits.  It fits the fill workspace of grids up to 2048 x 2048 cells
-// (about 20 MiB there); larger grids are refused.  All calls share it and it
+// (about 52 MiB there); larger grids are refused.  All calls share it and it
 // keeps the last call's contents, so each call first clears the parts that
 // must start at zero; calls that overlap on the GPU (other streams, other
 // host threads) race on it and must be serialized by the caller.
@@ -21,7 +21,7 @@
 
 namespace cageo {
 
-constexpr size_t kStaticFillBytes = (size_t)24 << 20;
+constexpr size_t kStaticFillBytes = (size_t)64 << 20;
 
 static __device__ __align__(256) unsigned char g_static_fill_scratch[kStaticFillBytes];
 

@@ -125,7 +125,7 @@ cageo_status cageo_pitfill(float* d_dem, float* d_filled, int W, int H,
  * forbids plug-ins from calling cudaMalloc, or a loop that must not pay an
  * allocation's latency or implicit synchronization.  Same semantics and
  * result as cageo_pitfill; its scratch is a fixed array inside the library
- * (cageo_pitfill_static_max_bytes(), 24 MiB, held on every GPU that loads
+ * (cageo_pitfill_static_max_bytes(), 64 MiB, held on every GPU that loads
  * the library until the process exits), enough for grids up to 2048 x 2048
  * cells; larger grids are refused with CAGEO_ERR_ARGUMENT.  The first call
  * on a device looks up the array's device address (make that first call

@@ -50,7 +50,7 @@ def test_static_fill_refuses_grids_beyond_its_scratch(cuda):
     import torch
     from cageo_gb300 import api
     lib = api.lib()
-    assert lib.cageo_pitfill_static_max_bytes() == 24 << 20
+    assert lib.cageo_pitfill_static_max_bytes() == 64 << 20
     dummy = torch.zeros(4, device=cuda)
     st = lib.cageo_pitfill_static(ctypes.c_void_p(dummy.data_ptr()),
                                   ctypes.c_void_p(dummy.data_ptr() + 8), 4096, 4096, -9999.0,
