@@ -63,14 +63,22 @@ __host__ __device__ inline float ordered_to_float(uint32_t u) {
 }
 
 // Grid-wide barrier for persistent kernels launched cooperatively (all
-// blocks co-resident).  Sense is a generation counter.  Every wait is
-// bounded: after `limit` polls the block records an error in *err and
+// blocks co-resident).  One thread per block arrives on `count`; the last
+// arrival resets it and bumps `generation`, which the others poll with an
+// exponential back-off.  `count` and `generation` live on different
+// 128-byte lines so arrivals do not queue behind polls.  Every wait is
+// bounded: after the poll limit the block records an error in *err and
 // returns false; callers then leave their loops.
 struct GridSync {
   unsigned int* count;
   unsigned int* generation;
   int* err;
 };
+
+// Scalar-block slots used by GridSync (uint32 indices: separate lines).
+constexpr int kBarCountSlot = 32;
+constexpr int kBarGenSlot = 64;
+constexpr int kScalarSlots = 96;
 
 __device__ inline bool grid_barrier(const GridSync& g, unsigned int nblocks) {
   __syncthreads();
@@ -80,22 +88,23 @@ __device__ inline bool grid_barrier(const GridSync& g, unsigned int nblocks) {
     unsigned int my = *gen;
     __threadfence();
     unsigned int arrived = atomicAdd(g.count, 1u);
+    ok = 1;
     if (arrived == nblocks - 1) {
-      atomicExch(g.count, 0u);
+      *(volatile unsigned int*)g.count = 0u;
       __threadfence();
       atomicAdd(g.generation, 1u);
-      ok = 1;
     } else {
-      ok = 1;
+      unsigned int ns = 32;
       long long polls = 0;
       while (*gen == my) {
-        if (++polls > 40000000LL) {  // a few seconds at most
+        if (++polls > 20000000LL) {  // several seconds
           atomicExch(g.err, 1);
           ok = 0;
           break;
         }
-        if (*((volatile int*)g.err)) { ok = 0; break; }
-        __nanosleep(64);
+        if ((polls & 63) == 0 && *((volatile int*)g.err)) { ok = 0; break; }
+        __nanosleep(ns);
+        if (ns < 256) ns <<= 1;
       }
     }
     __threadfence();

@@ -102,7 +102,7 @@ struct cageo_pipeline {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool graph_ok = false;
-  int64_t stats[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  int64_t stats[16] = {};
 };
 
 namespace {
@@ -298,9 +298,9 @@ extern "C" cageo_status cageo_pipeline_run(cageo_pipeline* p, uint32_t first, in
     }
   }
   CAGEO_CUDA(cudaStreamSynchronize(s));
-  int64_t fs[7] = {0, 0, 0, 0, 0, 0, 0}, layers = 0, jumps = 0;
+  int64_t fs[11] = {}, rs[3] = {}, jumps = 0;
   if ((st = fill_check_status(p->fw, fs))) return st;
-  if ((st = route_check_status(p->rw, &layers))) return st;
+  if ((st = route_check_status(p->rw, rs))) return st;
   if ((st = trace_check_status(p->tw, &jumps))) return st;
   uint32_t nredo = 0;
   CAGEO_CUDA(cudaMemcpy(&nredo, p->dscal + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost));
@@ -319,10 +319,12 @@ extern "C" cageo_status cageo_pipeline_run(cageo_pipeline* p, uint32_t first, in
   }
   p->stats[0] = fs[0];
   p->stats[1] = fs[1];
-  p->stats[2] = layers;
+  p->stats[2] = rs[0];
   p->stats[3] = jumps;
   p->stats[4] = nredo;
-  for (int k = 0; k < 5; k++) p->stats[5 + k] = fs[2 + k];
+  for (int k = 0; k < 9; k++) p->stats[5 + k] = fs[2 + k];
+  p->stats[14] = rs[1];
+  p->stats[15] = rs[2];
   return CAGEO_OK;
 }
 
@@ -370,12 +372,15 @@ extern "C" cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t reali
       break;
     }
     for (int i = 0; i < 6 && i < n; i++) cudaEventElapsedTime(&h_ms[i], ev[i], ev[i + 1]);
-    int64_t fs[7];
+    int64_t fs[11], rs[3];
     if ((st = fill_check_status(p->fw, fs))) break;
     p->stats[0] = fs[0];
     p->stats[1] = fs[1];
-    for (int k = 0; k < 5; k++) p->stats[5 + k] = fs[2 + k];
-    if ((st = route_check_status(p->rw, &p->stats[2]))) break;
+    for (int k = 0; k < 9; k++) p->stats[5 + k] = fs[2 + k];
+    if ((st = route_check_status(p->rw, rs))) break;
+    p->stats[2] = rs[0];
+    p->stats[14] = rs[1];
+    p->stats[15] = rs[2];
     st = trace_check_status(p->tw, &p->stats[3]);
   } while (0);
   for (auto& e : ev) cudaEventDestroy(e);
@@ -425,7 +430,7 @@ extern "C" cudaStream_t cageo_pipeline_stream(cageo_pipeline* p) { return p ? p-
 
 extern "C" cageo_status cageo_pipeline_stats(cageo_pipeline* p, int64_t* h_stats, int n) {
   CAGEO_CHECK_ARG(p && h_stats, "null argument");
-  for (int i = 0; i < n && i < 10; i++) h_stats[i] = p->stats[i];
+  for (int i = 0; i < n && i < 16; i++) h_stats[i] = p->stats[i];
   return CAGEO_OK;
 }
 

@@ -41,8 +41,6 @@ constexpr uint8_t FNODATA = 0x01, FOUTLET = 0x02, FNONPASS = 0x04, FCONF = 0x08,
 // Scalar block layout (unsigned ints).
 enum : int {
   S_MIN = 0,       // ordered min of q (minE)
-  S_BAR_COUNT = 1,
-  S_BAR_GEN = 2,
   S_ERR = 3,       // 0 ok, 1 barrier wait limit, 2 pass limit
   S_LIST = 4,      // 3 slots: worklist counts
   S_M = 7,         // 3 slots: ordered phase minima
@@ -55,7 +53,13 @@ enum : int {
   S_US_B = 16,     // microseconds of flood B up to its first convergence
   S_US_P = 17,     // microseconds of the phase loop
   S_PEND = 18,     // 3 slots: pending cells seen by a phase
-  S_SIZE = 32
+  S_TILES_A = 21,  // tiles processed by flood A
+  S_ROUNDS_A = 22, // sweep rounds run by flood A
+  S_TILES_B = 23,  // tiles processed by flood B (phases included)
+  S_ROUNDS_B = 24, // sweep rounds run by flood B
+  S_BAR_COUNT = kBarCountSlot,
+  S_BAR_GEN = kBarGenSlot,
+  S_SIZE = kScalarSlots
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -65,7 +69,7 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 constexpr int kTile = 32;
-constexpr int kWarps = 4;
+constexpr int kWarps = 12;  // one 384-thread block per SM (12 x 14 KB smem)
 constexpr int kRS = 35;           // relay row stride (34 used)
 constexpr int kWS = 33;           // W/q row stride
 constexpr int kFS = 36;           // flag row stride (bytes)
@@ -83,7 +87,7 @@ size_t fill_workspace_bytes(int W, int H) {
   size_t n = (size_t)W * H;
   size_t nt = (size_t)((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile);
   return align_up(n, 256) + align_up(nt * 4, 256) + align_up(2 * nt * 4, 256) +
-         3 * align_up(n * 4, 256) + 256;
+         align_up(nt, 256) + 3 * align_up(n * 4, 256) + 512;
 }
 
 FillWork fill_carve(void* base, int W, int H) {
@@ -100,6 +104,8 @@ FillWork fill_carve(void* base, int W, int H) {
   p += align_up(nt * 4, 256);
   w.lists = (int*)p;
   p += align_up(2 * nt * 4, 256);
+  w.tdone = (uint8_t*)p;
+  p += align_up(nt, 256);
   w.cand = (uint32_t*)p;
   p += align_up(n * 4, 256);
   w.aux = (uint32_t*)p;
@@ -127,17 +133,22 @@ struct FloodArgs {
 };
 
 __device__ __forceinline__ void enqueue(const FillWork& w, int t, int k) {
+  if (((volatile uint8_t*)w.tdone)[t]) return;  // every cell of the tile is final
   if (atomicMax(&w.queued[t], k) < k) {
+    const unsigned int nt = (unsigned int)(w.tiles_x * w.tiles_y);
     unsigned int pos = atomicAdd(&w.scal[S_LIST + k % 3], 1u);
-    w.lists[(k & 1) * (w.tiles_x * w.tiles_y) + pos] = t;
+    if (pos < nt) w.lists[(k & 1) * nt + pos] = t;
+    else atomicCAS((int*)(w.scal + S_ERR), 0, 3);  // never: each tile is queued once per pass
   }
 }
 
 // Relax cell (x, y) of the staged tile; returns true if it changed.
+// A cell whose incoming level has dropped below its own q (FBELOW) is final
+// in both floods: its value is q and its relay can no longer change.
 template <int MODE>
 __device__ __forceinline__ bool relax(WarpSmem& s, int x, int y) {
   uint8_t f = s.F[y * kFS + x];
-  if (f & (FNODATA | FOUTLET)) return false;
+  if (f & (FNODATA | FOUTLET | FBELOW)) return false;
   const float* r = &s.R[(y + 1) * kRS + (x + 1)];
   float m = fminf(fminf(fminf(r[-kRS - 1], r[-kRS]), fminf(r[-kRS + 1], r[-1])),
                   fminf(fminf(r[1], r[kRS - 1]), fminf(r[kRS], r[kRS + 1])));
@@ -161,6 +172,7 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
   const int W = w.W, H = w.H;
   const int tx = t % w.tiles_x, ty = t / w.tiles_x;
   const int x0 = tx * kTile, y0 = ty * kTile;
+#pragma unroll 4
   for (int idx = lane; idx < 34 * 34; idx += 32) {
     int hy = idx / 34, hx = idx - hy * 34;
     int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
@@ -181,13 +193,26 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
   }
   __syncwarp();
   bool capped = true;
+  int rounds = kMaxRounds;
   for (int round = 0; round < kMaxRounds; round++) {
     bool any = false;
-    for (int y = 0; y < kTile; y++) { any |= relax<MODE>(s, lane, y); __syncwarp(); }
-    for (int y = kTile - 1; y >= 0; y--) { any |= relax<MODE>(s, lane, y); __syncwarp(); }
-    for (int x = 0; x < kTile; x++) { any |= relax<MODE>(s, x, lane); __syncwarp(); }
-    for (int x = kTile - 1; x >= 0; x--) { any |= relax<MODE>(s, x, lane); __syncwarp(); }
-    if (!__any_sync(0xffffffffu, any)) { capped = false; break; }
+    // Down and up sweeps interleaved (two independent chains per lane),
+    // then right and left.
+    for (int k = 0; k < kTile; k++) {
+      any |= relax<MODE>(s, lane, k);
+      any |= relax<MODE>(s, lane, kTile - 1 - k);
+      __syncwarp();
+    }
+    for (int k = 0; k < kTile; k++) {
+      any |= relax<MODE>(s, k, lane);
+      any |= relax<MODE>(s, kTile - 1 - k, lane);
+      __syncwarp();
+    }
+    if (!__any_sync(0xffffffffu, any)) { capped = false; rounds = round + 1; break; }
+  }
+  if (lane == 0) {
+    atomicAdd(&w.scal[MODE == 0 ? S_TILES_A : S_TILES_B], 1u);
+    atomicAdd(&w.scal[MODE == 0 ? S_ROUNDS_A : S_ROUNDS_B], (unsigned int)rounds);
   }
   // Write back changed cells; note which borders changed.
   unsigned int sides = 0;  // 1 L, 2 R, 4 T, 8 B, 16 TL, 32 TR, 64 BL, 128 BR
@@ -209,6 +234,12 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
     }
   }
   sides = __reduce_or_sync(0xffffffffu, sides);
+  {
+    bool fin = true;
+    for (int idx = lane; idx < kTile * kTile; idx += 32)
+      fin &= (s.F[(idx >> 5) * kFS + (idx & 31)] & (FNODATA | FOUTLET | FBELOW)) != 0;
+    if (__all_sync(0xffffffffu, fin) && lane == 0) w.tdone[t] = 1;
+  }
   const int k = p + 1;
   // Lanes 0..8 queue self (if capped) and the 8 neighbours whose halo changed.
   if (lane < 9) {
@@ -413,9 +444,12 @@ __global__ void fill_init_kernel(const float* __restrict__ q, float* __restrict_
 
 // Between the floods: keep flood A's result (lower bound) in aux and
 // FBELOWA, confirm non-passable cells reached at a level >= q, reset W.
+// Also clears the worklist counts: flood A's last count slot is the one
+// flood B's first pass appends to.
 __global__ void fill_classify_kernel(float* __restrict__ Wg, uint8_t* __restrict__ F,
-                                     uint32_t* __restrict__ aux, int64_t n) {
+                                     uint32_t* __restrict__ aux, unsigned int* scal, int64_t n) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < 3) scal[S_LIST + i] = 0u;
   if (i >= n) return;
   uint8_t f = F[i];
   const float wa = Wg[i];
@@ -449,8 +483,8 @@ __global__ void quantize_min_kernel(float* __restrict__ d, int64_t n, float noda
 }
 
 __global__ void fill_scalars_kernel(unsigned int* s) {
-  int i = threadIdx.x;
-  if (i < S_SIZE) s[i] = (i == S_MIN || (i >= S_M && i < S_M + 3)) ? 0xffffffffu : 0u;
+  for (int i = threadIdx.x; i < S_SIZE; i += blockDim.x)
+    s[i] = (i == S_MIN || (i >= S_M && i < S_M + 3)) ? 0xffffffffu : 0u;
 }
 
 static int coop_blocks(const void* fn, size_t smem) {
@@ -489,10 +523,13 @@ cageo_status fill_run(const float* q, float* filled, const FillWork& w, float no
   fill_init_kernel<<<blocks, 256, 0, s>>>(q, filled, w.flags, w.scal + S_MIN, w.W, w.H, nodata);
   CAGEO_CUDA(cudaGetLastError());
   FloodArgs a{q, filled, w};
+  const size_t nt = (size_t)w.tiles_x * w.tiles_y;
+  CAGEO_CUDA(cudaMemsetAsync(w.tdone, 0, nt, s));
   cageo_status st = launch_flood<0>(a, s);
   if (st) return st;
-  fill_classify_kernel<<<blocks, 256, 0, s>>>(filled, w.flags, w.aux, n);
+  fill_classify_kernel<<<blocks, 256, 0, s>>>(filled, w.flags, w.aux, w.scal, n);
   CAGEO_CUDA(cudaGetLastError());
+  CAGEO_CUDA(cudaMemsetAsync(w.tdone, 0, nt, s));
   st = launch_flood<1>(a, s);
   if (st) return st;
   fill_final_kernel<<<blocks, 256, 0, s>>>(q, filled, n);
@@ -518,10 +555,15 @@ cageo_status fill_check_status(const FillWork& w, int64_t* stats) {
     stats[4] = h[S_US_A];
     stats[5] = h[S_US_B];
     stats[6] = h[S_US_P];
+    stats[7] = h[S_TILES_A];
+    stats[8] = h[S_ROUNDS_A];
+    stats[9] = h[S_TILES_B];
+    stats[10] = h[S_ROUNDS_B];
   }
   if (h[S_ERR]) {
-    set_error(h[S_ERR] == 1 ? "pit filling: a grid-wide wait hit its limit"
-                            : "pit filling: pass limit reached without convergence");
+    set_error(h[S_ERR] == 1   ? "pit filling: a grid-wide wait hit its limit"
+              : h[S_ERR] == 2 ? "pit filling: pass or loop limit reached without convergence"
+                              : "pit filling: internal worklist overflow");
     return CAGEO_ERR_NO_CONVERGENCE;
   }
   return CAGEO_OK;

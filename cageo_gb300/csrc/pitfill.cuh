@@ -15,6 +15,7 @@ struct FillWork {
   uint8_t* flags = nullptr;      // W*H
   int* queued = nullptr;         // ntiles: last pass a tile was queued for
   int* lists = nullptr;          // 2 * ntiles: tile worklists (double buffer)
+  uint8_t* tdone = nullptr;      // ntiles: 1 once every cell of the tile is final
   uint32_t* cand = nullptr;      // W*H: list of undecided cells of the phases
   uint32_t* aux = nullptr;       // W*H: flood A's result, then component labels
   uint32_t* cmin = nullptr;      // W*H: per-component phase minima (at roots)
@@ -37,9 +38,10 @@ cageo_status fill_quantize_min(float* d, const FillWork& w, float nodata,
 cageo_status fill_reset_scalars(const FillWork& w, cudaStream_t s);
 unsigned int* fill_min_slot(const FillWork& w);
 // Copies the device status (0 ok) and stats into host memory; the stream
-// must have been synchronized.  stats (7 entries): last pass number,
+// must have been synchronized.  stats (11 entries): last pass number,
 // phases, passes of flood A, passes of flood B before the first phase,
-// microseconds of flood A, of flood B to convergence, of the phase loop.
+// microseconds of flood A, of flood B to convergence, of the phase loop,
+// tiles and sweep rounds of flood A, tiles and rounds of flood B.
 cageo_status fill_check_status(const FillWork& w, int64_t* stats);
 
 }  // namespace cageo

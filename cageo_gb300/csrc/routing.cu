@@ -22,12 +22,13 @@
 namespace cageo {
 
 constexpr int kFlatInf = 0x3fffffff;
-enum : int { R_NFLAT = 0, R_BAR_COUNT = 1, R_BAR_GEN = 2, R_ERR = 3, R_CNT = 4, R_LAYERS = 7,
-             R_SIZE = 16 };
+enum : int { R_NFLAT = 0, R_ERR = 3, R_CNT = 4, R_LAYERS = 7, R_US_BFS = 8, R_BAR_COUNT = kBarCountSlot,
+             R_BAR_GEN = kBarGenSlot, R_SIZE = kScalarSlots };
+constexpr int kBfsThreads = 512;
 
 size_t route_workspace_bytes(int W, int H) {
   size_t n = (size_t)W * H;
-  return 3 * align_up(n * 4, 256) + 256;
+  return 3 * align_up(n * 4, 256) + 512;
 }
 
 RouteWork route_carve(void* base, int W, int H) {
@@ -125,13 +126,15 @@ __global__ void flat_mark_kernel(int* __restrict__ fd, RouteWork w) {
 
 // Frontier BFS: layer k -> k+1 over flat cells with elevation >= the
 // frontier cell's.  Persistent, one bounded grid barrier per layer.
-__global__ void flat_bfs_kernel(const float* __restrict__ dem, int* __restrict__ fd,
-                                RouteWork w) {
+__global__ void __launch_bounds__(kBfsThreads)
+flat_bfs_kernel(const float* __restrict__ dem, int* __restrict__ fd, RouteWork w) {
   const int W = w.W, H = w.H;
   const int64_t N = (int64_t)W * H;
   GridSync gs{w.scal + R_BAR_COUNT, w.scal + R_BAR_GEN, (int*)(w.scal + R_ERR)};
   volatile unsigned int* vs = w.scal;
   int k = 1;
+  unsigned long long t0;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
   while (true) {
     if (blockIdx.x == 0 && threadIdx.x == 0) vs[R_CNT + (k + 2) % 3] = 0u;
     const unsigned int n = vs[R_CNT + k % 3];
@@ -161,7 +164,12 @@ __global__ void flat_bfs_kernel(const float* __restrict__ dem, int* __restrict__
     }
     k++;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) vs[R_LAYERS] = (unsigned int)k;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    unsigned long long t1;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+    vs[R_LAYERS] = (unsigned int)k;
+    vs[R_US_BFS] = (unsigned int)((t1 - t0) / 1000);
+  }
 }
 
 // Directions of flat cells: last neighbour (N..NW) in the previous layer
@@ -200,7 +208,7 @@ __global__ void flat_final_kernel(int* __restrict__ fd, RouteWork w) {
 }
 
 __global__ void route_scalars_kernel(unsigned int* s) {
-  if (threadIdx.x < R_SIZE) s[threadIdx.x] = 0u;
+  for (int i = threadIdx.x; i < R_SIZE; i += blockDim.x) s[i] = 0u;
 }
 
 static int coop_blocks_bfs() {
@@ -209,15 +217,15 @@ static int coop_blocks_bfs() {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, flat_bfs_kernel, 256, 0);
-    blocks = std::max(1, per) * sms;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, flat_bfs_kernel, kBfsThreads, 0);
+    blocks = std::max(1, std::min(per, 2)) * sms;
   }
   return blocks;
 }
 
 cageo_status route_run(const float* filled, int8_t* dir, int* fd, const RouteWork& w,
                        cudaStream_t s) {
-  route_scalars_kernel<<<1, 32, 0, s>>>(w.scal);
+  route_scalars_kernel<<<1, 128, 0, s>>>(w.scal);
   dim3 b(32, 8), g((w.W + 31) / 32, (w.H + 7) / 8);
   d8_kernel<<<g, b, 0, s>>>(filled, (char2*)dir, fd, w);
   CAGEO_CUDA(cudaGetLastError());
@@ -233,17 +241,21 @@ cageo_status route_run(const float* filled, int8_t* dir, int* fd, const RouteWor
   RouteWork wc = w;
   void* params[] = {(void*)&f, (void*)&fdp, (void*)&wc};
   CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)flat_bfs_kernel, dim3(coop_blocks_bfs()),
-                                         dim3(256), params, 0, s));
+                                         dim3(kBfsThreads), params, 0, s));
   flat_dir_kernel<<<lb, 256, 0, s>>>(filled, (char2*)dir, fd, w);
   flat_final_kernel<<<lb, 256, 0, s>>>(fd, w);
   CAGEO_CUDA(cudaGetLastError());
   return CAGEO_OK;
 }
 
-cageo_status route_check_status(const RouteWork& w, int64_t* layers) {
+cageo_status route_check_status(const RouteWork& w, int64_t* stats) {
   unsigned int h[R_SIZE];
   CAGEO_CUDA(cudaMemcpy(h, w.scal, sizeof(h), cudaMemcpyDeviceToHost));
-  if (layers) *layers = h[R_LAYERS];
+  if (stats) {
+    stats[0] = h[R_LAYERS];
+    stats[1] = h[R_NFLAT];
+    stats[2] = h[R_US_BFS];
+  }
   if (h[R_ERR]) {
     set_error("flow routing: flat-surface BFS hit a wait or layer limit");
     return CAGEO_ERR_NO_CONVERGENCE;

@@ -17,7 +17,8 @@ size_t route_workspace_bytes(int W, int H);
 RouteWork route_carve(void* base, int W, int H);
 cageo_status route_run(const float* filled, int8_t* dir, int* flatdist,
                        const RouteWork& w, cudaStream_t s);
-cageo_status route_check_status(const RouteWork& w, int64_t* bfs_layers);
+// stats (3 entries, may be null): BFS layers, flat cells, BFS microseconds.
+cageo_status route_check_status(const RouteWork& w, int64_t* stats);
 
 struct TraceWork {
   int W = 0, H = 0;

@@ -28,10 +28,12 @@ namespace cageo {
 
 constexpr long long kResolved = 1LL << 32;
 constexpr int kStuck = (int)0x80000000;  // dead end marker, never a real label
-enum : int { T_BAR_COUNT = 0, T_BAR_GEN = 1, T_ERR = 2, T_ACTIVE = 3, T_JUMPS = 6, T_SIZE = 8 };
+enum : int { T_ERR = 2, T_ACTIVE = 3, T_JUMPS = 6, T_BAR_COUNT = kBarCountSlot,
+             T_BAR_GEN = kBarGenSlot, T_SIZE = kScalarSlots };
+constexpr int kJumpThreads = 512;
 
 size_t trace_workspace_bytes(int W, int H) {
-  return align_up((size_t)W * H * 8, 256) + 256;
+  return align_up((size_t)W * H * 8, 256) + 512;
 }
 
 TraceWork trace_carve(void* base, int W, int H) {
@@ -66,7 +68,7 @@ __global__ void trace_init_kernel(const char2* __restrict__ dir,
 
 // Pointer doubling in place (reading a neighbour's newer state only speeds
 // convergence).  Persistent; one bounded grid barrier per pass.
-__global__ void trace_jump_kernel(long long* st, TraceWork w) {
+__global__ void __launch_bounds__(kJumpThreads) trace_jump_kernel(long long* st, TraceWork w) {
   const int64_t N = (int64_t)w.W * w.H;
   GridSync gs{w.scal + T_BAR_COUNT, w.scal + T_BAR_GEN, (int*)(w.scal + T_ERR)};
   volatile unsigned int* vs = w.scal;
@@ -110,14 +112,14 @@ __global__ void trace_final_kernel(const long long* __restrict__ st, int* __rest
 }
 
 __global__ void trace_scalars_kernel(unsigned int* s) {
-  if (threadIdx.x < T_SIZE) s[threadIdx.x] = 0u;
+  for (int i = threadIdx.x; i < T_SIZE; i += blockDim.x) s[i] = 0u;
 }
 
 cageo_status trace_run(const int8_t* dir, const float* streams, int* label,
                        const TraceWork& w, cudaStream_t s) {
   const int64_t n = (int64_t)w.W * w.H;
   const unsigned blocks = (unsigned)((n + 255) / 256);
-  trace_scalars_kernel<<<1, 32, 0, s>>>(w.scal);
+  trace_scalars_kernel<<<1, 128, 0, s>>>(w.scal);
   trace_init_kernel<<<blocks, 256, 0, s>>>((const char2*)dir, streams, w.state, w.W, w.H);
   CAGEO_CUDA(cudaGetLastError());
   static int coop = 0;
@@ -125,14 +127,14 @@ cageo_status trace_run(const int8_t* dir, const float* streams, int* label,
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trace_jump_kernel, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trace_jump_kernel, kJumpThreads, 0);
     coop = std::max(1, per) * sms;
   }
   long long* stp = w.state;
   TraceWork wc = w;
   void* params[] = {(void*)&stp, (void*)&wc};
-  CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)trace_jump_kernel, dim3(coop), dim3(256),
-                                         params, 0, s));
+  CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)trace_jump_kernel, dim3(coop),
+                                         dim3(kJumpThreads), params, 0, s));
   trace_final_kernel<<<blocks, 256, 0, s>>>(w.state, label, n);
   CAGEO_CUDA(cudaGetLastError());
   return CAGEO_OK;

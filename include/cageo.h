@@ -217,7 +217,9 @@ cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t realization,
  * [2] flat-BFS layers, [3] trace jumps, [4] burn re-runs, [5] passes of
  * the lower-bound flood, [6] passes of the walled flood before the first
  * phase, [7..9] microseconds of the lower-bound flood, of the walled flood
- * to convergence and of the phase loop (last realization). */
+ * to convergence and of the phase loop, [10..13] tiles and sweep rounds of
+ * the two floods, [14] flat cells, [15] microseconds of the flat BFS (last
+ * realization). */
 cageo_status cageo_pipeline_stats(cageo_pipeline* p, int64_t* h_stats, int n);
 void cageo_pipeline_destroy(cageo_pipeline* p);
 

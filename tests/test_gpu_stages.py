@@ -58,6 +58,25 @@ def test_pitfill(cuda, oracle, W, H, seed):
     assert np.array_equal(bits(filled.cpu().numpy()), bits(f_ref)), "filled DEM"
 
 
+@pytest.mark.parametrize("realization", range(4))
+def test_pitfill_philox_noise(cuda, oracle, realization):
+    """Fill of realistic DEMs made from the library's own Philox noise (the
+    inputs the pipeline sees), 512 x 512."""
+    import torch
+    from cageo_gb300 import api
+    W = H = 512
+    dem, streams = make_case(W, H, seed=W)
+    r = api.filter_radius(60.0, 10.0)
+    taps = api.filter_build(api.FILTER_GAUSSIAN, 60.0, 10.0, r)
+    noise = torch.empty((H, W), dtype=torch.float32, device=cuda)
+    api.noise_philox(noise, 77, realization, 0.0, 1.5)
+    conv = oracle.convolve(noise.cpu().numpy(), taps, r, 1)
+    rdem = oracle.stream_burn(oracle.realistic_dem(dem, conv), streams)
+    _, f_ref = oracle.pitfill(rdem)
+    filled = api.pitfill(_t(rdem, cuda))
+    assert np.array_equal(bits(filled.cpu().numpy()), bits(f_ref))
+
+
 def test_pitfill_no_streams_and_nodata(cuda, oracle):
     """minE != 0 (no stream cell) and NODATA cells change the round-trip test."""
     from cageo_gb300 import api
