@@ -57,6 +57,9 @@ enum : int {
   S_ROUNDS_A = 22, // sweep rounds run by flood A
   S_TILES_B = 23,  // tiles processed by flood B (phases included)
   S_ROUNDS_B = 24, // sweep rounds run by flood B
+  S_KCYC_LOAD = 25,  // kilo-cycles (summed over tile visits) staging tiles
+  S_KCYC_SWEEP = 26, // kilo-cycles sweeping
+  S_KCYC_STORE = 27, // kilo-cycles writing back and queueing
   S_BAR_COUNT = kBarCountSlot,
   S_BAR_GEN = kBarGenSlot,
   S_SIZE = kScalarSlots
@@ -143,15 +146,14 @@ __device__ __forceinline__ void enqueue(const FillWork& w, int t, int k) {
 }
 
 // Relax cell (x, y) of the staged tile; returns true if it changed.
-// A cell whose incoming level has dropped below its own q (FBELOW) is final
-// in both floods: its value is q and its relay can no longer change.
+// Update cell (x, y) of the staged tile given m, the least relay among its
+// 8 neighbours; returns true if it changed.  A cell whose incoming level has
+// dropped below its own q (FBELOW) is final in both floods: its value is q
+// and its relay can no longer change.
 template <int MODE>
-__device__ __forceinline__ bool relax(WarpSmem& s, int x, int y) {
+__device__ __forceinline__ bool update_cell(WarpSmem& s, int x, int y, float m) {
   uint8_t f = s.F[y * kFS + x];
   if (f & (FNODATA | FOUTLET | FBELOW)) return false;
-  const float* r = &s.R[(y + 1) * kRS + (x + 1)];
-  float m = fminf(fminf(fminf(r[-kRS - 1], r[-kRS]), fminf(r[-kRS + 1], r[-1])),
-                  fminf(fminf(r[1], r[kRS - 1]), fminf(r[kRS], r[kRS + 1])));
   float w = s.Wv[y * kWS + x];
   float qv = s.Qv[y * kWS + x];
   float nw = fminf(w, fmaxf(qv, m));
@@ -165,6 +167,13 @@ __device__ __forceinline__ bool relax(WarpSmem& s, int x, int y) {
   return false;
 }
 
+// Least relay among the 8 neighbours of staged cell (x, y).
+__device__ __forceinline__ float nbr_min(const WarpSmem& s, int x, int y) {
+  const float* r = &s.R[(y + 1) * kRS + (x + 1)];
+  return fminf(fminf(fminf(r[-kRS - 1], r[-kRS]), fminf(r[-kRS + 1], r[-1])),
+               fminf(fminf(r[1], r[kRS - 1]), fminf(r[kRS], r[kRS + 1])));
+}
+
 template <int MODE>
 __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
                              int lane) {
@@ -172,6 +181,7 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
   const int W = w.W, H = w.H;
   const int tx = t % w.tiles_x, ty = t / w.tiles_x;
   const int x0 = tx * kTile, y0 = ty * kTile;
+  const long long c0 = clock64();
 #pragma unroll 4
   for (int idx = lane; idx < 34 * 34; idx += 32) {
     int hy = idx / 34, hx = idx - hy * 34;
@@ -192,24 +202,56 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
     }
   }
   __syncwarp();
+  const long long c1 = clock64();
+  // Sweeps.  A cell needs re-evaluating only after one of its 8 neighbours
+  // changed, so each phase carries warp-uniform masks of the rows (vertical
+  // phase) or columns (horizontal phase) to evaluate: all rows first, then
+  // the rows/columns next to a change.  A change also marks its neighbours
+  // for the rest of the current sweep.  Changes of a vertical phase select
+  // the columns of the following horizontal phase (which re-evaluates every
+  // neighbour of those changes) and vice versa, so a horizontal phase
+  // without a change leaves a fixpoint.
+  auto smear = [](unsigned int m) { return m | (m << 1) | (m >> 1); };
   bool capped = true;
   int rounds = kMaxRounds;
+  unsigned int next_rows = 0xffffffffu;  // rows to evaluate in the next vertical phase
   for (int round = 0; round < kMaxRounds; round++) {
-    bool any = false;
-    // Down and up sweeps interleaved (two independent chains per lane),
-    // then right and left.
+    unsigned int pend = next_rows, cch = 0;
     for (int k = 0; k < kTile; k++) {
-      any |= relax<MODE>(s, lane, k);
-      any |= relax<MODE>(s, lane, kTile - 1 - k);
+      const int d = k, u = kTile - 1 - k;
+      unsigned int b1 = 0, b2 = 0;
+      if ((pend >> d) & 1u) {
+        const float m = nbr_min(s, lane, d);
+        b1 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, lane, d, m));
+      }
+      if ((pend >> u) & 1u) {
+        const float m = nbr_min(s, lane, u);
+        b2 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, lane, u, m));
+      }
+      if (b1) { cch |= b1; pend |= smear(1u << d); }
+      if (b2) { cch |= b2; pend |= smear(1u << u); }
       __syncwarp();
     }
+    unsigned int pendc = smear(cch), rch2 = 0;
     for (int k = 0; k < kTile; k++) {
-      any |= relax<MODE>(s, k, lane);
-      any |= relax<MODE>(s, kTile - 1 - k, lane);
+      const int l = k, r = kTile - 1 - k;
+      unsigned int b1 = 0, b2 = 0;
+      if ((pendc >> l) & 1u) {
+        const float m = nbr_min(s, l, lane);
+        b1 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, l, lane, m));
+      }
+      if ((pendc >> r) & 1u) {
+        const float m = nbr_min(s, r, lane);
+        b2 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, r, lane, m));
+      }
+      if (b1) { rch2 |= b1; pendc |= smear(1u << l); }
+      if (b2) { rch2 |= b2; pendc |= smear(1u << r); }
       __syncwarp();
     }
-    if (!__any_sync(0xffffffffu, any)) { capped = false; rounds = round + 1; break; }
+    if (!rch2) { capped = false; rounds = round + 1; break; }
+    next_rows = smear(rch2);
   }
+  const long long c2 = clock64();
   if (lane == 0) {
     atomicAdd(&w.scal[MODE == 0 ? S_TILES_A : S_TILES_B], 1u);
     atomicAdd(&w.scal[MODE == 0 ? S_ROUNDS_A : S_ROUNDS_B], (unsigned int)rounds);
@@ -261,6 +303,12 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
       enqueue(w, ny * w.tiles_x + nx, k);
   }
   __syncwarp();
+  if (lane == 0) {
+    const long long c3 = clock64();
+    atomicAdd(&w.scal[S_KCYC_LOAD], (unsigned int)((c1 - c0) >> 10));
+    atomicAdd(&w.scal[S_KCYC_SWEEP], (unsigned int)((c2 - c1) >> 10));
+    atomicAdd(&w.scal[S_KCYC_STORE], (unsigned int)((c3 - c2) >> 10));
+  }
 }
 
 // Lock-free union-find over the undecided cells (labels in w.aux): links
@@ -288,7 +336,7 @@ __device__ __forceinline__ bool uf_unite(uint32_t* lab, uint32_t a, uint32_t b) 
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kWarps * 32)
+__global__ void __launch_bounds__(kWarps * 32, 1)
 fill_flood_kernel(FloodArgs a) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -559,6 +607,9 @@ cageo_status fill_check_status(const FillWork& w, int64_t* stats) {
     stats[8] = h[S_ROUNDS_A];
     stats[9] = h[S_TILES_B];
     stats[10] = h[S_ROUNDS_B];
+    stats[11] = h[S_KCYC_LOAD];
+    stats[12] = h[S_KCYC_SWEEP];
+    stats[13] = h[S_KCYC_STORE];
   }
   if (h[S_ERR]) {
     set_error(h[S_ERR] == 1   ? "pit filling: a grid-wide wait hit its limit"

@@ -38,10 +38,11 @@ cageo_status fill_quantize_min(float* d, const FillWork& w, float nodata,
 cageo_status fill_reset_scalars(const FillWork& w, cudaStream_t s);
 unsigned int* fill_min_slot(const FillWork& w);
 // Copies the device status (0 ok) and stats into host memory; the stream
-// must have been synchronized.  stats (11 entries): last pass number,
+// must have been synchronized.  stats (14 entries): last pass number,
 // phases, passes of flood A, passes of flood B before the first phase,
 // microseconds of flood A, of flood B to convergence, of the phase loop,
-// tiles and sweep rounds of flood A, tiles and rounds of flood B.
+// tiles and sweep rounds of flood A, tiles and rounds of flood B, and
+// kilo-cycles summed over tile visits spent staging, sweeping, storing.
 cageo_status fill_check_status(const FillWork& w, int64_t* stats);
 
 }  // namespace cageo

@@ -218,8 +218,9 @@ cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t realization,
  * the lower-bound flood, [6] passes of the walled flood before the first
  * phase, [7..9] microseconds of the lower-bound flood, of the walled flood
  * to convergence and of the phase loop, [10..13] tiles and sweep rounds of
- * the two floods, [14] flat cells, [15] microseconds of the flat BFS (last
- * realization). */
+ * the two floods, [14] flat cells, [15] microseconds of the flat BFS,
+ * [16..18] kilo-cycles summed over the fill's tile visits spent staging,
+ * sweeping and storing (last realization). */
 cageo_status cageo_pipeline_stats(cageo_pipeline* p, int64_t* h_stats, int n);
 void cageo_pipeline_destroy(cageo_pipeline* p);
 
