@@ -62,6 +62,22 @@ __host__ __device__ inline float ordered_to_float(uint32_t u) {
   return f;
 }
 
+// Appends for every lane of the calling warp whose `pred` is true, with a
+// single atomicAdd per warp; returns the lane's slot, or 0xffffffff when
+// `pred` is false.  All active lanes of the warp must call it together.
+__device__ __forceinline__ unsigned int warp_append(unsigned int* counter, bool pred) {
+  const unsigned int active = __activemask();
+  const unsigned int ball = __ballot_sync(active, pred);
+  if (!ball) return 0xffffffffu;
+  unsigned int lane;
+  asm volatile("mov.u32 %0, %%laneid;" : "=r"(lane));
+  const int leader = __ffs(ball) - 1;
+  unsigned int base = 0;
+  if ((int)lane == leader) base = atomicAdd(counter, (unsigned int)__popc(ball));
+  base = __shfl_sync(active, base, leader);
+  return pred ? base + (unsigned int)__popc(ball & ((1u << lane) - 1u)) : 0xffffffffu;
+}
+
 // Grid-wide barrier for persistent kernels launched cooperatively (all
 // blocks co-resident).  One thread per block arrives on `count`; the last
 // arrival resets it and bumps `generation`, which the others poll with an

@@ -93,6 +93,28 @@ __device__ inline void block_min_out(float local_min, const FrontEpilogue& e) {
   }
 }
 
+// 8 outputs along a line from a sliding window of 8 registers: out[j] =
+// sum_t v[j + t] * taps[t], t ascending, each sum starting at 0.
+__device__ __forceinline__ void conv_line8(const float* __restrict__ v, int stride,
+                                           const float* __restrict__ taps, int L,
+                                           float acc[8]) {
+  float win[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    win[j] = v[j * stride];
+    acc[j] = 0.0f;
+  }
+#pragma unroll 8
+  for (int t = 0; t < L; t++) {
+    const float tap = taps[t];
+#pragma unroll
+    for (int j = 0; j < 8; j++) acc[j] = __fadd_rn(acc[j], __fmul_rn(win[j], tap));
+#pragma unroll
+    for (int j = 0; j < 7; j++) win[j] = win[j + 1];
+    win[7] = (t + 1 < L) ? v[(t + 8) * stride] : 0.0f;
+  }
+}
+
 template <class Epi>
 __global__ void __launch_bounds__(kSepThreads)
 conv_sep_kernel(const float* __restrict__ in, int W, int H,
@@ -111,26 +133,28 @@ conv_sep_kernel(const float* __restrict__ in, int W, int H,
     s_in[idx] = in[(int64_t)gy * W + gx];
   }
   __syncthreads();
-  // Column pass: tmp[y][ix] = sum_t in[y+t][ix] * taps[t].
-  for (int idx = threadIdx.x; idx < IW * kSepTH; idx += blockDim.x) {
-    int y = idx / IW, ix = idx - y * IW;
-    float sum = 0.0f;
-    const float* col = s_in + y * IW + ix;
-    for (int t = 0; t < L; t++) sum = __fadd_rn(sum, __fmul_rn(col[t * IW], s_taps[t]));
-    s_tmp[idx] = sum;
+  // Column pass: tmp[y][ix] = sum_t in[y+t][ix] * taps[t], 8 rows per item.
+  for (int item = threadIdx.x; item < IW * (kSepTH / 8); item += blockDim.x) {
+    const int g = item / IW, ix = item - g * IW;
+    float acc[8];
+    conv_line8(s_in + (8 * g) * IW + ix, IW, s_taps, L, acc);
+#pragma unroll
+    for (int j = 0; j < 8; j++) s_tmp[(8 * g + j) * IW + ix] = acc[j];
   }
   __syncthreads();
-  // Row pass and store.
+  // Row pass (8 consecutive outputs per item) and store.
   float local_min = kInf;
-  for (int idx = threadIdx.x; idx < kSepTW * kSepTH; idx += blockDim.x) {
-    int y = idx / kSepTW, x = idx - y * kSepTW;
-    int gy = y0 + y, gx = x0 + x;
-    if (gy >= H || gx >= W) continue;
-    const float* row = s_tmp + y * IW + x;
-    float sum = 0.0f;
-    for (int t = 0; t < L; t++) sum = __fadd_rn(sum, __fmul_rn(row[t], s_taps[t]));
-    float q = epi((int64_t)gy * W + gx, sum);
-    local_min = fminf(local_min, q);
+  for (int item = threadIdx.x; item < kSepTH * (kSepTW / 8); item += blockDim.x) {
+    const int y = item / (kSepTW / 8), g = item - y * (kSepTW / 8);
+    float acc[8];
+    conv_line8(s_tmp + y * IW + 8 * g, 1, s_taps, L, acc);
+    const int gy = y0 + y;
+    if (gy >= H) continue;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const int gx = x0 + 8 * g + j;
+      if (gx < W) local_min = fminf(local_min, epi((int64_t)gy * W + gx, acc[j]));
+    }
   }
   block_min_out(local_min, epi);
 }

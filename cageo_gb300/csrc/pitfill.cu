@@ -383,11 +383,11 @@ fill_flood_kernel(FloodArgs a) {
           const bool unsure = wa != a.Wg[i] ||
                               ((f & FNONPASS) && (((f & FBELOWA) != 0) != ((f & FBELOW) != 0)));
           if (unsure) {
-            unsigned int pos = atomicAdd(&w.scal[S_CAND], 1u);
-            w.cand[pos] = (uint32_t)i;
             w.flags[i] = f | FUNSURE;
             w.aux[i] = (uint32_t)i;
           }
+          const unsigned int pos = warp_append(&w.scal[S_CAND], unsure);
+          if (unsure) w.cand[pos] = (uint32_t)i;
         }
         if (!grid_barrier(gs, nblocks)) break;
         const unsigned int nu = vs[S_CAND];

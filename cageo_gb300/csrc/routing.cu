@@ -11,9 +11,11 @@
 // neighbour in layer k-1 (layer 0 = cells with a direction, flatDist -1)
 // whose elevation is <= theirs, taking the direction of the LAST such
 // neighbour in N..NW order.  Layer numbers are breadth-first distances, so
-// they are computed here by a frontier BFS (one grid-wide barrier per
-// layer, persistent cooperative kernel) and the directions by one final
-// pass that applies the last-match rule to the finished distances.
+// they are computed here as shortest-path distances by tile relaxation (a
+// persistent cooperative kernel: one warp sweeps a 32x32 tile of the tiles
+// that hold flat cells until stable, and queues the neighbouring tiles when
+// its border changed), and the directions by one final pass that applies
+// the last-match rule to the finished distances.
 #include <algorithm>
 #include "common.cuh"
 #include "routing.cuh"
@@ -22,27 +24,51 @@
 namespace cageo {
 
 constexpr int kFlatInf = 0x3fffffff;
-enum : int { R_NFLAT = 0, R_ERR = 3, R_CNT = 4, R_LAYERS = 7, R_US_BFS = 8, R_BAR_COUNT = kBarCountSlot,
-             R_BAR_GEN = kBarGenSlot, R_SIZE = kScalarSlots };
-constexpr int kBfsThreads = 512;
+enum : int { R_NFLAT = 0, R_ERR = 3, R_LIST = 4, R_LAYERS = 7, R_US_BFS = 8, R_PASSES = 9,
+             R_BAR_COUNT = kBarCountSlot, R_BAR_GEN = kBarGenSlot, R_SIZE = kScalarSlots };
+constexpr int kFT = 32;          // flat tile size
+constexpr int kFWarps = 16;      // warps per block of the flat kernel
+constexpr int kFRS = 35;         // staged row stride
 
 size_t route_workspace_bytes(int W, int H) {
-  size_t n = (size_t)W * H;
-  return 3 * align_up(n * 4, 256) + 512;
+  const size_t n = (size_t)W * H;
+  const size_t nt = (size_t)((W + kFT - 1) / kFT) * ((H + kFT - 1) / kFT);
+  return align_up(n * 4, 256) + align_up(nt, 256) + align_up(nt * 4, 256) +
+         align_up(2 * nt * 4, 256) + 512;
 }
 
 RouteWork route_carve(void* base, int W, int H) {
   RouteWork w;
   w.W = W;
   w.H = H;
-  size_t n = (size_t)W * H;
+  w.tiles_x = (W + kFT - 1) / kFT;
+  w.tiles_y = (H + kFT - 1) / kFT;
+  const size_t n = (size_t)W * H, nt = (size_t)w.tiles_x * w.tiles_y;
   char* p = (char*)base;
   w.flats = (uint32_t*)p;
   p += align_up(n * 4, 256);
-  w.front = (uint32_t*)p;
-  p += 2 * align_up(n * 4, 256);
+  w.tflat = (uint8_t*)p;
+  p += align_up(nt, 256);
+  w.queued = (int*)p;
+  p += align_up(nt * 4, 256);
+  w.lists = (int*)p;
+  p += align_up(2 * nt * 4, 256);
   w.scal = (unsigned int*)p;
   return w;
+}
+
+// Loads the flat-distance code and elevation of the 8 neighbours (N..NW) of
+// cell (x, y) with independent loads; outside the grid: code INT_MIN.
+__device__ __forceinline__ void gather8(const float* __restrict__ dem, const int* __restrict__ fd,
+                                        int W, int H, int x, int y, int* nf, float* ne) {
+#pragma unroll
+  for (int n = 0; n < 8; n++) {
+    const int nx = x + d8_dx(n), ny = y + d8_dy(n);
+    const bool in = nx >= 0 && ny >= 0 && nx < W && ny < H;
+    const int64_t ni = (int64_t)ny * W + nx;
+    nf[n] = in ? ((volatile const int*)fd)[ni] : (int)0x80000000;
+    ne[n] = in ? dem[ni] : 0.0f;
+  }
 }
 
 // Steepest-descent pass.  flatdist: -1 direction, -2 stream, kFlatInf flat.
@@ -56,118 +82,212 @@ __global__ void d8_kernel(const float* __restrict__ dem, char2* __restrict__ dir
   int dxi = 0, dyi = 0;
   if (x == 0) dxi = -1; else if (x == W - 1) dxi = 1;
   if (y == 0) dyi = -1; else if (y == H - 1) dyi = 1;
+  bool flat = false;
   if (dxi || dyi) {
     dir[i] = make_char2((signed char)dxi, (signed char)dyi);
     fd[i] = -1;
-    return;
-  }
-  const float c = dem[i];
-  if (c == 0.0f) {
-    dir[i] = make_char2(0, 0);
-    fd[i] = -2;
-    return;
-  }
-  float steepest = 0.0f;
-  int sdx = 0, sdy = 0;
-#pragma unroll
-  for (int n = 0; n < 8; n++) {
-    const int dx = d8_dx(n), dy = d8_dy(n);
-    float s = __fsub_rn(c, dem[(int64_t)(y + dy) * W + (x + dx)]);
-    if (s > 0.0f) {
-      if (n & 1) s = __fdiv_rn(s, 1.41421356237309505f);
-      if (s > steepest) { steepest = s; sdx = dx; sdy = dy; }
-    }
-  }
-  if (steepest > 0.0f) {
-    dir[i] = make_char2((signed char)sdx, (signed char)sdy);
-    fd[i] = -1;
   } else {
-    dir[i] = make_char2(0, 0);
-    fd[i] = kFlatInf;
-    unsigned int pos = atomicAdd(&w.scal[R_NFLAT], 1u);
-    w.flats[pos] = (uint32_t)i;
-  }
-}
-
-// Layer 1: flat cells next to a cell with a direction (flatDist -1) whose
-// elevation is <= theirs.
-__global__ void flat_seed_kernel(const float* __restrict__ dem, int* __restrict__ fd,
-                                 RouteWork w) {
-  const unsigned int nf = w.scal[R_NFLAT];
-  const int W = w.W, H = w.H;
-  for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < nf;
-       j += gridDim.x * blockDim.x) {
-    uint32_t c = w.flats[j];
-    int x = (int)(c % (uint32_t)W), y = (int)(c / (uint32_t)W);
-    const float e = dem[c];
-    bool seed = false;
-    for (int n = 0; n < 8 && !seed; n++) {
-      int nx = x + d8_dx(n), ny = y + d8_dy(n);
-      if (nx < 0 || ny < 0 || nx >= W || ny >= H) continue;
-      int64_t ni = (int64_t)ny * W + nx;
-      seed = fd[ni] == -1 && dem[ni] <= e;
-    }
-    if (seed) {
-      // Distances are written after the scan of every flat cell (next kernel)
-      // so that no cell of this kernel sees another's layer-1 mark.
-      unsigned int pos = atomicAdd(&w.scal[R_CNT + 1], 1u);
-      w.front[(size_t)1 * W * H + pos] = c;
-    }
-  }
-}
-
-__global__ void flat_mark_kernel(int* __restrict__ fd, RouteWork w) {
-  const unsigned int n1 = w.scal[R_CNT + 1];
-  const int64_t N = (int64_t)w.W * w.H;
-  for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < n1;
-       j += gridDim.x * blockDim.x)
-    fd[w.front[N + j]] = 1;
-}
-
-// Frontier BFS: layer k -> k+1 over flat cells with elevation >= the
-// frontier cell's.  Persistent, one bounded grid barrier per layer.
-__global__ void __launch_bounds__(kBfsThreads)
-flat_bfs_kernel(const float* __restrict__ dem, int* __restrict__ fd, RouteWork w) {
-  const int W = w.W, H = w.H;
-  const int64_t N = (int64_t)W * H;
-  GridSync gs{w.scal + R_BAR_COUNT, w.scal + R_BAR_GEN, (int*)(w.scal + R_ERR)};
-  volatile unsigned int* vs = w.scal;
-  int k = 1;
-  unsigned long long t0;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
-  while (true) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) vs[R_CNT + (k + 2) % 3] = 0u;
-    const unsigned int n = vs[R_CNT + k % 3];
-    const uint32_t* cur = w.front + (size_t)(k & 1) * N;
-    uint32_t* nxt = w.front + (size_t)((k + 1) & 1) * N;
-    for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < n;
-         j += gridDim.x * blockDim.x) {
-      uint32_t c = cur[j];
-      int x = (int)(c % (uint32_t)W), y = (int)(c / (uint32_t)W);
-      const float e = dem[c];
-      for (int q = 0; q < 8; q++) {
-        int nx = x + d8_dx(q), ny = y + d8_dy(q);
-        if (nx < 0 || ny < 0 || nx >= W || ny >= H) continue;
-        int64_t ni = (int64_t)ny * W + nx;
-        if (fd[ni] == kFlatInf && e <= dem[ni] &&
-            atomicCAS(&fd[ni], kFlatInf, k + 1) == kFlatInf) {
-          unsigned int pos = atomicAdd(&w.scal[R_CNT + (k + 1) % 3], 1u);
-          nxt[pos] = (uint32_t)ni;
+    const float c = dem[i];
+    if (c == 0.0f) {
+      dir[i] = make_char2(0, 0);
+      fd[i] = -2;
+    } else {
+      float steepest = 0.0f;
+      int sdx = 0, sdy = 0;
+#pragma unroll
+      for (int n = 0; n < 8; n++) {
+        const int dx = d8_dx(n), dy = d8_dy(n);
+        float s = __fsub_rn(c, dem[(int64_t)(y + dy) * W + (x + dx)]);
+        // A diagonal drop only shrinks when divided by sqrt(2), so the
+        // (slow, correctly rounded) division is needed only when the
+        // undivided drop already beats the steepest so far.
+        if (s > 0.0f && s > steepest) {
+          if (n & 1) s = __fdiv_rn(s, 1.41421356237309505f);
+          if (s > steepest) { steepest = s; sdx = dx; sdy = dy; }
         }
       }
+      if (steepest > 0.0f) {
+        dir[i] = make_char2((signed char)sdx, (signed char)sdy);
+        fd[i] = -1;
+      } else {
+        dir[i] = make_char2(0, 0);
+        fd[i] = kFlatInf;
+        flat = true;
+      }
+    }
+  }
+  const unsigned int pos = warp_append(&w.scal[R_NFLAT], flat);
+  if (flat) {
+    w.flats[pos] = (uint32_t)i;
+    w.tflat[(y / kFT) * w.tiles_x + x / kFT] = 1;
+  }
+}
+
+// ---- flat distances by tile relaxation ----------------------------------
+// Staged value of a cell for its neighbours: 0 for a cell with a direction
+// (layer 0), the current distance of a flat cell, "infinite" otherwise.
+__device__ __forceinline__ int flat_relay(int code) {
+  return code == -1 ? 0 : (code >= 0 ? code : kFlatInf);
+}
+
+struct FlatSmem {
+  int R[34 * kFRS];      // staged relay values (tile + halo)
+  float E[34 * kFRS];    // staged elevations
+  uint8_t isflat[kFT * 36];
+};
+
+__device__ __forceinline__ void flat_enqueue(const RouteWork& w, int t, int k) {
+  if (!((volatile uint8_t*)w.tflat)[t]) return;  // no flat cell: nothing to do
+  if (atomicMax(&w.queued[t], k) < k) {
+    const unsigned int nt = (unsigned int)(w.tiles_x * w.tiles_y);
+    unsigned int pos = atomicAdd(&w.scal[R_LIST + k % 3], 1u);
+    if (pos < nt) w.lists[(k & 1) * nt + pos] = t;
+    else atomicCAS((int*)(w.scal + R_ERR), 0, 3);  // never: each tile is queued once per pass
+  }
+}
+
+// Relax flat cell (x, y): one more than the least distance among neighbours
+// whose elevation is <= its own.
+__device__ __forceinline__ bool flat_update(FlatSmem& s, int x, int y) {
+  if (!s.isflat[y * 36 + x]) return false;
+  const int b = (y + 1) * kFRS + (x + 1);
+  const float e = s.E[b];
+  int m = kFlatInf;
+#pragma unroll
+  for (int n = 0; n < 8; n++) {
+    const int o = d8_dy(n) * kFRS + d8_dx(n);
+    const int v = s.R[b + o];
+    if (s.E[b + o] <= e && v < m) m = v;
+  }
+  if (m < kFlatInf && m + 1 < s.R[b]) {
+    s.R[b] = m + 1;
+    s.isflat[y * 36 + x] = 3;  // flat and changed
+    return true;
+  }
+  return false;
+}
+
+__device__ void flat_tile(FlatSmem& s, const float* __restrict__ dem, int* fd, const RouteWork& w,
+                          int t, int p, int lane) {
+  const int W = w.W, H = w.H;
+  const int tx = t % w.tiles_x, ty = t / w.tiles_x;
+  const int x0 = tx * kFT, y0 = ty * kFT;
+#pragma unroll 4
+  for (int idx = lane; idx < 34 * 34; idx += 32) {
+    const int hy = idx / 34, hx = idx - hy * 34;
+    const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
+    int code = -2;
+    float e = 0.0f;
+    if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+      const int64_t i = (int64_t)gy * W + gx;
+      code = ((volatile int*)fd)[i];
+      e = dem[i];
+    }
+    s.R[hy * kFRS + hx] = flat_relay(code);
+    s.E[hy * kFRS + hx] = e;
+    if (hx >= 1 && hx <= kFT && hy >= 1 && hy <= kFT)
+      s.isflat[(hy - 1) * 36 + hx - 1] = (code == kFlatInf || code >= 1) ? 1 : 0;
+  }
+  __syncwarp();
+  auto smear = [](unsigned int m) { return m | (m << 1) | (m >> 1); };
+  bool capped = true;
+  unsigned int next_rows = 0xffffffffu;
+  for (int round = 0; round < 64; round++) {
+    unsigned int pend = next_rows, cch = 0;
+    for (int k = 0; k < kFT; k++) {
+      const int d = k, u = kFT - 1 - k;
+      unsigned int b1 = 0, b2 = 0;
+      if ((pend >> d) & 1u) b1 = __ballot_sync(0xffffffffu, flat_update(s, lane, d));
+      if ((pend >> u) & 1u) b2 = __ballot_sync(0xffffffffu, flat_update(s, lane, u));
+      if (b1) { cch |= b1; pend |= smear(1u << d); }
+      if (b2) { cch |= b2; pend |= smear(1u << u); }
+      __syncwarp();
+    }
+    unsigned int pendc = smear(cch), rch2 = 0;
+    for (int k = 0; k < kFT; k++) {
+      const int l = k, r = kFT - 1 - k;
+      unsigned int b1 = 0, b2 = 0;
+      if ((pendc >> l) & 1u) b1 = __ballot_sync(0xffffffffu, flat_update(s, l, lane));
+      if ((pendc >> r) & 1u) b2 = __ballot_sync(0xffffffffu, flat_update(s, r, lane));
+      if (b1) { rch2 |= b1; pendc |= smear(1u << l); }
+      if (b2) { rch2 |= b2; pendc |= smear(1u << r); }
+      __syncwarp();
+    }
+    if (!rch2) { capped = false; break; }
+    next_rows = smear(rch2);
+  }
+  unsigned int sides = 0;
+  for (int idx = lane; idx < kFT * kFT; idx += 32) {
+    const int y = idx >> 5, x = idx & 31;
+    if (s.isflat[y * 36 + x] == 3) {
+      fd[(int64_t)(y0 + y) * W + (x0 + x)] = s.R[(y + 1) * kFRS + (x + 1)];
+      if (x == 0) sides |= 1;
+      if (x == kFT - 1) sides |= 2;
+      if (y == 0) sides |= 4;
+      if (y == kFT - 1) sides |= 8;
+      if (x == 0 && y == 0) sides |= 16;
+      if (x == kFT - 1 && y == 0) sides |= 32;
+      if (x == 0 && y == kFT - 1) sides |= 64;
+      if (x == kFT - 1 && y == kFT - 1) sides |= 128;
+    }
+  }
+  sides = __reduce_or_sync(0xffffffffu, sides);
+  if (lane < 9) {
+    int dx = 0, dy = 0;
+    bool want = false;
+    switch (lane) {
+      case 0: want = capped; break;
+      case 1: dx = -1; want = sides & 1; break;
+      case 2: dx = 1; want = sides & 2; break;
+      case 3: dy = -1; want = sides & 4; break;
+      case 4: dy = 1; want = sides & 8; break;
+      case 5: dx = -1; dy = -1; want = sides & 16; break;
+      case 6: dx = 1; dy = -1; want = sides & 32; break;
+      case 7: dx = -1; dy = 1; want = sides & 64; break;
+      case 8: dx = 1; dy = 1; want = sides & 128; break;
+    }
+    const int nx = tx + dx, ny = ty + dy;
+    if (want && nx >= 0 && ny >= 0 && nx < w.tiles_x && ny < w.tiles_y)
+      flat_enqueue(w, ny * w.tiles_x + nx, p + 1);
+  }
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(kFWarps * 32, 1)
+flat_relax_kernel(const float* __restrict__ dem, int* fd, RouteWork w) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  FlatSmem& s = reinterpret_cast<FlatSmem*>(smraw)[warp];
+  const int ntiles = w.tiles_x * w.tiles_y;
+  const int gwarp = blockIdx.x * kFWarps + warp, nwarps = gridDim.x * kFWarps;
+  GridSync gs{w.scal + R_BAR_COUNT, w.scal + R_BAR_GEN, (int*)(w.scal + R_ERR)};
+  volatile unsigned int* vs = w.scal;
+  unsigned long long t0;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  int p = 2;  // queued[] starts at 0
+  bool full = true;
+  while (true) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) vs[R_LIST + (p + 2) % 3] = 0u;
+    const int n = full ? ntiles : (int)vs[R_LIST + p % 3];
+    const int* list = w.lists + (p & 1) * ntiles;
+    for (int i = gwarp; i < n; i += nwarps) {
+      const int t = full ? i : list[i];
+      if (full && !w.tflat[t]) continue;
+      flat_tile(s, dem, fd, w, t, p, lane);
     }
     if (!grid_barrier(gs, gridDim.x)) break;
-    if (vs[R_CNT + (k + 1) % 3] == 0u) break;
-    if (k > 1 << 28) {
+    if (vs[R_LIST + (p + 1) % 3] == 0u) break;
+    if (p > (1 << 24)) {
       if (threadIdx.x == 0) atomicCAS((int*)(w.scal + R_ERR), 0, 2);
       break;
     }
-    k++;
+    full = false;
+    p++;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     unsigned long long t1;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
-    vs[R_LAYERS] = (unsigned int)k;
+    vs[R_PASSES] = (unsigned int)(p - 1);
     vs[R_US_BFS] = (unsigned int)((t1 - t0) / 1000);
   }
 }
@@ -186,13 +306,13 @@ __global__ void flat_dir_kernel(const float* __restrict__ dem, char2* __restrict
     int x = (int)(c % (uint32_t)W), y = (int)(c / (uint32_t)W);
     const float e = dem[c];
     const int want = d == 1 ? -1 : d - 1;
+    int nf[8];
+    float ne[8];
+    gather8(dem, fd, W, H, x, y, nf, ne);
     int got = -1;
-    for (int n = 0; n < 8; n++) {
-      int nx = x + d8_dx(n), ny = y + d8_dy(n);
-      if (nx < 0 || ny < 0 || nx >= W || ny >= H) continue;
-      int64_t ni = (int64_t)ny * W + nx;
-      if (fd[ni] == want && dem[ni] <= e) got = n;
-    }
+#pragma unroll
+    for (int n = 0; n < 8; n++)
+      if (nf[n] == want && ne[n] <= e) got = n;
     if (got >= 0) dir[c] = make_char2((signed char)d8_dx(got), (signed char)d8_dy(got));
   }
 }
@@ -211,37 +331,36 @@ __global__ void route_scalars_kernel(unsigned int* s) {
   for (int i = threadIdx.x; i < R_SIZE; i += blockDim.x) s[i] = 0u;
 }
 
-static int coop_blocks_bfs() {
-  static int blocks = 0;
-  if (!blocks) {
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, flat_bfs_kernel, kBfsThreads, 0);
-    blocks = std::max(1, std::min(per, 2)) * sms;
-  }
-  return blocks;
-}
-
 cageo_status route_run(const float* filled, int8_t* dir, int* fd, const RouteWork& w,
                        cudaStream_t s) {
+  const size_t nt = (size_t)w.tiles_x * w.tiles_y;
   route_scalars_kernel<<<1, 128, 0, s>>>(w.scal);
+  CAGEO_CUDA(cudaMemsetAsync(w.tflat, 0, nt, s));
+  CAGEO_CUDA(cudaMemsetAsync(w.queued, 0, nt * 4, s));
   dim3 b(32, 8), g((w.W + 31) / 32, (w.H + 7) / 8);
   d8_kernel<<<g, b, 0, s>>>(filled, (char2*)dir, fd, w);
   CAGEO_CUDA(cudaGetLastError());
-  int sms = 0, dev = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const unsigned lb = (unsigned)sms * 8;
-  flat_seed_kernel<<<lb, 256, 0, s>>>(filled, fd, w);
-  flat_mark_kernel<<<lb, 256, 0, s>>>(fd, w);
-  CAGEO_CUDA(cudaGetLastError());
+  static int coop = 0;
+  const size_t smem = sizeof(FlatSmem) * kFWarps;
+  if (!coop) {
+    CAGEO_CUDA(cudaFuncSetAttribute(flat_relax_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, flat_relax_kernel, kFWarps * 32, smem);
+    coop = std::max(1, per) * sms;
+  }
   const float* f = filled;
   int* fdp = fd;
   RouteWork wc = w;
   void* params[] = {(void*)&f, (void*)&fdp, (void*)&wc};
-  CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)flat_bfs_kernel, dim3(coop_blocks_bfs()),
-                                         dim3(kBfsThreads), params, 0, s));
+  CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)flat_relax_kernel, dim3(coop),
+                                         dim3(kFWarps * 32), params, smem, s));
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const unsigned lb = (unsigned)sms * 8;
   flat_dir_kernel<<<lb, 256, 0, s>>>(filled, (char2*)dir, fd, w);
   flat_final_kernel<<<lb, 256, 0, s>>>(fd, w);
   CAGEO_CUDA(cudaGetLastError());
@@ -252,12 +371,12 @@ cageo_status route_check_status(const RouteWork& w, int64_t* stats) {
   unsigned int h[R_SIZE];
   CAGEO_CUDA(cudaMemcpy(h, w.scal, sizeof(h), cudaMemcpyDeviceToHost));
   if (stats) {
-    stats[0] = h[R_LAYERS];
+    stats[0] = h[R_PASSES];
     stats[1] = h[R_NFLAT];
     stats[2] = h[R_US_BFS];
   }
   if (h[R_ERR]) {
-    set_error("flow routing: flat-surface BFS hit a wait or layer limit");
+    set_error("flow routing: flat-surface relaxation hit a wait or pass limit");
     return CAGEO_ERR_NO_CONVERGENCE;
   }
   return CAGEO_OK;

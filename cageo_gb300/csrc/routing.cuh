@@ -9,20 +9,24 @@ namespace cageo {
 
 struct RouteWork {
   int W = 0, H = 0;
+  int tiles_x = 0, tiles_y = 0;
   uint32_t* flats = nullptr;     // W*H: flat cells
-  uint32_t* front = nullptr;     // 2 * W*H: BFS frontiers
+  uint8_t* tflat = nullptr;      // per 32x32 tile: holds a flat cell
+  int* queued = nullptr;         // per tile: last pass it was queued for
+  int* lists = nullptr;          // 2 * ntiles: tile worklists
   unsigned int* scal = nullptr;  // counters, barrier, error
 };
 size_t route_workspace_bytes(int W, int H);
 RouteWork route_carve(void* base, int W, int H);
 cageo_status route_run(const float* filled, int8_t* dir, int* flatdist,
                        const RouteWork& w, cudaStream_t s);
-// stats (3 entries, may be null): BFS layers, flat cells, BFS microseconds.
+// stats (3 entries, may be null): flat relaxation passes, flat cells,
+// microseconds of the flat relaxation.
 cageo_status route_check_status(const RouteWork& w, int64_t* stats);
 
 struct TraceWork {
   int W = 0, H = 0;
-  long long* state = nullptr;    // W*H: packed pointer / label
+  int* state = nullptr;          // W*H: packed pointer / label
   unsigned int* scal = nullptr;
 };
 size_t trace_workspace_bytes(int W, int H);

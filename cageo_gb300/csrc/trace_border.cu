@@ -6,9 +6,9 @@
 // it leaves the grid (OUTSIDE) or steps onto a stream cell s (label
 // (int)(-streams[s])).  The reference walks each path serially with caching;
 // the label of a cell depends only on where its path ends, so here every
-// cell holds a packed state -- "points to cell p" or "resolved to label l"
-// -- and repeatedly jumps p <- state[p] (pointer doubling) until all are
-// resolved: O(log path length) grid passes.  A cell without a direction
+// cell holds a packed 32-bit state -- "points to cell p" or "resolved to
+// label l" -- and repeatedly jumps p <- state[p] (pointer doubling) until
+// all are resolved: O(log path length) grid passes.  A cell without a direction
 // (0,0) is a dead end: the reference's walk never terminates there, leaves
 // the path at 0 and its connect pass then copies the label of cell 0; such
 // cells and label-0 terminals take the label of cell 0 here too.  (The
@@ -26,68 +26,85 @@
 
 namespace cageo {
 
-constexpr long long kResolved = 1LL << 32;
-constexpr int kStuck = (int)0x80000000;  // dead end marker, never a real label
+// Packed per-cell state (int32): >= 0 points to a cell; < 0 is resolved,
+// holding code(label) = label - 1 (labels are <= 0, so label 0 stays
+// negative); kStuckCode marks a dead end.  Stream values whose negation
+// does not fit (|streams| >= 2^31 - 1) are outside the supported range.
+constexpr int kStuckCode = (int)0x80000000;
+constexpr int kJumpThreads = 256;
 enum : int { T_ERR = 2, T_ACTIVE = 3, T_JUMPS = 6, T_BAR_COUNT = kBarCountSlot,
              T_BAR_GEN = kBarGenSlot, T_SIZE = kScalarSlots };
-constexpr int kJumpThreads = 512;
+
+__device__ __forceinline__ int label_code(int label) { return label - 1; }
 
 size_t trace_workspace_bytes(int W, int H) {
-  return align_up((size_t)W * H * 8, 256) + 512;
+  const size_t n = (size_t)W * H;
+  return align_up(n * 4, 256) + 512;
 }
 
 TraceWork trace_carve(void* base, int W, int H) {
   TraceWork w;
   w.W = W;
   w.H = H;
-  w.state = (long long*)base;
-  w.scal = (unsigned int*)((char*)base + align_up((size_t)W * H * 8, 256));
+  const size_t n = (size_t)W * H;
+  char* p = (char*)base;
+  w.state = (int*)p;
+  p += align_up(n * 4, 256);
+  w.scal = (unsigned int*)p;
   return w;
-}
-
-__device__ inline long long resolved(int label) {
-  return kResolved | (long long)(unsigned int)label;
 }
 
 __global__ void trace_init_kernel(const char2* __restrict__ dir,
                                   const float* __restrict__ streams,
-                                  long long* __restrict__ st, int W, int H) {
+                                  int* __restrict__ st, int W, int H) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)W * H) return;
-  if (streams[i] >= 0.0f) { st[i] = resolved(kLake); return; }
+  if (streams[i] >= 0.0f) { st[i] = label_code(kLake); return; }
   int x = (int)(i % W), y = (int)(i / W);
   char2 d = dir[i];
   int nx = x + d.x, ny = y + d.y;
-  if (nx < 0 || nx >= W || ny < 0 || ny >= H) { st[i] = resolved(kOutside); return; }
-  if (d.x == 0 && d.y == 0) { st[i] = resolved(kStuck); return; }
+  if (nx < 0 || nx >= W || ny < 0 || ny >= H) { st[i] = label_code(kOutside); return; }
+  if (d.x == 0 && d.y == 0) { st[i] = kStuckCode; return; }
   int64_t n = (int64_t)ny * W + nx;
   float s = streams[n];
-  if (s >= 0.0f) { st[i] = resolved((int)(-s)); return; }
-  st[i] = n;
+  if (s >= 0.0f) { st[i] = label_code((int)(-s)); return; }
+  st[i] = (int)n;
 }
 
 // Pointer doubling in place (reading a neighbour's newer state only speeds
-// convergence).  Persistent; one bounded grid barrier per pass.
-__global__ void __launch_bounds__(kJumpThreads) trace_jump_kernel(long long* st, TraceWork w) {
+// convergence).  Each thread takes 4 cells per iteration so their dependent
+// load pairs overlap.  Persistent; one bounded grid barrier per pass.
+__global__ void __launch_bounds__(kJumpThreads, 8) trace_jump_kernel(int* st, TraceWork w) {
   const int64_t N = (int64_t)w.W * w.H;
   GridSync gs{w.scal + T_BAR_COUNT, w.scal + T_BAR_GEN, (int*)(w.scal + T_ERR)};
   volatile unsigned int* vs = w.scal;
+  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int pass = 0;
   while (true) {
     // Slot pass%3 is written during this pass and read after its barrier;
     // slot (pass+1)%3 was last read before the previous barrier.
     if (blockIdx.x == 0 && threadIdx.x == 0) vs[T_ACTIVE + (pass + 1) % 3] = 0u;
-    unsigned int active = 0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N;
-         i += (int64_t)gridDim.x * blockDim.x) {
-      long long s = st[i];
-      if (s & kResolved) continue;
-      long long t = ((volatile long long*)st)[s];
-      st[i] = t;
-      if (!(t & kResolved)) active = 1;
+    bool active = false;
+    for (int64_t base = tid; base < N; base += 4 * nthreads) {
+      int s[4], t[4];
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const int64_t i = base + k * nthreads;
+        s[k] = i < N ? st[i] : -1;
+      }
+#pragma unroll
+      for (int k = 0; k < 4; k++) t[k] = s[k] >= 0 ? ((volatile int*)st)[s[k]] : s[k];
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        if (s[k] >= 0) {
+          st[base + k * nthreads] = t[k];
+          active |= t[k] >= 0;
+        }
+      }
     }
-    active = __reduce_or_sync(0xffffffffu, active);
-    if ((threadIdx.x & 31) == 0 && active) atomicOr(&w.scal[T_ACTIVE + pass % 3], 1u);
+    if (__any_sync(0xffffffffu, active) && (threadIdx.x & 31) == 0)
+      atomicOr(&w.scal[T_ACTIVE + pass % 3], 1u);
     if (!grid_barrier(gs, gridDim.x)) break;
     if (vs[T_ACTIVE + pass % 3] == 0u) break;
     if (++pass > 64) {  // 2^64 exceeds any path length: a cycle
@@ -99,14 +116,16 @@ __global__ void __launch_bounds__(kJumpThreads) trace_jump_kernel(long long* st,
 }
 
 // Labels; dead ends and label-0 terminals take cell 0's label.
-__global__ void trace_final_kernel(const long long* __restrict__ st, int* __restrict__ label,
+__global__ void trace_final_kernel(const int* __restrict__ st, int* __restrict__ label,
                                    int64_t n) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  int l = (int)(unsigned int)st[i];
-  if (l >= 0 || l == kStuck) {
-    int l0 = (int)(unsigned int)st[0];
-    l = (l0 == kStuck || l0 >= 0) ? 0 : l0;
+  const int c = st[i];
+  int l = c == kStuckCode ? 0 : c + 1;
+  if (l >= 0) {
+    const int c0 = st[0];
+    const int l0 = c0 == kStuckCode ? 0 : c0 + 1;
+    l = l0 >= 0 ? 0 : l0;
   }
   label[i] = l;
 }
@@ -130,7 +149,7 @@ cageo_status trace_run(const int8_t* dir, const float* streams, int* label,
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trace_jump_kernel, kJumpThreads, 0);
     coop = std::max(1, per) * sms;
   }
-  long long* stp = w.state;
+  int* stp = w.state;
   TraceWork wc = w;
   void* params[] = {(void*)&stp, (void*)&wc};
   CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)trace_jump_kernel, dim3(coop),
