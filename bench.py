@@ -45,6 +45,15 @@ FALLBACK_HBM = 6800.0
 # Algorithmic bytes per cell of each stage (unfused compulsory I/O).
 STAGE_BYTES = {"noise": 4, "front": 40, "fill": 8, "route": 5, "trace": 6, "border": 12}
 PIPE_BYTES = 75
+# DRAM bytes per cell moved by one pit fill (both flood launches), from the
+# ncu capture summarised in profiles/fill_flood_plain4096.md (4096^2 case,
+# 1702 MB for 16.8 M cells), applied per cell to the benchmark grid.
+FILL_TRAFFIC_PER_CELL = 1702.2e6 / (4096 * 4096)
+# Kernels per realization on the graph path: fill 6 (scalars, init, two
+# floods, classify, final), noise 1, front 1, routing 5 (scalars, d8, flat
+# relaxation, flat directions, flat final), tracing 4 (scalars, init, jump,
+# final), border 1, realization end 1.
+KERNELS_PER_REALIZATION = 19
 
 
 def peak_hbm():
@@ -281,17 +290,17 @@ def main():
         "stage_ms": stage_ms,
         "fill_stats": stats,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
-                     "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                     "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": FILL_TRAFFIC_PER_CELL * N if dom == "fill" else None,
+                     "traffic_note": "DRAM bytes of one fill, ncu at 4096^2 scaled by cells"
+                     if dom == "fill" else None,
                      "algorithmic_bytes_per_cell": STAGE_BYTES[dom], "peak_kind": peak_kind},
         "pipeline_roofline": {"achieved": value / world * N * PIPE_BYTES / 1e9, "peak": hbm,
                               "frac": value / world * N * PIPE_BYTES / 1e9 / hbm,
                               "bytes_per_cell": PIPE_BYTES},
         "clocks": clocks.summary(),
     }
-    # Kernel launches per realization: noise, front, fill (scalars, memset,
-    # init, 2 floods, classify, final), route (scalars, d8, seed, mark, bfs,
-    # dir, final), trace (scalars, init, jump, final), border, end.
-    line["gpu_launches"] = args.steps * 21
+    line["gpu_launches"] = args.steps * KERNELS_PER_REALIZATION
     if not args.no_cpu_baseline:
         rate, threads, sec = cpu_rate(dem, streams, p, args.cpu_steps, 50_000)
         line["cpu_baseline"] = {"value": rate, "unit": "realizations/s", "cores": threads,
