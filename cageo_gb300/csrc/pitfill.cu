@@ -60,6 +60,8 @@ enum : int {
   S_KCYC_LOAD = 25,  // kilo-cycles (summed over tile visits) staging tiles
   S_KCYC_SWEEP = 26, // kilo-cycles sweeping
   S_KCYC_STORE = 27, // kilo-cycles writing back and queueing
+  S_PASS_US_A = 36,  // 24 slots: microseconds of flood A's first passes
+  S_PASS_US_B = 68,  // 24 slots: the same for flood B (phases included)
   S_BAR_COUNT = kBarCountSlot,
   S_BAR_GEN = kBarGenSlot,
   S_SIZE = kScalarSlots
@@ -72,17 +74,19 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 constexpr int kTile = 32;
-constexpr int kWarps = 12;  // one 384-thread block per SM (12 x 14 KB smem)
+constexpr int kWarps = 16;  // one 512-thread block per SM (16 x 10 KB smem)
 constexpr int kRS = 35;           // relay row stride (34 used)
 constexpr int kWS = 33;           // W/q row stride
 constexpr int kFS = 36;           // flag row stride (bytes)
 constexpr int kMaxRounds = 64;
 constexpr int kMaxPasses = 1000000;
 
+// Per-warp staged tile: relay values with halo, W and flags of the tile's
+// own cells.  q is static during a flood and is read through the read-only
+// cache instead of being staged.
 struct WarpSmem {
   float R[34 * kRS];
   float Wv[kTile * kWS];
-  float Qv[kTile * kWS];
   uint8_t F[kTile * kFS];
 };
 
@@ -90,7 +94,7 @@ size_t fill_workspace_bytes(int W, int H) {
   size_t n = (size_t)W * H;
   size_t nt = (size_t)((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile);
   return align_up(n, 256) + align_up(nt * 4, 256) + align_up(2 * nt * 4, 256) +
-         align_up(nt, 256) + 3 * align_up(n * 4, 256) + 512;
+         3 * align_up(nt, 256) + 3 * align_up(n * 4, 256) + 512;
 }
 
 FillWork fill_carve(void* base, int W, int H) {
@@ -108,6 +112,10 @@ FillWork fill_carve(void* base, int W, int H) {
   w.lists = (int*)p;
   p += align_up(2 * nt * 4, 256);
   w.tdone = (uint8_t*)p;
+  p += align_up(nt, 256);
+  w.tseed = (uint8_t*)p;
+  p += align_up(nt, 256);
+  w.tconv = (uint8_t*)p;
   p += align_up(nt, 256);
   w.cand = (uint32_t*)p;
   p += align_up(n * 4, 256);
@@ -151,11 +159,12 @@ __device__ __forceinline__ void enqueue(const FillWork& w, int t, int k) {
 // dropped below its own q (FBELOW) is final in both floods: its value is q
 // and its relay can no longer change.
 template <int MODE>
-__device__ __forceinline__ bool update_cell(WarpSmem& s, int x, int y, float m) {
+__device__ __forceinline__ bool update_cell(WarpSmem& s, const float* __restrict__ qt, int W,
+                                            int x, int y, float m) {
   uint8_t f = s.F[y * kFS + x];
   if (f & (FNODATA | FOUTLET | FBELOW)) return false;
   float w = s.Wv[y * kWS + x];
-  float qv = s.Qv[y * kWS + x];
+  float qv = __ldg(qt + (int64_t)y * W + x);
   float nw = fminf(w, fmaxf(qv, m));
   uint8_t nf = f | ((m < qv) ? FBELOW : 0);
   if (nw != w || nf != f) {
@@ -197,12 +206,12 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
     s.R[hy * kRS + hx] = relay<MODE>(wv, fv, qv);
     if (hx >= 1 && hx <= kTile && hy >= 1 && hy <= kTile) {
       s.Wv[(hy - 1) * kWS + hx - 1] = wv;
-      s.Qv[(hy - 1) * kWS + hx - 1] = qv;
       s.F[(hy - 1) * kFS + hx - 1] = fv;
     }
   }
   __syncwarp();
   const long long c1 = clock64();
+  const float* qt = a.q + (int64_t)y0 * W + x0;  // q of the tile's cell (0, 0)
   // Sweeps.  A cell needs re-evaluating only after one of its 8 neighbours
   // changed, so each phase carries warp-uniform masks of the rows (vertical
   // phase) or columns (horizontal phase) to evaluate: all rows first, then
@@ -212,37 +221,42 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
   // neighbour of those changes) and vice versa, so a horizontal phase
   // without a change leaves a fixpoint.
   auto smear = [](unsigned int m) { return m | (m << 1) | (m >> 1); };
+  // A tile that converged on an earlier visit is a fixpoint for its old halo:
+  // only its border rows and columns need evaluating first.
+  const bool revisit = w.tconv[t] != 0;
   bool capped = true;
   int rounds = kMaxRounds;
-  unsigned int next_rows = 0xffffffffu;  // rows to evaluate in the next vertical phase
+  unsigned int next_rows = revisit ? 0x80000001u : 0xffffffffu;
+  unsigned int first_cols = revisit ? 0x80000001u : 0u;
   for (int round = 0; round < kMaxRounds; round++) {
-    unsigned int pend = next_rows, cch = 0;
+    unsigned int pend = next_rows, cch = first_cols;
+    first_cols = 0;
     for (int k = 0; k < kTile; k++) {
       const int d = k, u = kTile - 1 - k;
       unsigned int b1 = 0, b2 = 0;
       if ((pend >> d) & 1u) {
         const float m = nbr_min(s, lane, d);
-        b1 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, lane, d, m));
+        b1 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, qt, W, lane, d, m));
       }
       if ((pend >> u) & 1u) {
         const float m = nbr_min(s, lane, u);
-        b2 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, lane, u, m));
+        b2 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, qt, W, lane, u, m));
       }
       if (b1) { cch |= b1; pend |= smear(1u << d); }
       if (b2) { cch |= b2; pend |= smear(1u << u); }
       __syncwarp();
     }
-    unsigned int pendc = smear(cch), rch2 = 0;
+    unsigned int pendc = smear(cch) | cch, rch2 = 0;
     for (int k = 0; k < kTile; k++) {
       const int l = k, r = kTile - 1 - k;
       unsigned int b1 = 0, b2 = 0;
       if ((pendc >> l) & 1u) {
         const float m = nbr_min(s, l, lane);
-        b1 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, l, lane, m));
+        b1 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, qt, W, l, lane, m));
       }
       if ((pendc >> r) & 1u) {
         const float m = nbr_min(s, r, lane);
-        b2 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, r, lane, m));
+        b2 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, qt, W, r, lane, m));
       }
       if (b1) { rch2 |= b1; pendc |= smear(1u << l); }
       if (b2) { rch2 |= b2; pendc |= smear(1u << r); }
@@ -253,6 +267,7 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
   }
   const long long c2 = clock64();
   if (lane == 0) {
+    w.tconv[t] = capped ? 0 : 1;
     atomicAdd(&w.scal[MODE == 0 ? S_TILES_A : S_TILES_B], 1u);
     atomicAdd(&w.scal[MODE == 0 ? S_ROUNDS_A : S_ROUNDS_B], (unsigned int)rounds);
   }
@@ -358,8 +373,18 @@ fill_flood_kernel(FloodArgs a) {
     if (blockIdx.x == 0 && threadIdx.x == 0) vs[S_LIST + (p + 2) % 3] = 0u;
     int n = full ? ntiles : (int)vs[S_LIST + p % 3];
     const int* list = w.lists + (p & 1) * ntiles;
-    for (int i = gwarp; i < n; i += nwarps) process_tile<MODE>(s, a, full ? i : list[i], p, lane);
+    for (int i = gwarp; i < n; i += nwarps) {
+      // The first pass starts from outlets only: a tile without a relaying
+      // outlet cannot change before a neighbour does, which queues it.
+      if (full && !w.tseed[i]) continue;
+      process_tile<MODE>(s, a, full ? i : list[i], p, lane);
+    }
     if (!grid_barrier(gs, nblocks)) break;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && p - p0 < 24) {
+      static_assert(S_PASS_US_A + 24 <= kBarGenSlot && S_PASS_US_B + 24 <= kScalarSlots, "slots");
+      const unsigned long long tn = global_ns();
+      vs[(MODE == 0 ? S_PASS_US_A : S_PASS_US_B) + (p - p0)] = (unsigned int)((tn - t_start) / 1000);
+    }
     if (p - p0 > kMaxPasses) {
       if (threadIdx.x == 0) atomicCAS((int*)(w.scal + S_ERR), 0, 2);
       break;
@@ -376,18 +401,41 @@ fill_flood_kernel(FloodArgs a) {
       if (!cand_built) {
         t_conv = global_ns();
         if (blockIdx.x == 0 && threadIdx.x == 0) vs[S_PASSES_B] = (unsigned int)(p - p0 + 1);
-        for (int64_t i = tid0; i < ncell; i += tstride) {
-          uint8_t f = w.flags[i];
-          if (f & (FNODATA | FOUTLET)) continue;
-          const float wa = __uint_as_float(w.aux[i]);
-          const bool unsure = wa != a.Wg[i] ||
-                              ((f & FNONPASS) && (((f & FBELOWA) != 0) != ((f & FBELOW) != 0)));
-          if (unsure) {
-            w.flags[i] = f | FUNSURE;
-            w.aux[i] = (uint32_t)i;
+        // Four cells per thread and iteration (independent loads); the
+        // arrays are 256-byte aligned so the vector loads are aligned.
+        for (int64_t b4 = tid0 * 4; b4 < ncell; b4 += tstride * 4) {
+          uint8_t fv[4];
+          float wav[4], wbv[4];
+          if (b4 + 4 <= ncell) {
+            const uchar4 f4 = *reinterpret_cast<const uchar4*>(w.flags + b4);
+            const uint4 a4 = *reinterpret_cast<const uint4*>(w.aux + b4);
+            const float4 w4 = *reinterpret_cast<const float4*>(a.Wg + b4);
+            fv[0] = f4.x; fv[1] = f4.y; fv[2] = f4.z; fv[3] = f4.w;
+            wav[0] = __uint_as_float(a4.x); wav[1] = __uint_as_float(a4.y);
+            wav[2] = __uint_as_float(a4.z); wav[3] = __uint_as_float(a4.w);
+            wbv[0] = w4.x; wbv[1] = w4.y; wbv[2] = w4.z; wbv[3] = w4.w;
+          } else {
+            for (int k = 0; k < 4; k++) {
+              const bool in = b4 + k < ncell;
+              fv[k] = in ? w.flags[b4 + k] : FNODATA;
+              wav[k] = in ? __uint_as_float(w.aux[b4 + k]) : 0.0f;
+              wbv[k] = in ? a.Wg[b4 + k] : 0.0f;
+            }
           }
-          const unsigned int pos = warp_append(&w.scal[S_CAND], unsure);
-          if (unsure) w.cand[pos] = (uint32_t)i;
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            const uint8_t f = fv[k];
+            const bool unsure = !(f & (FNODATA | FOUTLET)) &&
+                                (wav[k] != wbv[k] ||
+                                 ((f & FNONPASS) && (((f & FBELOWA) != 0) != ((f & FBELOW) != 0))));
+            const int64_t i = b4 + k;
+            if (unsure) {
+              w.flags[i] = f | FUNSURE;
+              w.aux[i] = (uint32_t)i;
+            }
+            const unsigned int pos = warp_append(&w.scal[S_CAND], unsure);
+            if (unsure) w.cand[pos] = (uint32_t)i;
+          }
         }
         if (!grid_barrier(gs, nblocks)) break;
         const unsigned int nu = vs[S_CAND];
@@ -444,6 +492,7 @@ fill_flood_kernel(FloodArgs a) {
         if (a.Wg[c] < kInf) {
           // The cell now relays: every tile whose halo holds it must rerun.
           int cx = (int)(c % (uint32_t)w.W), cy = (int)(c / (uint32_t)w.W);
+          w.tconv[(cy / kTile) * w.tiles_x + cx / kTile] = 0;  // its neighbours inside must rerun
           int tx0 = max(cx - 1, 0) / kTile, tx1 = min(cx + 1, w.W - 1) / kTile;
           int ty0 = max(cy - 1, 0) / kTile, ty1 = min(cy + 1, w.H - 1) / kTile;
           for (int ty = ty0; ty <= ty1; ty++)
@@ -473,7 +522,8 @@ fill_flood_kernel(FloodArgs a) {
 
 __global__ void fill_init_kernel(const float* __restrict__ q, float* __restrict__ Wg,
                                  uint8_t* __restrict__ F, const unsigned int* minslot,
-                                 int W, int H, float nodata) {
+                                 uint8_t* __restrict__ tseed, int tiles_x, int W, int H,
+                                 float nodata) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)W * H) return;
   const float minE = ordered_to_float(*minslot);
@@ -488,6 +538,7 @@ __global__ void fill_init_kernel(const float* __restrict__ q, float* __restrict_
   }
   F[i] = f;
   Wg[i] = (f & (FNODATA | FOUTLET)) ? qv : kInf;
+  if ((f & FOUTLET) && !(f & FNONPASS)) tseed[(y / kTile) * tiles_x + x / kTile] = 1;
 }
 
 // Between the floods: keep flood A's result (lower bound) in aux and
@@ -568,16 +619,20 @@ cageo_status fill_run(const float* q, float* filled, const FillWork& w, float no
                       cudaStream_t s) {
   const int64_t n = (int64_t)w.W * w.H;
   const unsigned blocks = (unsigned)((n + 255) / 256);
-  fill_init_kernel<<<blocks, 256, 0, s>>>(q, filled, w.flags, w.scal + S_MIN, w.W, w.H, nodata);
+  const size_t nt = (size_t)w.tiles_x * w.tiles_y;
+  CAGEO_CUDA(cudaMemsetAsync(w.tseed, 0, nt, s));
+  fill_init_kernel<<<blocks, 256, 0, s>>>(q, filled, w.flags, w.scal + S_MIN, w.tseed,
+                                          w.tiles_x, w.W, w.H, nodata);
   CAGEO_CUDA(cudaGetLastError());
   FloodArgs a{q, filled, w};
-  const size_t nt = (size_t)w.tiles_x * w.tiles_y;
   CAGEO_CUDA(cudaMemsetAsync(w.tdone, 0, nt, s));
+  CAGEO_CUDA(cudaMemsetAsync(w.tconv, 0, nt, s));
   cageo_status st = launch_flood<0>(a, s);
   if (st) return st;
   fill_classify_kernel<<<blocks, 256, 0, s>>>(filled, w.flags, w.aux, w.scal, n);
   CAGEO_CUDA(cudaGetLastError());
   CAGEO_CUDA(cudaMemsetAsync(w.tdone, 0, nt, s));
+  CAGEO_CUDA(cudaMemsetAsync(w.tconv, 0, nt, s));
   st = launch_flood<1>(a, s);
   if (st) return st;
   fill_final_kernel<<<blocks, 256, 0, s>>>(q, filled, n);

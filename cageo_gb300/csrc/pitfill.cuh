@@ -16,6 +16,8 @@ struct FillWork {
   int* queued = nullptr;         // ntiles: last pass a tile was queued for
   int* lists = nullptr;          // 2 * ntiles: tile worklists (double buffer)
   uint8_t* tdone = nullptr;      // ntiles: 1 once every cell of the tile is final
+  uint8_t* tseed = nullptr;      // ntiles: tile holds a relaying outlet
+  uint8_t* tconv = nullptr;      // ntiles: tile converged on its last visit
   uint32_t* cand = nullptr;      // W*H: list of undecided cells of the phases
   uint32_t* aux = nullptr;       // W*H: flood A's result, then component labels
   uint32_t* cmin = nullptr;      // W*H: per-component phase minima (at roots)

@@ -33,8 +33,7 @@ constexpr int kFRS = 35;         // staged row stride
 size_t route_workspace_bytes(int W, int H) {
   const size_t n = (size_t)W * H;
   const size_t nt = (size_t)((W + kFT - 1) / kFT) * ((H + kFT - 1) / kFT);
-  return align_up(n * 4, 256) + align_up(nt, 256) + align_up(nt * 4, 256) +
-         align_up(2 * nt * 4, 256) + 512;
+  return align_up(nt, 256) + align_up(nt * 4, 256) + align_up(2 * nt * 4, 256) + 512;
 }
 
 RouteWork route_carve(void* base, int W, int H) {
@@ -45,8 +44,7 @@ RouteWork route_carve(void* base, int W, int H) {
   w.tiles_y = (H + kFT - 1) / kFT;
   const size_t n = (size_t)W * H, nt = (size_t)w.tiles_x * w.tiles_y;
   char* p = (char*)base;
-  w.flats = (uint32_t*)p;
-  p += align_up(n * 4, 256);
+  (void)n;
   w.tflat = (uint8_t*)p;
   p += align_up(nt, 256);
   w.queued = (int*)p;
@@ -116,11 +114,10 @@ __global__ void d8_kernel(const float* __restrict__ dem, char2* __restrict__ dir
       }
     }
   }
-  const unsigned int pos = warp_append(&w.scal[R_NFLAT], flat);
-  if (flat) {
-    w.flats[pos] = (uint32_t)i;
-    w.tflat[(y / kFT) * w.tiles_x + x / kFT] = 1;
-  }
+  if (flat) w.tflat[(y / kFT) * w.tiles_x + x / kFT] = 1;
+  const unsigned int nflat = __popc(__ballot_sync(__activemask(), flat));
+  if (nflat && (threadIdx.x & 31) == __ffs(__ballot_sync(__activemask(), flat)) - 1)
+    atomicAdd(&w.scal[R_NFLAT], nflat);  // statistics only
 }
 
 // ---- flat distances by tile relaxation ----------------------------------
@@ -296,13 +293,12 @@ flat_relax_kernel(const float* __restrict__ dem, int* fd, RouteWork w) {
 // (or with flatDist -1 for layer 1) whose elevation is <= the cell's.
 __global__ void flat_dir_kernel(const float* __restrict__ dem, char2* __restrict__ dir,
                                 int* __restrict__ fd, RouteWork w) {
-  const unsigned int nf = w.scal[R_NFLAT];
   const int W = w.W, H = w.H;
-  for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < nf;
-       j += gridDim.x * blockDim.x) {
-    uint32_t c = w.flats[j];
-    int d = fd[c];
-    if (d == kFlatInf) continue;
+  const int64_t N = (int64_t)W * H;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < N;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int d = fd[c];
+    if (d < 1 || d == kFlatInf) continue;  // not a flat cell with a layer
     int x = (int)(c % (uint32_t)W), y = (int)(c / (uint32_t)W);
     const float e = dem[c];
     const int want = d == 1 ? -1 : d - 1;
@@ -319,12 +315,10 @@ __global__ void flat_dir_kernel(const float* __restrict__ dem, char2* __restrict
 
 // Unresolved flats end as flatDist 0 with no direction.
 __global__ void flat_final_kernel(int* __restrict__ fd, RouteWork w) {
-  const unsigned int nf = w.scal[R_NFLAT];
-  for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < nf;
-       j += gridDim.x * blockDim.x) {
-    uint32_t c = w.flats[j];
+  const int64_t N = (int64_t)w.W * w.H;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < N;
+       c += (int64_t)gridDim.x * blockDim.x)
     if (fd[c] == kFlatInf) fd[c] = 0;
-  }
 }
 
 __global__ void route_scalars_kernel(unsigned int* s) {
@@ -360,7 +354,7 @@ cageo_status route_run(const float* filled, int8_t* dir, int* fd, const RouteWor
   int sms = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const unsigned lb = (unsigned)sms * 8;
+  const unsigned lb = (unsigned)sms * 16;
   flat_dir_kernel<<<lb, 256, 0, s>>>(filled, (char2*)dir, fd, w);
   flat_final_kernel<<<lb, 256, 0, s>>>(fd, w);
   CAGEO_CUDA(cudaGetLastError());

@@ -10,7 +10,6 @@ namespace cageo {
 struct RouteWork {
   int W = 0, H = 0;
   int tiles_x = 0, tiles_y = 0;
-  uint32_t* flats = nullptr;     // W*H: flat cells
   uint8_t* tflat = nullptr;      // per 32x32 tile: holds a flat cell
   int* queued = nullptr;         // per tile: last pass it was queued for
   int* lists = nullptr;          // 2 * ntiles: tile worklists
