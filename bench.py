@@ -212,7 +212,9 @@ def main():
     cfg = dict(cell_size=p["cell"], filter_model=api.FILTER_GAUSSIAN,
                practical_range=p["range_m"], error_stddev=p["sigma"], seed=1)
     pipe = api.Pipeline(dem, streams, **cfg)
-    base = rank * 1_000_000  # disjoint realization numbers per rank
+    from cageo_gb300.replicas import realization_range
+    # disjoint realization numbers per rank (replicas; weak scaling)
+    base, _ = realization_range(rank, world, world * 1_000_000)
     # Warm-up: graph capture + stage profile.
     pipe.run(base, args.warmup)
     stage_ms = pipe.profile(base + args.warmup)

@@ -1,0 +1,120 @@
+"""The drainage command line (reference options and file formats) and the
+Philox noise generator."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from cases import make_case
+
+pytestmark = pytest.mark.gpu
+
+
+def _write_inputs(tmp_path, dem, streams, nodata=-9999.0):
+    from cageo_gb300 import api
+    H, W = dem.shape
+    d = tmp_path / "DEM"
+    d.mkdir()
+    for name, grid in (("dem10", dem), ("streams", streams)):
+        api.write_header(str(d / (name + ".hdr")), W, H, 10.0, nodata)
+        api.write_raster(str(d / (name + ".bin")), grid)
+    return d
+
+
+def test_drainage_cli_matches_oracle(cuda, oracle, tmp_path):
+    import torch
+    from cageo_gb300 import _build, api
+    dem, streams = make_case(160, 120, seed=21)
+    d = _write_inputs(tmp_path, dem, streams)
+    cmd = [_build.DRAINAGE, "--dem-path", str(d), "--filter-type", "Gaussian",
+           "--practical-range", "60", "--error-standard-deviation", "1.5", "-i", "3",
+           "--seed", "9", "-o", "counts.bin"]
+    r = subprocess.run(cmd, cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "DEM size: 160 x 120" in r.stdout
+    got = api.read_raster(str(tmp_path / "counts.bin"), dem.shape)
+    rr = api.filter_radius(60.0, 10.0)
+    taps = api.filter_build(api.FILTER_GAUSSIAN, 60.0, 10.0, rr)
+    noise = torch.empty(dem.shape, dtype=torch.float32, device=cuda)
+    mc = np.zeros_like(dem)
+    for k in range(3):
+        api.noise_philox(noise, 9, k, 0.0, 1.5)
+        mc, *_ = oracle.realization(dem, streams, noise.cpu().numpy(), taps, rr, 1, mc)
+    assert np.array_equal(got, mc)
+
+
+def test_drainage_cli_frames_and_refusals(cuda, tmp_path):
+    from cageo_gb300 import _build, api
+    dem, streams = make_case(64, 48, seed=22)
+    d = _write_inputs(tmp_path, dem, streams)
+    base = [_build.DRAINAGE, "--dem-path", str(d), "-i", "2", "--seed", "3"]
+    r = subprocess.run(base + ["-o", "f.bin", "--output-option", "frames"], cwd=tmp_path,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    f0 = api.read_raster(str(tmp_path / "f_0000.bin"), dem.shape)
+    f1 = api.read_raster(str(tmp_path / "f_0001.bin"), dem.shape)
+    assert np.all(f1 >= f0) and f1.max() <= 2
+    assert subprocess.run(base + ["--cpu"], cwd=tmp_path, capture_output=True).returncode != 0
+    assert subprocess.run(base + ["--filter-type", "Spherical"], cwd=tmp_path,
+                          capture_output=True).returncode != 0
+    assert subprocess.run(base + ["--bogus"], cwd=tmp_path, capture_output=True).returncode != 0
+    # header mismatch between DEM and streams
+    api.write_header(str(d / "streams.hdr"), 65, 48, 10.0, -9999.0)
+    r = subprocess.run(base, cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode != 0 and "don't match" in r.stdout
+
+
+def _philox_np(ctr, key):
+    """Philox4x32-10 (Salmon et al. 2011) restated with numpy uint64 arithmetic."""
+    c = [x.astype(np.uint64) for x in ctr]
+    k0, k1 = np.uint64(key[0]), np.uint64(key[1])
+    M0, M1 = np.uint64(0xD2511F53), np.uint64(0xCD9E8D57)
+    mask = np.uint64(0xFFFFFFFF)
+    for _ in range(10):
+        p0, p1 = M0 * c[0], M1 * c[2]
+        hi0, lo0 = p0 >> np.uint64(32), p0 & mask
+        hi1, lo1 = p1 >> np.uint64(32), p1 & mask
+        c = [hi1 ^ c[1] ^ k0, lo1, hi0 ^ c[3] ^ k1, lo0]
+        k0 = (k0 + np.uint64(0x9E3779B9)) & mask
+        k1 = (k1 + np.uint64(0xBB67AE85)) & mask
+    return c
+
+
+def test_noise_matches_philox_restatement(cuda):
+    import torch
+    from cageo_gb300 import api
+    H, W, seed, real = 64, 96, 0x1234_5678_9ABC, 7
+    t = torch.empty((H, W), dtype=torch.float32, device=cuda)
+    api.noise_philox(t, seed, real, 2.0, 0.5)
+    got = t.cpu().numpy().reshape(-1)
+    g = np.arange(H * W // 4, dtype=np.uint64)
+    c = _philox_np([g, np.full_like(g, real), np.full_like(g, 0x63616765), np.zeros_like(g)],
+                   (seed & 0xFFFFFFFF, seed >> 32))
+    u = [((x >> np.uint64(8)).astype(np.float64) + 0.5) / 16777216.0 for x in c]
+    z = np.empty(H * W)
+    rad0, rad1 = np.sqrt(-2 * np.log(u[0])), np.sqrt(-2 * np.log(u[2]))
+    z[0::4], z[1::4] = rad0 * np.cos(2 * np.pi * u[1]), rad0 * np.sin(2 * np.pi * u[1])
+    z[2::4], z[3::4] = rad1 * np.cos(2 * np.pi * u[3]), rad1 * np.sin(2 * np.pi * u[3])
+    np.testing.assert_allclose(got, 2.0 + 0.5 * z, rtol=0, atol=2e-5)  # float32 log/sincos
+
+
+def test_noise_statistics_and_determinism(cuda):
+    import torch
+    from cageo_gb300 import api
+    t = torch.empty((2048, 2048), dtype=torch.float32, device=cuda)
+    api.noise_philox(t, 42, 0, 1.0, 3.0)
+    a = t.clone()
+    assert abs(float(a.mean()) - 1.0) < 0.01 and abs(float(a.std()) - 3.0) < 0.01
+    assert torch.isfinite(a).all()
+    api.noise_philox(t, 42, 0, 1.0, 3.0)
+    assert torch.equal(a, t)
+    api.noise_philox(t, 42, 1, 1.0, 3.0)
+    assert not torch.equal(a, t)
+    # odd sizes: the tail group is written, nothing beyond it
+    u = torch.full((3, 7), 99.0, device=cuda)
+    api.noise_philox(u[:, :5].contiguous(), 1, 0)  # contiguity copy is written, original untouched
+    assert float(u.max()) == 99.0
+    v = torch.empty(21, device=cuda)
+    api.noise_philox(v.view(3, 7), 1, 0)
+    assert torch.isfinite(v).all()

@@ -1,0 +1,87 @@
+"""Host-side behaviour of the C ABI that needs no GPU: argument validation
+(refused before any device work), error strings, raster I/O."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from cageo_gb300 import api
+
+P = ctypes.c_void_p
+
+
+def _err():
+    return api.lib().cageo_last_error_string().decode()
+
+
+def test_argument_checks_refuse_before_device_work():
+    L = api.lib()
+    a, b = P(4096), P(8192)  # never dereferenced: every call below fails its checks first
+    assert L.cageo_convolve(a, b, 10, 10, 1, a, 10, None) == 1 and "radius" in _err()
+    assert L.cageo_convolve(a, a, 10, 10, 1, a, 2, None) == 1 and "in place" in _err()
+    assert L.cageo_convolve(a, b, 10, 10, 7, a, 2, None) == 1
+    assert L.cageo_pitfill(a, b, 70000, 10, -9999.0, 0, None, 0, None) == 1 and "65535" in _err()
+    assert L.cageo_pitfill(a, a, 10, 10, -9999.0, 0, None, 0, None) == 1
+    assert L.cageo_pitfill(a, b, 10, 10, -9999.0, 3, None, 0, None) == 1
+    assert L.cageo_stream_burn(a, b, 10, 10, 6, -9999.0, -9999.0, None) == 1 and "bevel" in _err()
+    assert L.cageo_noise_philox(None, 10, 10, 1, 0, 0.0, 1.0, None) == 1
+    assert L.cageo_pitfill_static(a, b, 4096, 4096, -9999.0, 0, None) == 1
+    cfg = api.PipelineConfig(64, 64, 10.0, 9, 60.0, 0.0, 1.0, 2, -9999.0, -9999.0, 1, 1)
+    p = P()
+    assert L.cageo_pipeline_create(ctypes.byref(p), ctypes.byref(cfg), a, b) == 1
+    cfg.filter_model = 1
+    cfg.practical_range = 400.0  # radius 100 >= 64
+    assert L.cageo_pipeline_create(ctypes.byref(p), ctypes.byref(cfg), a, b) == 1
+    assert not p.value
+
+
+def test_workspace_sizes_scale_with_grid():
+    L = api.lib()
+    s1, s2 = L.cageo_pitfill_workspace_size(512, 512), L.cageo_pitfill_workspace_size(1024, 1024)
+    assert 0 < s1 < s2
+    assert L.cageo_pitfill_workspace_size(0, 10) == 0
+    assert L.cageo_trace_workspace_size(100, 100) > 4 * 100 * 100
+    assert L.cageo_route_workspace_size(100, 100) > 4 * 100 * 100
+
+
+def test_raster_roundtrip(tmp_path):
+    hdr = tmp_path / "dem.hdr"
+    api.write_header(str(hdr), 7, 5, 10.0, -9999.0, xll=3383178.75, yll=6720450.0)
+    info = api.read_header(str(hdr))
+    assert (info.ncols, info.nrows, info.cellsize, info.nodata_value) == (7, 5, 10.0, -9999.0)
+    assert info.xllcorner == pytest.approx(3383178.75)
+    data = np.arange(35, dtype=np.float32).reshape(5, 7)
+    api.write_raster(str(tmp_path / "dem.bin"), data)
+    assert np.array_equal(api.read_raster(str(tmp_path / "dem.bin"), (5, 7)), data)
+
+
+def test_raster_errors(tmp_path):
+    api.write_raster(str(tmp_path / "x.bin"), np.zeros(10, np.float32))
+    with pytest.raises(api.CageoError) as e:
+        api.read_raster(str(tmp_path / "x.bin"), (3, 4))
+    assert e.value.status == 5
+    with pytest.raises(api.CageoError) as e:
+        api.read_raster(str(tmp_path / "missing.bin"), (3, 4))
+    assert e.value.status == 4
+    (tmp_path / "bad.hdr").write_text("ncols 4\nnrows 4\ncolour blue\n")
+    with pytest.raises(api.CageoError) as e:
+        api.read_header(str(tmp_path / "bad.hdr"))
+    assert e.value.status == 5 and "colour" in _err()
+    (tmp_path / "bo.hdr").write_text("ncols 4\nnrows 4\nbyteorder VAX\n")
+    with pytest.raises(api.CageoError):
+        api.read_header(str(tmp_path / "bo.hdr"))
+    # the reference's sample header parses
+    (tmp_path / "ref.hdr").write_text("ncols\t\t1560\nnrows\t\t1341\nxllcorner\t3383178.7509533\n"
+                                      "yllcorner\t6720450\ncellsize\t10\nNODATA_value\t-9999\n"
+                                      "byteorder\tLSBFIRST\n")
+    i = api.read_header(str(tmp_path / "ref.hdr"))
+    assert (i.ncols, i.nrows, i.byteorder_msb) == (1560, 1341, 0)
+
+
+def test_synthetic_streams_follow_accumulation():
+    from cageo_gb300 import synth
+    dem = synth.add_pits(synth.fbm_dem(64, 48, 0.8, 2, 10.0, 60.0), 5, 2)
+    s, acc = synth.make_streams(dem, 40, ids="components", return_accum=True)
+    assert np.all((s >= 0) == (acc > 40))
+    assert acc.max() <= 64 * 48 and acc.min() >= 1
+    assert s[s >= 0].min() >= 1  # stream ids start at 1 (0 would alias index 0 in tracing)

@@ -1,0 +1,54 @@
+"""Multi-rank host logic of the replica path on CPU with gloo (world size 2):
+disjoint, covering realization shares and the final count sum."""
+import os
+import socket
+
+import numpy as np
+import pytest
+
+from cageo_gb300.replicas import realization_range
+
+
+def test_realization_range_partitions():
+    for world in (1, 2, 3, 8):
+        for total in (0, 1, 7, 100):
+            seen = []
+            for r in range(world):
+                s, c = realization_range(r, world, total, first=5)
+                seen.extend(range(s, s + c))
+            assert seen == list(range(5, 5 + total))
+    with pytest.raises(ValueError):
+        realization_range(2, 2, 10)
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _worker(rank, world, port, out):
+    import torch
+    import torch.distributed as dist
+    from cageo_gb300.replicas import realization_range, sum_counts
+    dist.init_process_group("gloo", init_method="tcp://127.0.0.1:%d" % port, rank=rank,
+                            world_size=world)
+    start, count = realization_range(rank, world, 10)
+    # Stand-in for a pipeline's counts: each realization k adds k+1 to every cell.
+    counts = torch.full((4, 5), float(sum(k + 1 for k in range(start, start + count))))
+    sum_counts(counts)
+    out[rank] = counts.numpy().copy()
+    dist.destroy_process_group()
+
+
+def test_gloo_world2_count_sum():
+    import torch.multiprocessing as mp
+    port = _free_port()
+    with mp.Manager() as m:
+        out = m.dict()
+        mp.start_processes(_worker, args=(2, port, out), nprocs=2, join=True, start_method="spawn")
+        expect = float(sum(k + 1 for k in range(10)))
+        for r in range(2):
+            assert np.all(out[r] == expect)
