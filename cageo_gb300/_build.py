@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["common.cu", "noise_conv.cu", "surface.cu", "pitfill.cu", "routing.cu",
               "trace_border.cu", "pipeline.cu", "pitfill_static.cu"]
-HOST_SOURCES = ["filter.cpp", "raster_io.cpp"]
+HOST_SOURCES = ["filter.cpp", "raster_io.cpp", "jpeg.cpp"]
 
 LIB = os.path.join(OUT, "libcageo.so")
 SYNTH = os.path.join(OUT, "libcageo_synth.so")

@@ -75,6 +75,9 @@ _SIGS = {
     "cageo_pipeline_stats": ([_vp, _vp, _i], _i),
     "cageo_pipeline_profile": ([_vp, ctypes.c_uint32, _vp, _i], _i),
     "cageo_pipeline_destroy": ([_vp], None),
+    "cageo_to_bytes": ([_vp, _vp, _i, _i, _vp], _i),
+    "cageo_write_jpeg": ([ctypes.c_char_p, _vp, _i, _i, _i], _i),
+    "cageo_pipeline_counts_bytes": ([_vp, _vp], _i),
     "cageo_read_header": ([ctypes.c_char_p, ctypes.POINTER(RasterInfo)], _i),
     "cageo_write_header": ([ctypes.c_char_p, ctypes.POINTER(RasterInfo)], _i),
     "cageo_read_raster": ([ctypes.c_char_p, _vp, _sz], _i),
@@ -306,6 +309,22 @@ class Pipeline:
             self.close()
         except Exception:
             pass
+
+
+def to_bytes(counts):
+    """uint8 image rintf(255*((v-min)/max)) of a float CUDA grid (the reference's JPEG bytes)."""
+    import torch
+    _grid(counts, torch.float32, "counts")
+    H, W = counts.shape
+    out = torch.empty((H, W), dtype=torch.uint8, device=counts.device)
+    _check(lib().cageo_to_bytes(_ptr(counts), _ptr(out), W, H, _stream()))
+    return out
+
+
+def write_jpeg(path, gray, quality=85):
+    g = np.ascontiguousarray(gray, np.uint8)
+    H, W = g.shape
+    _check(lib().cageo_write_jpeg(os.fsencode(path), g.ctypes.data_as(_vp), W, H, quality))
 
 
 # ---- A10 --------------------------------------------------------------------------

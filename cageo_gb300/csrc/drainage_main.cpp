@@ -9,11 +9,15 @@
 //   -i/--iterations N (10)    --gpu[=B]  --cpu[=B]
 //   -o/--output-file FILE (.bin | .jpg)  --output-option end|frames
 //
+// Outputs: .bin = raw float32 counts; .jpg (the reference's default type) =
+// the counts scaled to bytes as (uint8)rintf(255*((v-min)/max)) and written
+// as a baseline grayscale JPEG of quality 85.
+//
 // Additive options: --seed N (default: the current time, like the
 // reference's time(NULL)+iteration seeding), --bevel-radius N (2; the
 // reference has no flag for it), --no-graphs.  Output files go to the
 // working directory under the stem of -o (the reference keeps only the
-// stem), as raw float32 counts.  This driver runs on the GPU only; --cpu
+// stem).  This driver runs on the GPU only; --cpu
 // is refused rather than silently using another implementation.
 #include <chrono>
 #include <cstdio>
@@ -50,7 +54,7 @@ void usage() {
       "  -i [ --iterations ] arg (=10) Number of Monte Carlo iterations\n"
       "  --gpu [=arg(=1)] (=1)        Run algorithm on GPU\n"
       "  --cpu [=arg(=1)] (=0)        Run algorithm on CPU (not available in this build)\n"
-      "  -o [ --output-file ] arg     Write result into file (*.bin)\n"
+      "  -o [ --output-file ] arg     Write result into file (*.bin raw float32 counts, *.jpg image)\n"
       "  --output-option arg          end | frames\n"
       "  --seed arg                   Noise seed (default: current time)\n"
       "  --bevel-radius arg (=2)      Stream burning bevel radius (1..5)\n"
@@ -137,10 +141,7 @@ int main(int argc, char** argv) {
     else if (o.output_option == "frames") opt = FRAMES;
     else { std::printf("Unknown output option provided: %s. Exiting...\n", o.output_option.c_str()); return 1; }
   }
-  if (opt != NONE && ext != ".bin") {
-    std::fprintf(stderr, "JPEG output is not available in this build; use -o NAME.bin\n");
-    return 1;
-  }
+  const bool jpeg = ext != ".bin";  // ".jpg" or no extension, as in the reference
   int model;
   if (o.filter == "Gaussian") model = CAGEO_FILTER_GAUSSIAN;
   else if (o.filter == "Exponential") model = CAGEO_FILTER_EXPONENTIAL;
@@ -161,6 +162,7 @@ int main(int argc, char** argv) {
   const int W = di.ncols, H = di.nrows;
   const size_t N = (size_t)W * H;
   std::vector<float> dem(N), streams(N), counts(N);
+  std::vector<uint8_t> image(jpeg ? N : 0);
   if (cageo_read_raster((o.dem_path + "/" + o.dem + ".bin").c_str(), dem.data(), N)) return fail("DEM raster");
   if (cageo_read_raster((o.dem_path + "/" + o.stream + ".bin").c_str(), streams.data(), N)) return fail("stream raster");
   const int r = cageo_filter_radius(o.range, di.cellsize);
@@ -189,11 +191,17 @@ int main(int argc, char** argv) {
     if (cageo_pipeline_run(p, (uint32_t)it, batch)) { cageo_pipeline_destroy(p); return fail("realization"); }
     it += batch;
     if ((opt == END && it == o.iterations) || opt == FRAMES) {
-      if (cageo_pipeline_counts(p, counts.data())) { cageo_pipeline_destroy(p); return fail("counts"); }
       char name[4096];
-      if (opt == FRAMES) std::snprintf(name, sizeof(name), "%s_%04d.bin", out_name.c_str(), it - 1);
-      else std::snprintf(name, sizeof(name), "%s.bin", out_name.c_str());
-      if (cageo_write_raster(name, counts.data(), N)) { cageo_pipeline_destroy(p); return fail("output"); }
+      const char* suffix = jpeg ? ".jpg" : ".bin";
+      if (opt == FRAMES) std::snprintf(name, sizeof(name), "%s_%04d%s", out_name.c_str(), it - 1, suffix);
+      else std::snprintf(name, sizeof(name), "%s%s", out_name.c_str(), suffix);
+      if (jpeg) {
+        if (cageo_pipeline_counts_bytes(p, image.data())) { cageo_pipeline_destroy(p); return fail("counts"); }
+        if (cageo_write_jpeg(name, image.data(), W, H, 85)) { cageo_pipeline_destroy(p); return fail("output"); }
+      } else {
+        if (cageo_pipeline_counts(p, counts.data())) { cageo_pipeline_destroy(p); return fail("counts"); }
+        if (cageo_write_raster(name, counts.data(), N)) { cageo_pipeline_destroy(p); return fail("output"); }
+      }
     }
   }
   double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

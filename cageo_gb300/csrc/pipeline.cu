@@ -35,6 +35,8 @@ cageo_status launch_realistic(const float* dem, float* field, int64_t n, float n
 cageo_status launch_burn_stage(const float* src, float* dst, const float* streams, int W,
                                int H, int bevel, float nodata_dem, float nodata_stream,
                                cudaStream_t s);
+cageo_status launch_to_bytes(const float* in, uint8_t* out, int64_t n, unsigned int* mm,
+                             cudaStream_t s);
 
 // Accumulate the border mask unless the realization was flagged; a flagged
 // realization index is appended to the redo list.
@@ -406,6 +408,22 @@ extern "C" cageo_status cageo_pipeline_counts(cageo_pipeline* p, float* h_out) {
   CAGEO_CUDA(cudaMemcpyAsync(h_out, p->tmp, sizeof(float) * p->N, cudaMemcpyDeviceToHost,
                              p->stream));
   CAGEO_CUDA(cudaStreamSynchronize(p->stream));
+  return CAGEO_OK;
+}
+
+extern "C" cageo_status cageo_pipeline_counts_bytes(cageo_pipeline* p, uint8_t* h_out) {
+  CAGEO_CHECK_ARG(p && h_out, "null argument");
+  cudaStream_t s = p->stream;
+  counts_to_float_kernel<<<(unsigned)((p->N + 255) / 256), 256, 0, s>>>(p->counts, p->tmp, p->N);
+  CAGEO_CUDA(cudaGetLastError());
+  // The byte image is staged in the noise buffer and the min/max pair in the
+  // flat-distance grid; both are rewritten by the next realization.
+  uint8_t* bytes = (uint8_t*)p->noise;
+  unsigned int* mm = (unsigned int*)p->flatdist;
+  cageo_status st = launch_to_bytes(p->tmp, bytes, p->N, mm, s);
+  if (st) return st;
+  CAGEO_CUDA(cudaMemcpyAsync(h_out, bytes, (size_t)p->N, cudaMemcpyDeviceToHost, s));
+  CAGEO_CUDA(cudaStreamSynchronize(s));
   return CAGEO_OK;
 }
 

@@ -146,9 +146,64 @@ cageo_status launch_burn_stage(const float* src, float* dst, const float* stream
   return CAGEO_OK;
 }
 
+// Byte image of a count grid for the JPEG output
+// (src/utils/tobytearray/ToByteArrayAlgorithmCPUOpenMP.h:33-52):
+// (uint8) rintf(255 * ((v - min) / max)) with the grid's min and max.
+__global__ void minmax_kernel(const float* __restrict__ in, int64_t n, unsigned int* mm) {
+  float lo = kInf, hi = -kInf;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float v = in[i];
+    lo = fminf(lo, v);
+    hi = fmaxf(hi, v);
+  }
+  unsigned int a = float_to_ordered(lo), b = float_to_ordered(hi);
+  a = __reduce_min_sync(0xffffffffu, a);
+  b = __reduce_max_sync(0xffffffffu, b);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&mm[0], a);
+    atomicMax(&mm[1], b);
+  }
+}
+
+__global__ void to_bytes_kernel(const float* __restrict__ in, uint8_t* __restrict__ out,
+                                int64_t n, const unsigned int* mm) {
+  const float lo = ordered_to_float(mm[0]), hi = ordered_to_float(mm[1]);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float s = __fmul_rn(255.0f, __fdiv_rn(__fsub_rn(in[i], lo), hi));
+    // Out-of-range or NaN results (an all-zero grid divides by 0) give 0.
+    const float r = rintf(s);
+    out[i] = (r >= 0.0f && r <= 255.0f) ? (uint8_t)r : (uint8_t)0;
+  }
+}
+
+__global__ void minmax_init_kernel(unsigned int* mm) {
+  mm[0] = 0xffffffffu;
+  mm[1] = 0u;
+}
+
+cageo_status launch_to_bytes(const float* in, uint8_t* out, int64_t n, unsigned int* mm,
+                             cudaStream_t s) {
+  minmax_init_kernel<<<1, 1, 0, s>>>(mm);
+  minmax_kernel<<<1024, 256, 0, s>>>(in, n, mm);
+  to_bytes_kernel<<<1024, 256, 0, s>>>(in, out, n, mm);
+  CAGEO_CUDA(cudaGetLastError());
+  return CAGEO_OK;
+}
+
 }  // namespace cageo
 
 using namespace cageo;
+
+extern "C" cageo_status cageo_to_bytes(const float* d_in, uint8_t* d_out, int W, int H,
+                                       cudaStream_t stream) {
+  CAGEO_CHECK_ARG(d_in && d_out && valid_dims(W, H), "pointers and size");
+  Scratch ws;
+  cageo_status st = ws.acquire(nullptr, 0, 2 * sizeof(unsigned int), stream);
+  if (st) return st;
+  return launch_to_bytes(d_in, d_out, (int64_t)W * H, (unsigned int*)ws.ptr, stream);
+}
 
 extern "C" cageo_status cageo_realistic_dem(const float* d_dem, float* d_field, int W, int H,
                                             float nodata_dem, cudaStream_t stream) {

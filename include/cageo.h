@@ -201,6 +201,8 @@ cageo_status cageo_pipeline_run(cageo_pipeline* p, uint32_t first_realization,
 /* Border counts so far as float (the reference's CatchmentBorderType). */
 cageo_status cageo_pipeline_counts(cageo_pipeline* p, float* h_out);
 cageo_status cageo_pipeline_counts_device(cageo_pipeline* p, float* d_out);
+/* Border counts as the reference's JPEG byte image (cageo_to_bytes), host. */
+cageo_status cageo_pipeline_counts_bytes(cageo_pipeline* p, uint8_t* h_out);
 /* Stage outputs of the most recent realization (any pointer may be NULL):
  * filled surface (float), dir (2 int8 per cell), labels (int32).  Host. */
 cageo_status cageo_pipeline_last_stages(cageo_pipeline* p, float* h_filled,
@@ -236,6 +238,16 @@ typedef struct {
   float nodata_value;
   int byteorder_msb;  /* 1 for MSBFIRST; the reference parses but ignores it */
 } cageo_raster_info;
+/* Byte image for the JPEG output: (uint8)rintf(255*((v-min)/max)) with the
+ * grid's min and max, replacing ToByteArrayAlgorithm::execute
+ * (src/utils/tobytearray/ToByteArrayAlgorithmCPUOpenMP.h:33-52).  A grid
+ * whose max is 0 gives 0 everywhere. */
+cageo_status cageo_to_bytes(const float* d_in, uint8_t* d_out, int W, int H,
+                            cudaStream_t stream);
+/* Baseline grayscale JFIF writer (quality 1..100; the reference uses jpge's
+ * default 85, src/main.cpp:265-270).  Host only. */
+cageo_status cageo_write_jpeg(const char* path, const uint8_t* h_gray, int W, int H,
+                              int quality);
 cageo_status cageo_read_header(const char* path, cageo_raster_info* info);
 cageo_status cageo_write_header(const char* path, const cageo_raster_info* info);
 cageo_status cageo_read_raster(const char* path, float* h_out, size_t count);

@@ -118,3 +118,32 @@ def test_noise_statistics_and_determinism(cuda):
     v = torch.empty(21, device=cuda)
     api.noise_philox(v.view(3, 7), 1, 0)
     assert torch.isfinite(v).all()
+
+
+def test_to_bytes_matches_reference_formula(cuda):
+    import torch
+    from cageo_gb300 import api
+    rng = np.random.default_rng(4)
+    counts = rng.integers(0, 37, size=(100, 130)).astype(np.float32)
+    got = api.to_bytes(torch.from_numpy(counts).to(cuda)).cpu().numpy()
+    lo, hi = np.float32(counts.min()), np.float32(counts.max())
+    ref = np.rint(np.float32(255.0) * ((counts - lo) / hi)).astype(np.uint8)
+    assert np.array_equal(got, ref)
+    zero = api.to_bytes(torch.zeros((4, 4), device=cuda)).cpu().numpy()
+    assert np.all(zero == 0)
+
+
+def test_drainage_cli_jpeg(cuda, tmp_path):
+    import torch
+    from cageo_gb300 import _build, api
+    from jpeg_decode import decode
+    dem, streams = make_case(96, 72, seed=23)
+    d = _write_inputs(tmp_path, dem, streams)
+    base = [_build.DRAINAGE, "--dem-path", str(d), "-i", "4", "--seed", "5"]
+    assert subprocess.run(base + ["-o", "c.bin"], cwd=tmp_path, capture_output=True).returncode == 0
+    assert subprocess.run(base + ["-o", "c.jpg"], cwd=tmp_path, capture_output=True).returncode == 0
+    counts = api.read_raster(str(tmp_path / "c.bin"), dem.shape)
+    img = api.to_bytes(torch.from_numpy(counts).to(cuda)).cpu().numpy()
+    back = decode(str(tmp_path / "c.jpg"))
+    assert back.shape == img.shape
+    assert np.mean(np.abs(back.astype(int) - img.astype(int))) < 12
