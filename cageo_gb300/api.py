@@ -67,6 +67,7 @@ _SIGS = {
     "cageo_pipeline_create_device": ([ctypes.POINTER(_vp), ctypes.POINTER(PipelineConfig), _vp,
                                       _vp], _i),
     "cageo_pipeline_run": ([_vp, ctypes.c_uint32, _i], _i),
+    "cageo_pipeline_run_filter": ([_vp, ctypes.c_uint32, _i, _i, _f, _f, _f], _i),
     "cageo_pipeline_counts": ([_vp, _vp], _i),
     "cageo_pipeline_counts_device": ([_vp, _vp], _i),
     "cageo_pipeline_last_stages": ([_vp, _vp, _vp, _vp], _i),
@@ -251,6 +252,11 @@ class Pipeline:
 
     def run(self, first, count):
         _check(lib().cageo_pipeline_run(self._p, first, count))
+
+    def run_filter(self, first, count, filter_model, practical_range, error_mean, error_stddev):
+        """Run with this filter and error model (kept for later runs)."""
+        _check(lib().cageo_pipeline_run_filter(self._p, first, count, filter_model,
+                                               practical_range, error_mean, error_stddev))
 
     def counts(self, out=None):
         """Float counts: a new host numpy array, or into `out` (a CUDA tensor, or a

@@ -164,6 +164,9 @@ cageo_status run_stage_path(cageo_pipeline* p, uint32_t r) {
   return CAGEO_OK;
 }
 
+// Largest filter radius a pipeline accepts (per-call filters included).
+constexpr int kMaxRunRadius = 64;
+
 template <typename T>
 cageo_status dalloc(T** ptr, size_t bytes) {
   CAGEO_CUDA(cudaMalloc((void**)ptr, bytes ? bytes : 16));
@@ -183,6 +186,7 @@ cageo_status create_common(cageo_pipeline** out, const cageo_pipeline_config* cf
   CAGEO_CHECK_ARG(cfg->cell_size > 0 && cfg->practical_range > 0, "range and cell size");
   const int r = cageo_filter_radius(cfg->practical_range, cfg->cell_size);
   CAGEO_CHECK_ARG(r >= 0 && r < W && r < H, "filter radius must be below the grid size");
+  CAGEO_CHECK_ARG(r <= kMaxRunRadius, "filter radius above 64");
   auto* p = new cageo_pipeline();
   p->cfg = *cfg;
   p->W = W;
@@ -202,7 +206,8 @@ cageo_status create_common(cageo_pipeline** out, const cageo_pipeline_config* cf
   const int taps = cfg->filter_model == CAGEO_FILTER_GAUSSIAN ? L : L * L;
   if ((st = dalloc(&p->dem, fb)) || (st = dalloc(&p->streams, fb)) ||
       (st = dalloc(&p->noise, fb)) || (st = dalloc(&p->q, fb)) || (st = dalloc(&p->filled, fb)) ||
-      (st = dalloc(&p->tmp, fb)) || (st = dalloc(&p->filter, sizeof(float) * taps)) ||
+      (st = dalloc(&p->tmp, fb)) ||
+      (st = dalloc(&p->filter, sizeof(float) * (2 * kMaxRunRadius + 1) * (2 * kMaxRunRadius + 1))) ||
       (st = dalloc(&p->code, (size_t)p->N)) || (st = dalloc(&p->dir, 2 * (size_t)p->N)) ||
       (st = dalloc(&p->flatdist, 4 * (size_t)p->N)) || (st = dalloc(&p->label, 4 * (size_t)p->N)) ||
       (st = dalloc(&p->counts, 4 * (size_t)p->N)) ||
@@ -389,6 +394,37 @@ extern "C" cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t reali
   } while (0);
   for (auto& e : ev) cudaEventDestroy(e);
   return st;
+}
+
+extern "C" cageo_status cageo_pipeline_run_filter(cageo_pipeline* p, uint32_t first, int count,
+                                                  int model, float practical_range,
+                                                  float error_mean, float error_stddev) {
+  CAGEO_CHECK_ARG(p && count >= 0, "pipeline and count");
+  CAGEO_CHECK_ARG(model == CAGEO_FILTER_GAUSSIAN || model == CAGEO_FILTER_EXPONENTIAL,
+                  "filter model");
+  CAGEO_CHECK_ARG(practical_range > 0, "practical range");
+  const int r = cageo_filter_radius(practical_range, p->cfg.cell_size);
+  CAGEO_CHECK_ARG(r >= 0 && r < p->W && r < p->H && r <= kMaxRunRadius,
+                  "filter radius must be below the grid size and 64");
+  const int L = 2 * r + 1, taps = model == CAGEO_FILTER_GAUSSIAN ? L : L * L;
+  std::vector<float> hf(taps);
+  cageo_status st = cageo_filter_build(model, practical_range, p->cfg.cell_size, r, hf.data());
+  if (st) return st;
+  CAGEO_CUDA(cudaStreamSynchronize(p->stream));
+  CAGEO_CUDA(cudaMemcpy(p->filter, hf.data(), sizeof(float) * taps, cudaMemcpyHostToDevice));
+  p->cfg.filter_model = model;
+  p->cfg.practical_range = practical_range;
+  p->cfg.error_mean = error_mean;
+  p->cfg.error_stddev = error_stddev;
+  p->radius = r;
+  // The captured graph holds the old filter's launch shapes: drop it.
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  p->exec = nullptr;
+  p->graph = nullptr;
+  p->graph_ok = false;
+  p->cfg.use_graphs = 0;
+  return cageo_pipeline_run(p, first, count);
 }
 
 extern "C" cageo_status cageo_pipeline_counts_device(cageo_pipeline* p, float* d_out) {

@@ -107,6 +107,20 @@ WORKLOADS = {
 }
 
 
+# The batched benchmark: a 2048^2 DEM and three uneven tiles (width x height).
+BATCH_SHAPES = [(2048, 2048), (257, 1013), (1500, 733), (3001, 401)]
+
+
+def batched_grids(seed=5, scale=1.0, ids="ones"):
+    """(dem, streams) for each batch shape: fBm (Hurst 0.8, 0-300 m), pits, threshold 2000."""
+    grids = []
+    for k, (w, h) in enumerate(BATCH_SHAPES):
+        w, h = max(int(w * scale), 16), max(int(h * scale), 16)
+        dem = add_pits(fbm_dem(w, h, 0.8, seed + k, 0.0, 300.0), max(w * h // 2000, 1), seed + k)
+        grids.append((dem, make_streams(dem, max(int(2000 * scale * scale), 20), ids=ids)))
+    return grids
+
+
 def workload(name, ids="ones", scale=None):
     """(dem, streams, params) for a named workload; `scale` shrinks width/height."""
     p = dict(WORKLOADS[name])

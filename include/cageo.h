@@ -198,6 +198,12 @@ cageo_status cageo_pipeline_create_device(cageo_pipeline** out,
                                           const float* d_streams);
 cageo_status cageo_pipeline_run(cageo_pipeline* p, uint32_t first_realization,
                                 int count);
+/* Same with another filter and error model from now on (rebuilt on the
+ * host; radius <= 64): for batches whose realizations draw their practical
+ * range and error standard deviation.  Runs without a CUDA graph. */
+cageo_status cageo_pipeline_run_filter(cageo_pipeline* p, uint32_t first_realization,
+                                       int count, int model, float practical_range,
+                                       float error_mean, float error_stddev);
 /* Border counts so far as float (the reference's CatchmentBorderType). */
 cageo_status cageo_pipeline_counts(cageo_pipeline* p, float* h_out);
 cageo_status cageo_pipeline_counts_device(cageo_pipeline* p, float* d_out);
