@@ -72,6 +72,8 @@ _SIGS = {
     "cageo_pipeline_counts_device": ([_vp, _vp], _i),
     "cageo_pipeline_last_stages": ([_vp, _vp, _vp, _vp], _i),
     "cageo_pipeline_reset_counts": ([_vp], _i),
+    "cageo_pipeline_save": ([_vp, ctypes.c_char_p, ctypes.c_uint32], _i),
+    "cageo_pipeline_load": ([_vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint32)], _i),
     "cageo_pipeline_stream": ([_vp], _vp),
     "cageo_pipeline_stats": ([_vp, _vp, _i], _i),
     "cageo_pipeline_profile": ([_vp, ctypes.c_uint32, _vp, _i], _i),
@@ -279,6 +281,15 @@ class Pipeline:
         _check(lib().cageo_pipeline_last_stages(self._p, f.ctypes.data_as(_vp),
                                                 d.ctypes.data_as(_vp), lab.ctypes.data_as(_vp)))
         return f, d, lab
+
+    def save(self, path, next_realization):
+        _check(lib().cageo_pipeline_save(self._p, os.fsencode(path), next_realization))
+
+    def load(self, path):
+        """Restore counts from a checkpoint; returns the next realization number."""
+        nxt = ctypes.c_uint32()
+        _check(lib().cageo_pipeline_load(self._p, os.fsencode(path), ctypes.byref(nxt)))
+        return nxt.value
 
     def reset_counts(self):
         _check(lib().cageo_pipeline_reset_counts(self._p))

@@ -32,7 +32,7 @@ namespace {
 
 struct Options {
   std::string dem = "dem10", stream = "streams", dem_path = "DEM", stream_path = "DEM";
-  std::string filter = "Gaussian", output_file, output_option;
+  std::string filter = "Gaussian", output_file, output_option, checkpoint, resume;
   float range = 60.0f, mean = 0.0f, sd = 1.0f;
   int iterations = 10, bevel = 2;
   bool gpu = true, cpu = false, graphs = true, have_seed = false;
@@ -58,7 +58,9 @@ void usage() {
       "  --output-option arg          end | frames\n"
       "  --seed arg                   Noise seed (default: current time)\n"
       "  --bevel-radius arg (=2)      Stream burning bevel radius (1..5)\n"
-      "  --no-graphs                  Launch kernels directly instead of a CUDA graph\n");
+      "  --no-graphs                  Launch kernels directly instead of a CUDA graph\n"
+      "  --checkpoint arg             Save counts + next realization here after each output\n"
+      "  --resume arg                 Continue from a checkpoint (same grid and --seed)\n");
 }
 
 bool parse_bool(const std::string& v) { return !(v == "0" || v == "false" || v == "off"); }
@@ -97,6 +99,8 @@ int parse(int argc, char** argv, Options* o) {
     else if (a == "--seed") { if (!next(&v)) return 1; o->seed = std::strtoull(v.c_str(), nullptr, 10); o->have_seed = true; }
     else if (a == "--bevel-radius") { if (!next(&v)) return 1; o->bevel = std::atoi(v.c_str()); }
     else if (a == "--no-graphs") { o->graphs = false; }
+    else if (a == "--checkpoint") { if (!next(&o->checkpoint)) return 1; }
+    else if (a == "--resume") { if (!next(&o->resume)) return 1; }
     else { std::fprintf(stderr, "unrecognised option '%s'\n", argv[i]); return 1; }
   }
   return 0;
@@ -185,11 +189,23 @@ int main(int argc, char** argv) {
   std::printf("Seed: %llu\n", (unsigned long long)cfg.seed);
   cageo_pipeline* p = nullptr;
   if (cageo_pipeline_create(&p, &cfg, dem.data(), streams.data())) return fail("pipeline");
+  int start = 0;
+  if (!o.resume.empty()) {
+    uint32_t nxt = 0;
+    if (cageo_pipeline_load(p, o.resume.c_str(), &nxt)) { cageo_pipeline_destroy(p); return fail("resume"); }
+    start = (int)nxt;
+    std::printf("Resuming at realization %d\n", start);
+  }
   auto t0 = std::chrono::steady_clock::now();
-  for (int it = 0; it < o.iterations;) {
-    int batch = opt == FRAMES ? 1 : o.iterations;
+  for (int it = start; it < o.iterations;) {
+    // One realization per call when every realization is written or saved.
+    const int batch = (opt == FRAMES || !o.checkpoint.empty()) ? 1 : o.iterations - it;
     if (cageo_pipeline_run(p, (uint32_t)it, batch)) { cageo_pipeline_destroy(p); return fail("realization"); }
     it += batch;
+    if (!o.checkpoint.empty() && cageo_pipeline_save(p, o.checkpoint.c_str(), (uint32_t)it)) {
+      cageo_pipeline_destroy(p);
+      return fail("checkpoint");
+    }
     if ((opt == END && it == o.iterations) || opt == FRAMES) {
       char name[4096];
       const char* suffix = jpeg ? ".jpg" : ".bin";
@@ -207,8 +223,9 @@ int main(int argc, char** argv) {
   double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   int64_t st[5] = {0};
   cageo_pipeline_stats(p, st, 5);
+  const int done = o.iterations - start;
   std::fprintf(stderr, "\n***********\n\n%d realizations in %.3f s: %.3f realizations/s, %.3e cells/s\n",
-               o.iterations, sec, o.iterations / sec, o.iterations * (double)N / sec);
+               done, sec, done / sec, done * (double)N / sec);
   std::fprintf(stderr, "last realization: fill passes %lld, phases %lld, flat layers %lld\n",
                (long long)st[0], (long long)st[1], (long long)st[2]);
   cageo_pipeline_destroy(p);

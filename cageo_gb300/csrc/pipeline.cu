@@ -16,6 +16,8 @@
 // the stage kernels, which follow the reference step by step.  With a
 // NODATA of 0 every realization takes the stage path.
 #include <cmath>
+#include <cstdio>
+#include <cstring>
 #include <vector>
 #include "common.cuh"
 #include "front.cuh"
@@ -425,6 +427,66 @@ extern "C" cageo_status cageo_pipeline_run_filter(cageo_pipeline* p, uint32_t fi
   p->graph_ok = false;
   p->cfg.use_graphs = 0;
   return cageo_pipeline_run(p, first, count);
+}
+
+// Checkpoint file: "CAGEOCK1", int32 W, H, uint64 seed, uint32 next
+// realization, then W*H uint32 counts (native byte order).
+extern "C" cageo_status cageo_pipeline_save(cageo_pipeline* p, const char* path,
+                                            uint32_t next_realization) {
+  CAGEO_CHECK_ARG(p && path, "null argument");
+  std::vector<uint32_t> h((size_t)p->N);
+  CAGEO_CUDA(cudaStreamSynchronize(p->stream));
+  CAGEO_CUDA(cudaMemcpy(h.data(), p->counts, 4 * (size_t)p->N, cudaMemcpyDeviceToHost));
+  FILE* f = std::fopen(path, "wb");
+  if (!f) {
+    set_error("unable to open \"%s\" for writing", path);
+    return CAGEO_ERR_IO;
+  }
+  const int32_t wh[2] = {p->W, p->H};
+  const uint64_t seed = p->cfg.seed;
+  bool ok = std::fwrite("CAGEOCK1", 1, 8, f) == 8 && std::fwrite(wh, 4, 2, f) == 2 &&
+            std::fwrite(&seed, 8, 1, f) == 1 && std::fwrite(&next_realization, 4, 1, f) == 1 &&
+            std::fwrite(h.data(), 4, h.size(), f) == h.size();
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) {
+    set_error("short write to \"%s\"", path);
+    return CAGEO_ERR_IO;
+  }
+  return CAGEO_OK;
+}
+
+extern "C" cageo_status cageo_pipeline_load(cageo_pipeline* p, const char* path,
+                                            uint32_t* next_realization) {
+  CAGEO_CHECK_ARG(p && path && next_realization, "null argument");
+  FILE* f = std::fopen(path, "rb");
+  if (!f) {
+    set_error("unable to open checkpoint \"%s\"", path);
+    return CAGEO_ERR_IO;
+  }
+  char magic[8];
+  int32_t wh[2];
+  uint64_t seed = 0;
+  uint32_t next = 0;
+  std::vector<uint32_t> h((size_t)p->N);
+  bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "CAGEOCK1", 8) == 0 &&
+            std::fread(wh, 4, 2, f) == 2 && std::fread(&seed, 8, 1, f) == 1 &&
+            std::fread(&next, 4, 1, f) == 1;
+  if (ok && (wh[0] != p->W || wh[1] != p->H || seed != p->cfg.seed)) {
+    std::fclose(f);
+    set_error("checkpoint \"%s\" is for a %dx%d grid with seed %llu", path, wh[0], wh[1],
+              (unsigned long long)seed);
+    return CAGEO_ERR_FORMAT;
+  }
+  ok = ok && std::fread(h.data(), 4, h.size(), f) == h.size();
+  std::fclose(f);
+  if (!ok) {
+    set_error("\"%s\" is not a complete checkpoint", path);
+    return CAGEO_ERR_FORMAT;
+  }
+  CAGEO_CUDA(cudaStreamSynchronize(p->stream));
+  CAGEO_CUDA(cudaMemcpy(p->counts, h.data(), 4 * (size_t)p->N, cudaMemcpyHostToDevice));
+  *next_realization = next;
+  return CAGEO_OK;
 }
 
 extern "C" cageo_status cageo_pipeline_counts_device(cageo_pipeline* p, float* d_out) {

@@ -214,6 +214,14 @@ cageo_status cageo_pipeline_counts_bytes(cageo_pipeline* p, uint8_t* h_out);
 cageo_status cageo_pipeline_last_stages(cageo_pipeline* p, float* h_filled,
                                         int8_t* h_dir, int* h_label);
 cageo_status cageo_pipeline_reset_counts(cageo_pipeline* p);
+/* Checkpoint / resume of a long Monte Carlo run (no counterpart in the
+ * reference, whose only persistence is the per-frame output,
+ * src/main.cpp:250-256): the count grid, the seed and the next realization
+ * number.  Loading refuses a checkpoint of another grid size or seed. */
+cageo_status cageo_pipeline_save(cageo_pipeline* p, const char* path,
+                                 uint32_t next_realization);
+cageo_status cageo_pipeline_load(cageo_pipeline* p, const char* path,
+                                 uint32_t* next_realization);
 cudaStream_t cageo_pipeline_stream(cageo_pipeline* p);
 /* One realization with CUDA events between stages (fused path, no graph);
  * it is accumulated like any other.  h_ms[0..5]: noise, front

@@ -147,3 +147,21 @@ def test_drainage_cli_jpeg(cuda, tmp_path):
     back = decode(str(tmp_path / "c.jpg"))
     assert back.shape == img.shape
     assert np.mean(np.abs(back.astype(int) - img.astype(int))) < 12
+
+
+def test_drainage_cli_checkpoint_resume(cuda, tmp_path):
+    from cageo_gb300 import _build, api
+    dem, streams = make_case(80, 64, seed=24)
+    d = _write_inputs(tmp_path, dem, streams)
+    base = [_build.DRAINAGE, "--dem-path", str(d), "--seed", "8"]
+    full = subprocess.run(base + ["-i", "4", "-o", "full.bin"], cwd=tmp_path, capture_output=True)
+    assert full.returncode == 0
+    part = subprocess.run(base + ["-i", "2", "--checkpoint", "ck.bin"], cwd=tmp_path,
+                          capture_output=True)
+    assert part.returncode == 0
+    rest = subprocess.run(base + ["-i", "4", "--resume", "ck.bin", "-o", "resumed.bin"],
+                          cwd=tmp_path, capture_output=True, text=True)
+    assert rest.returncode == 0 and "Resuming at realization 2" in rest.stdout
+    a = api.read_raster(str(tmp_path / "full.bin"), dem.shape)
+    b = api.read_raster(str(tmp_path / "resumed.bin"), dem.shape)
+    assert np.array_equal(a, b)

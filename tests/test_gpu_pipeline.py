@@ -72,3 +72,20 @@ def test_pipeline_graph_equals_direct(cuda):
     b.run(0, 6)
     assert np.array_equal(a.counts(), b.counts())
     assert a.counts().max() <= 6
+
+
+def test_checkpoint_resume(cuda, tmp_path):
+    from cageo_gb300 import api
+    dem, streams = make_case(120, 90, seed=31)
+    a = api.Pipeline(dem, streams, seed=4)
+    a.run(0, 5)
+    b = api.Pipeline(dem, streams, seed=4)
+    b.run(0, 3)
+    b.save(str(tmp_path / "ck.bin"), 3)
+    c = api.Pipeline(dem, streams, seed=4)
+    assert c.load(str(tmp_path / "ck.bin")) == 3
+    c.run(3, 2)
+    assert np.array_equal(a.counts(), c.counts())
+    other = api.Pipeline(dem, streams, seed=5)
+    with pytest.raises(api.CageoError):
+        other.load(str(tmp_path / "ck.bin"))
