@@ -18,8 +18,14 @@ from . import _build
 FILTER_EXPONENTIAL = 0
 FILTER_GAUSSIAN = 1
 FILL_CPU_COMPAT = 0
+FILL_EXACT = 1
+ROUTE_CPU_COMPAT = 0
+ROUTE_GPU_ORDER = 1
+TRACE_CPU_COMPAT = 0
+TRACE_DEAD_END_ERROR = 1
 OUTSIDE = -9999
 LAKE = -9998
+ERROR = -9996
 
 
 class CageoError(RuntimeError):
@@ -34,7 +40,8 @@ class PipelineConfig(ctypes.Structure):
                 ("practical_range", ctypes.c_float), ("error_mean", ctypes.c_float),
                 ("error_stddev", ctypes.c_float), ("bevel_radius", ctypes.c_int),
                 ("nodata_dem", ctypes.c_float), ("nodata_stream", ctypes.c_float),
-                ("seed", ctypes.c_uint64), ("use_graphs", ctypes.c_int)]
+                ("seed", ctypes.c_uint64), ("use_graphs", ctypes.c_int),
+                ("fill_mode", ctypes.c_int)]
 
 
 class RasterInfo(ctypes.Structure):
@@ -60,8 +67,10 @@ _SIGS = {
     "cageo_pitfill_static": ([_vp, _vp, _i, _i, _f, _i, _vp], _i),
     "cageo_route_workspace_size": ([_i, _i], _sz),
     "cageo_route_d8": ([_vp, _vp, _vp, _i, _i, _vp, _sz, _vp], _i),
+    "cageo_route_d8_mode": ([_vp, _vp, _vp, _i, _i, _f, _i, _vp, _sz, _vp], _i),
     "cageo_trace_workspace_size": ([_i, _i], _sz),
     "cageo_trace": ([_vp, _vp, _vp, _i, _i, _vp, _sz, _vp], _i),
+    "cageo_trace_mode": ([_vp, _vp, _vp, _i, _i, _i, _vp, _sz, _vp], _i),
     "cageo_border_accumulate": ([_vp, _vp, _i, _i, _vp], _i),
     "cageo_pipeline_create": ([ctypes.POINTER(_vp), ctypes.POINTER(PipelineConfig), _vp, _vp], _i),
     "cageo_pipeline_create_device": ([ctypes.POINTER(_vp), ctypes.POINTER(PipelineConfig), _vp,
@@ -182,36 +191,38 @@ def stream_burn(dem, streams, bevel_radius=2, nodata_dem=-9999.0, nodata_stream=
     return dem
 
 
-def pitfill(dem, nodata_dem=-9999.0, workspace=None):
-    """Quantizes `dem` in place (as the reference does) and returns the filled grid."""
+def pitfill(dem, nodata_dem=-9999.0, workspace=None, mode=FILL_CPU_COMPAT):
+    """Returns the filled grid.  CPU_COMPAT quantizes `dem` in place (as the
+    reference's CPU path does); EXACT leaves it unchanged."""
     import torch
     _grid(dem, torch.float32, "dem")
     H, W = dem.shape
     filled = torch.empty_like(dem)
     ws, wsb = (None, 0) if workspace is None else (_ptr(workspace), workspace.numel())
-    _check(lib().cageo_pitfill(_ptr(dem), _ptr(filled), W, H, nodata_dem, FILL_CPU_COMPAT, ws, wsb,
+    _check(lib().cageo_pitfill(_ptr(dem), _ptr(filled), W, H, nodata_dem, mode, ws, wsb,
                                _stream()))
     return filled
 
 
-def route_d8(filled, with_flatdist=False):
+def route_d8(filled, with_flatdist=False, mode=ROUTE_CPU_COMPAT, nodata_dem=-9999.0):
     import torch
     _grid(filled, torch.float32, "filled")
     H, W = filled.shape
     d = torch.empty((H, W, 2), dtype=torch.int8, device=filled.device)
     fd = torch.empty((H, W), dtype=torch.int32, device=filled.device) if with_flatdist else None
-    _check(lib().cageo_route_d8(_ptr(filled), _ptr(d), _ptr(fd) if fd is not None else None, W, H,
-                                None, 0, _stream()))
+    _check(lib().cageo_route_d8_mode(_ptr(filled), _ptr(d), _ptr(fd) if fd is not None else None,
+                                     W, H, nodata_dem, mode, None, 0, _stream()))
     return (d, fd) if with_flatdist else d
 
 
-def trace(dirs, streams):
+def trace(dirs, streams, mode=TRACE_CPU_COMPAT):
     import torch
     _grid(dirs, torch.int8, "dirs")
     _grid(streams, torch.float32, "streams")
     H, W = streams.shape
     lab = torch.empty((H, W), dtype=torch.int32, device=streams.device)
-    _check(lib().cageo_trace(_ptr(dirs), _ptr(streams), _ptr(lab), W, H, None, 0, _stream()))
+    _check(lib().cageo_trace_mode(_ptr(dirs), _ptr(streams), _ptr(lab), W, H, mode, None, 0,
+                                  _stream()))
     return lab
 
 
@@ -235,12 +246,13 @@ class Pipeline:
 
     def __init__(self, dem, streams, cell_size=10.0, filter_model=FILTER_GAUSSIAN,
                  practical_range=60.0, error_mean=0.0, error_stddev=1.0, bevel_radius=2,
-                 nodata_dem=-9999.0, nodata_stream=-9999.0, seed=0, use_graphs=True):
+                 nodata_dem=-9999.0, nodata_stream=-9999.0, seed=0, use_graphs=True,
+                 fill_mode=FILL_CPU_COMPAT):
         H, W = dem.shape
         self.shape = (H, W)
         cfg = PipelineConfig(W, H, cell_size, filter_model, practical_range, error_mean,
                              error_stddev, bevel_radius, nodata_dem, nodata_stream, seed,
-                             1 if use_graphs else 0)
+                             1 if use_graphs else 0, fill_mode)
         self._p = ctypes.c_void_p()
         if isinstance(dem, np.ndarray):
             d = np.ascontiguousarray(dem, np.float32)

@@ -15,7 +15,10 @@
 //
 // Additive options: --seed N (default: the current time, like the
 // reference's time(NULL)+iteration seeding), --bevel-radius N (2; the
-// reference has no flag for it), --no-graphs.  Output files go to the
+// reference has no flag for it), --no-graphs, --fill cpu|exact (cpu: the
+// reference CPU path's semantics, the default; exact: its GPU path's exact
+// float fill, flat order and dead-end handling), --checkpoint FILE,
+// --resume FILE.  Output files go to the
 // working directory under the stem of -o (the reference keeps only the
 // stem).  This driver runs on the GPU only; --cpu
 // is refused rather than silently using another implementation.
@@ -32,7 +35,7 @@ namespace {
 
 struct Options {
   std::string dem = "dem10", stream = "streams", dem_path = "DEM", stream_path = "DEM";
-  std::string filter = "Gaussian", output_file, output_option, checkpoint, resume;
+  std::string filter = "Gaussian", output_file, output_option, checkpoint, resume, fill = "cpu";
   float range = 60.0f, mean = 0.0f, sd = 1.0f;
   int iterations = 10, bevel = 2;
   bool gpu = true, cpu = false, graphs = true, have_seed = false;
@@ -59,6 +62,7 @@ void usage() {
       "  --seed arg                   Noise seed (default: current time)\n"
       "  --bevel-radius arg (=2)      Stream burning bevel radius (1..5)\n"
       "  --no-graphs                  Launch kernels directly instead of a CUDA graph\n"
+      "  --fill arg (=cpu)            cpu: CPU-path semantics; exact: GPU-path exact float fill\n"
       "  --checkpoint arg             Save counts + next realization here after each output\n"
       "  --resume arg                 Continue from a checkpoint (same grid and --seed)\n");
 }
@@ -99,6 +103,13 @@ int parse(int argc, char** argv, Options* o) {
     else if (a == "--seed") { if (!next(&v)) return 1; o->seed = std::strtoull(v.c_str(), nullptr, 10); o->have_seed = true; }
     else if (a == "--bevel-radius") { if (!next(&v)) return 1; o->bevel = std::atoi(v.c_str()); }
     else if (a == "--no-graphs") { o->graphs = false; }
+    else if (a == "--fill") {
+      if (!next(&o->fill)) return 1;
+      if (o->fill != "cpu" && o->fill != "exact") {
+        std::fprintf(stderr, "--fill must be 'cpu' or 'exact'\n");
+        return 1;
+      }
+    }
     else if (a == "--checkpoint") { if (!next(&o->checkpoint)) return 1; }
     else if (a == "--resume") { if (!next(&o->resume)) return 1; }
     else { std::fprintf(stderr, "unrecognised option '%s'\n", argv[i]); return 1; }
@@ -186,6 +197,7 @@ int main(int argc, char** argv) {
   cfg.nodata_stream = si.nodata_value;
   cfg.seed = o.have_seed ? o.seed : (unsigned long long)std::time(nullptr);
   cfg.use_graphs = o.graphs ? 1 : 0;
+  cfg.fill_mode = o.fill == "exact" ? CAGEO_FILL_EXACT : CAGEO_FILL_CPU_COMPAT;
   std::printf("Seed: %llu\n", (unsigned long long)cfg.seed);
   cageo_pipeline* p = nullptr;
   if (cageo_pipeline_create(&p, &cfg, dem.data(), streams.data())) return fail("pipeline");

@@ -25,6 +25,7 @@ struct FrontParams {
   unsigned int* min_ord;   // ordered-uint min of q (pit-fill minE)
   int* anomaly;            // set when the precomputed burn factor may not apply
   float nodata_dem;
+  int quantize;            // 1: the CPU fill's 1 mm quantization; 0: raw (exact fill)
   float factor[kMaxBurnClasses + 1];  // factor[0] unused
 };
 
@@ -41,7 +42,7 @@ __device__ inline float front_epilogue(const FrontParams& p, int64_t i,
   }
   int k = c & 0x1f;
   if (k) v = __fmul_rn(v, p.factor[k]);
-  float q = fill_quantize(v, p.nodata_dem);
+  float q = p.quantize ? fill_quantize(v, p.nodata_dem) : v;
   p.q[i] = q;
   return q;
 }

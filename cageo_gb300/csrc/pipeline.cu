@@ -3,7 +3,9 @@
 //
 // A realization is: noise (Philox) -> fused convolution + realistic DEM +
 // burning + quantization (front) -> pit fill -> routing -> tracing ->
-// border counts.  The launch sequence of one realization reads the
+// border counts.  In exact mode the front does not quantize and the fill,
+// routing and tracing follow the reference's GPU path instead of its CPU
+// path.  The launch sequence of one realization reads the
 // realization number from device memory, so it is captured once in a CUDA
 // graph and replayed; the data-dependent loops (fill passes, flat BFS
 // layers, pointer jumps) run inside persistent kernels and need no host
@@ -122,6 +124,27 @@ void free_all(cageo_pipeline* p) {
   if (p->stream) cudaStreamDestroy(p->stream);
 }
 
+bool exact_mode(const cageo_pipeline* p) { return p->cfg.fill_mode == CAGEO_FILL_EXACT; }
+
+// Fill, routing and tracing of the current realization in the pipeline's
+// mode; p->q holds the (quantized or raw) burned realistic DEM.
+cageo_status enqueue_fill(cageo_pipeline* p) {
+  if (exact_mode(p))
+    return fill_run_exact(p->q, p->filled, p->fw, p->cfg.nodata_dem, nullptr, p->stream);
+  return fill_run(p->q, p->filled, p->fw, p->cfg.nodata_dem, p->stream);
+}
+
+cageo_status enqueue_route(cageo_pipeline* p) {
+  return route_run(p->filled, p->dir, p->flatdist, p->rw, p->stream,
+                   exact_mode(p) ? CAGEO_ROUTE_GPU_ORDER : CAGEO_ROUTE_CPU_COMPAT,
+                   p->cfg.nodata_dem);
+}
+
+cageo_status enqueue_trace(cageo_pipeline* p) {
+  return trace_run(p->dir, p->streams, p->label, p->tw, p->stream,
+                   exact_mode(p) ? CAGEO_TRACE_DEAD_END_ERROR : CAGEO_TRACE_CPU_COMPAT);
+}
+
 // Launch sequence of one realization on the fast path.  The realization
 // number is read from dscal[0] by the noise kernel.
 cageo_status enqueue_fast(cageo_pipeline* p) {
@@ -133,9 +156,9 @@ cageo_status enqueue_fast(cageo_pipeline* p) {
     return st;
   if ((st = launch_front(p->noise, p->W, p->H, c.filter_model, p->filter, p->radius, p->fp, s)))
     return st;
-  if ((st = fill_run(p->q, p->filled, p->fw, c.nodata_dem, s))) return st;
-  if ((st = route_run(p->filled, p->dir, p->flatdist, p->rw, s))) return st;
-  if ((st = trace_run(p->dir, p->streams, p->label, p->tw, s))) return st;
+  if ((st = enqueue_fill(p))) return st;
+  if ((st = enqueue_route(p))) return st;
+  if ((st = enqueue_trace(p))) return st;
   dim3 b(32, 8), g((p->W + 31) / 32, (p->H + 7) / 8);
   border_gated_kernel<<<g, b, 0, s>>>(p->label, p->counts, p->W, p->H, (const int*)p->dscal + 1);
   realization_end_kernel<<<1, 32, 0, s>>>(p->dscal, (int*)p->dscal + 1, p->dscal + 3,
@@ -158,10 +181,10 @@ cageo_status run_stage_path(cageo_pipeline* p, uint32_t r) {
   if ((st = launch_burn_stage(p->tmp, p->q, p->streams, p->W, p->H, c.bevel_radius, c.nodata_dem,
                               c.nodata_stream, s)))
     return st;
-  if ((st = fill_quantize_min(p->q, p->fw, c.nodata_dem, s))) return st;
-  if ((st = fill_run(p->q, p->filled, p->fw, c.nodata_dem, s))) return st;
-  if ((st = route_run(p->filled, p->dir, p->flatdist, p->rw, s))) return st;
-  if ((st = trace_run(p->dir, p->streams, p->label, p->tw, s))) return st;
+  if (!exact_mode(p) && (st = fill_quantize_min(p->q, p->fw, c.nodata_dem, s))) return st;
+  if ((st = enqueue_fill(p))) return st;
+  if ((st = enqueue_route(p))) return st;
+  if ((st = enqueue_trace(p))) return st;
   if ((st = border_u32(p->label, p->counts, p->W, p->H, s))) return st;
   return CAGEO_OK;
 }
@@ -185,6 +208,8 @@ cageo_status create_common(cageo_pipeline** out, const cageo_pipeline_config* cf
                       cfg->filter_model == CAGEO_FILTER_EXPONENTIAL,
                   "filter model");
   CAGEO_CHECK_ARG(cfg->bevel_radius >= 1 && cfg->bevel_radius <= 5, "bevel radius must be 1..5");
+  CAGEO_CHECK_ARG(cfg->fill_mode == CAGEO_FILL_CPU_COMPAT || cfg->fill_mode == CAGEO_FILL_EXACT,
+                  "fill mode");
   CAGEO_CHECK_ARG(cfg->cell_size > 0 && cfg->practical_range > 0, "range and cell size");
   const int r = cageo_filter_radius(cfg->practical_range, cfg->cell_size);
   CAGEO_CHECK_ARG(r >= 0 && r < W && r < H, "filter radius must be below the grid size");
@@ -245,6 +270,7 @@ cageo_status create_common(cageo_pipeline** out, const cageo_pipeline_config* cf
   p->fp.min_ord = fill_min_slot(p->fw);
   p->fp.anomaly = (int*)p->dscal + 1;
   p->fp.nodata_dem = cfg->nodata_dem;
+  p->fp.quantize = cfg->fill_mode == CAGEO_FILL_EXACT ? 0 : 1;
   PCUDA(cudaStreamSynchronize(s));
 #undef PCUDA
   *out = p;
@@ -365,11 +391,11 @@ extern "C" cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t reali
     if ((st = launch_front(p->noise, p->W, p->H, c.filter_model, p->filter, p->radius, p->fp, s)))
       break;
     cudaEventRecord(ev[2], s);
-    if ((st = fill_run(p->q, p->filled, p->fw, c.nodata_dem, s))) break;
+    if ((st = enqueue_fill(p))) break;
     cudaEventRecord(ev[3], s);
-    if ((st = route_run(p->filled, p->dir, p->flatdist, p->rw, s))) break;
+    if ((st = enqueue_route(p))) break;
     cudaEventRecord(ev[4], s);
-    if ((st = trace_run(p->dir, p->streams, p->label, p->tw, s))) break;
+    if ((st = enqueue_trace(p))) break;
     cudaEventRecord(ev[5], s);
     dim3 b(32, 8), g((p->W + 31) / 32, (p->H + 7) / 8);
     border_gated_kernel<<<g, b, 0, s>>>(p->label, p->counts, p->W, p->H,

@@ -1,5 +1,8 @@
 // pitfill.cu -- A6 pit filling with the semantics of the reference's CPU
-// path (src/pitfilling/PitFillingAlgorithmCPUOpenMP.h:68-242).
+// path (src/pitfilling/PitFillingAlgorithmCPUOpenMP.h:68-242), and the exact
+// float fill of its GPU path (src/pitfilling/PitFillingAlgorithmGPUCUDA.cu:
+// 201-381) as a second mode: flood A alone on the unquantized grid, every
+// outlet relaying, unreached cells ending at the GPU path's 99990000.
 //
 // The CPU fill is a bucket priority-flood over 1 mm levels in which a
 // popped cell expands its neighbours only if its value v survives
@@ -541,6 +544,32 @@ __global__ void fill_init_kernel(const float* __restrict__ q, float* __restrict_
   if ((f & FOUTLET) && !(f & FNONPASS)) tseed[(y / kTile) * tiles_x + x / kTile] = 1;
 }
 
+// Exact mode (the reference's GPU fill, src/pitfilling/PitFillingAlgorithmGPUCUDA.cu:201-231):
+// NODATA cells keep NODATA and never relay; border cells and cells equal to
+// 0 are outlets that keep their elevation and relay it; every other cell
+// starts at +inf, or at a warm-start value no lower than its elevation.
+__global__ void fill_init_exact_kernel(const float* __restrict__ v, float* __restrict__ Wg,
+                                       uint8_t* __restrict__ F, const float* __restrict__ warm,
+                                       uint8_t* __restrict__ tseed, int tiles_x, int W, int H,
+                                       float nodata) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)W * H) return;
+  int x = (int)(i % W), y = (int)(i / W);
+  const float e = v[i];
+  uint8_t f = 0;
+  if (e == nodata) f = FNODATA;
+  else if (x == 0 || y == 0 || x == W - 1 || y == H - 1 || e == 0.0f) f = FOUTLET;
+  F[i] = f;
+  Wg[i] = f ? e : (warm ? fmaxf(warm[i], e) : kInf);
+  if (f == FOUTLET) tseed[(y / kTile) * tiles_x + x / kTile] = 1;
+}
+
+// Cells no outlet reaches keep the reference's initial value.
+__global__ void fill_final_exact_kernel(float* __restrict__ Wg, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && Wg[i] == kInf) Wg[i] = 99990000.0f;
+}
+
 // Between the floods: keep flood A's result (lower bound) in aux and
 // FBELOWA, confirm non-passable cells reached at a level >= q, reset W.
 // Also clears the worklist counts: flood A's last count slot is the one
@@ -640,6 +669,27 @@ cageo_status fill_run(const float* q, float* filled, const FillWork& w, float no
   return CAGEO_OK;
 }
 
+cageo_status fill_run_exact(const float* v, float* filled, const FillWork& w, float nodata,
+                            const float* warm, cudaStream_t s) {
+  const int64_t n = (int64_t)w.W * w.H;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  const size_t nt = (size_t)w.tiles_x * w.tiles_y;
+  // A warm start may hold values above the answer anywhere: every tile is
+  // visited on the first pass.
+  CAGEO_CUDA(cudaMemsetAsync(w.tseed, warm ? 1 : 0, nt, s));
+  fill_init_exact_kernel<<<blocks, 256, 0, s>>>(v, filled, w.flags, warm, w.tseed, w.tiles_x,
+                                                w.W, w.H, nodata);
+  CAGEO_CUDA(cudaGetLastError());
+  CAGEO_CUDA(cudaMemsetAsync(w.tdone, 0, nt, s));
+  CAGEO_CUDA(cudaMemsetAsync(w.tconv, 0, nt, s));
+  FloodArgs a{v, filled, w};
+  cageo_status st = launch_flood<0>(a, s);
+  if (st) return st;
+  fill_final_exact_kernel<<<blocks, 256, 0, s>>>(filled, n);
+  CAGEO_CUDA(cudaGetLastError());
+  return CAGEO_OK;
+}
+
 cageo_status fill_quantize_min(float* d, const FillWork& w, float nodata, cudaStream_t s) {
   const int64_t n = (int64_t)w.W * w.H;
   quantize_min_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, n, nodata, w.scal + S_MIN);
@@ -690,14 +740,18 @@ extern "C" cageo_status cageo_pitfill(float* d_dem, float* d_filled, int W, int 
   CAGEO_CHECK_ARG(d_dem && d_filled && valid_dims(W, H), "pointers and size");
   CAGEO_CHECK_ARG(W <= 65535 && H <= 65535, "width and height must be <= 65535");
   CAGEO_CHECK_ARG(d_dem != d_filled, "the filled grid must not alias the DEM");
-  CAGEO_CHECK_ARG(mode == CAGEO_FILL_CPU_COMPAT, "fill mode");
+  CAGEO_CHECK_ARG(mode == CAGEO_FILL_CPU_COMPAT || mode == CAGEO_FILL_EXACT, "fill mode");
   Scratch ws;
   cageo_status st = ws.acquire(d_workspace, workspace_bytes, fill_workspace_bytes(W, H), stream);
   if (st) return st;
   FillWork w = fill_carve(ws.ptr, W, H);
   if ((st = fill_reset_scalars(w, stream))) return st;
-  if ((st = fill_quantize_min(d_dem, w, nodata_dem, stream))) return st;
-  if ((st = fill_run(d_dem, d_filled, w, nodata_dem, stream))) return st;
+  if (mode == CAGEO_FILL_EXACT) {
+    if ((st = fill_run_exact(d_dem, d_filled, w, nodata_dem, nullptr, stream))) return st;
+  } else {
+    if ((st = fill_quantize_min(d_dem, w, nodata_dem, stream))) return st;
+    if ((st = fill_run(d_dem, d_filled, w, nodata_dem, stream))) return st;
+  }
   CAGEO_CUDA(cudaStreamSynchronize(stream));
   return fill_check_status(w, nullptr);
 }

@@ -32,6 +32,13 @@ FillWork fill_carve(void* base, int W, int H);
 // fill_check_status after the stream has drained.
 cageo_status fill_run(const float* q, float* filled, const FillWork& w,
                       float nodata, cudaStream_t s);
+// Exact float fill of v (the reference's GPU path): no quantization, no
+// minimum needed.  `warm` (may be null): per-cell start values; a start
+// below the answer anywhere gives a lower fixpoint, so callers verify a
+// warm-started result (every cell must drain to an outlet) and rerun cold
+// where it fails.
+cageo_status fill_run_exact(const float* v, float* filled, const FillWork& w, float nodata,
+                            const float* warm, cudaStream_t s);
 // Quantize d in place (the reference's step (i)) and reduce its minimum
 // into the scalar block.
 cageo_status fill_quantize_min(float* d, const FillWork& w, float nodata,

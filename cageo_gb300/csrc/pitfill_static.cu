@@ -60,7 +60,7 @@ extern "C" cageo_status cageo_pitfill_static(float* d_dem, float* d_filled, int 
   CAGEO_CHECK_ARG(d_dem && d_filled && valid_dims(W, H), "pointers and size");
   CAGEO_CHECK_ARG(W <= 65535 && H <= 65535, "width and height must be <= 65535");
   CAGEO_CHECK_ARG(d_dem != d_filled, "the filled grid must not alias the DEM");
-  CAGEO_CHECK_ARG(mode == CAGEO_FILL_CPU_COMPAT, "fill mode");
+  CAGEO_CHECK_ARG(mode == CAGEO_FILL_CPU_COMPAT || mode == CAGEO_FILL_EXACT, "fill mode");
   const size_t need = fill_workspace_bytes(W, H);
   if (need > kStaticFillBytes) {
     set_error("a %d x %d grid needs %zu bytes of fill scratch; the static scratch holds %zu "
@@ -73,8 +73,12 @@ extern "C" cageo_status cageo_pitfill_static(float* d_dem, float* d_filled, int 
   if (st) return st;
   FillWork w = fill_carve(base, W, H);
   if ((st = fill_reset_scalars(w, stream))) return st;
-  if ((st = fill_quantize_min(d_dem, w, nodata_dem, stream))) return st;
-  if ((st = fill_run(d_dem, d_filled, w, nodata_dem, stream))) return st;
+  if (mode == CAGEO_FILL_EXACT) {
+    if ((st = fill_run_exact(d_dem, d_filled, w, nodata_dem, nullptr, stream))) return st;
+  } else {
+    if ((st = fill_quantize_min(d_dem, w, nodata_dem, stream))) return st;
+    if ((st = fill_run(d_dem, d_filled, w, nodata_dem, stream))) return st;
+  }
   CAGEO_CUDA(cudaStreamSynchronize(stream));
   return fill_check_status(w, nullptr);
 }

@@ -16,6 +16,14 @@
 // that hold flat cells until stable, and queues the neighbouring tiles when
 // its border changed), and the directions by one final pass that applies
 // the last-match rule to the finished distances.
+//
+// The GPU-order mode follows the reference's GPU routing instead
+// (src/flowrouting/FlowRoutingAlgorithmGPUCUDAOriginal.cu:200-271 and
+// :391-437): NODATA cells get flatDist -3 and are skipped as neighbours;
+// layer 1 may drain into any cell with a negative flatDist (streams too)
+// whose non-NODATA elevation is <= the flat cell's; a later layer k drains
+// into a cell of an earlier layer; the FIRST match in the order N, W, E,
+// S, NW, NE, SW, SE wins.  The layer numbers are again BFS distances.
 #include <algorithm>
 #include "common.cuh"
 #include "routing.cuh"
@@ -24,6 +32,7 @@
 namespace cageo {
 
 constexpr int kFlatInf = 0x3fffffff;
+constexpr int kOffGrid = (int)0x80000000;  // staged code of a cell outside the grid
 enum : int { R_NFLAT = 0, R_ERR = 3, R_LIST = 4, R_LAYERS = 7, R_US_BFS = 8, R_PASSES = 9,
              R_BAR_COUNT = kBarCountSlot, R_BAR_GEN = kBarGenSlot, R_SIZE = kScalarSlots };
 constexpr int kFT = 32;          // flat tile size
@@ -69,9 +78,11 @@ __device__ __forceinline__ void gather8(const float* __restrict__ dem, const int
   }
 }
 
-// Steepest-descent pass.  flatdist: -1 direction, -2 stream, kFlatInf flat.
+// Steepest-descent pass.  flatdist: -1 direction, -2 stream, -3 NODATA
+// (GPU order only), kFlatInf flat.
+template <bool GPU>
 __global__ void d8_kernel(const float* __restrict__ dem, char2* __restrict__ dir,
-                          int* __restrict__ fd, RouteWork w) {
+                          int* __restrict__ fd, RouteWork w, float nodata) {
   const int W = w.W, H = w.H;
   int x = blockIdx.x * blockDim.x + threadIdx.x;
   int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -89,13 +100,18 @@ __global__ void d8_kernel(const float* __restrict__ dem, char2* __restrict__ dir
     if (c == 0.0f) {
       dir[i] = make_char2(0, 0);
       fd[i] = -2;
+    } else if (GPU && c == nodata) {
+      dir[i] = make_char2(0, 0);
+      fd[i] = -3;
     } else {
       float steepest = 0.0f;
       int sdx = 0, sdy = 0;
 #pragma unroll
       for (int n = 0; n < 8; n++) {
         const int dx = d8_dx(n), dy = d8_dy(n);
-        float s = __fsub_rn(c, dem[(int64_t)(y + dy) * W + (x + dx)]);
+        const float e = dem[(int64_t)(y + dy) * W + (x + dx)];
+        if (GPU && e == nodata) continue;
+        float s = __fsub_rn(c, e);
         // A diagonal drop only shrinks when divided by sqrt(2), so the
         // (slow, correctly rounded) division is needed only when the
         // undivided drop already beats the steepest so far.
@@ -121,10 +137,14 @@ __global__ void d8_kernel(const float* __restrict__ dem, char2* __restrict__ dir
 }
 
 // ---- flat distances by tile relaxation ----------------------------------
-// Staged value of a cell for its neighbours: 0 for a cell with a direction
-// (layer 0), the current distance of a flat cell, "infinite" otherwise.
-__device__ __forceinline__ int flat_relay(int code) {
-  return code == -1 ? 0 : (code >= 0 ? code : kFlatInf);
+// Staged value of a cell for its neighbours: 0 for a cell a first-layer flat
+// cell may drain into (CPU: a direction; GPU order: a direction or a stream,
+// with an elevation that is not NODATA), the current distance of a flat
+// cell, "infinite" otherwise.
+__device__ __forceinline__ int flat_relay(int code, float e, bool gpu, float nodata) {
+  if (code >= 0) return code;
+  if (gpu) return ((code == -1 || code == -2) && e != nodata) ? 0 : kFlatInf;
+  return code == -1 ? 0 : kFlatInf;
 }
 
 struct FlatSmem {
@@ -165,7 +185,7 @@ __device__ __forceinline__ bool flat_update(FlatSmem& s, int x, int y) {
 }
 
 __device__ void flat_tile(FlatSmem& s, const float* __restrict__ dem, int* fd, const RouteWork& w,
-                          int t, int p, int lane) {
+                          int t, int p, int lane, bool gpu, float nodata) {
   const int W = w.W, H = w.H;
   const int tx = t % w.tiles_x, ty = t / w.tiles_x;
   const int x0 = tx * kFT, y0 = ty * kFT;
@@ -173,14 +193,14 @@ __device__ void flat_tile(FlatSmem& s, const float* __restrict__ dem, int* fd, c
   for (int idx = lane; idx < 34 * 34; idx += 32) {
     const int hy = idx / 34, hx = idx - hy * 34;
     const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
-    int code = -2;
+    int code = kOffGrid;
     float e = 0.0f;
     if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
       const int64_t i = (int64_t)gy * W + gx;
       code = ((volatile int*)fd)[i];
       e = dem[i];
     }
-    s.R[hy * kFRS + hx] = flat_relay(code);
+    s.R[hy * kFRS + hx] = flat_relay(code, e, gpu, nodata);
     s.E[hy * kFRS + hx] = e;
     if (hx >= 1 && hx <= kFT && hy >= 1 && hy <= kFT)
       s.isflat[(hy - 1) * 36 + hx - 1] = (code == kFlatInf || code >= 1) ? 1 : 0;
@@ -251,7 +271,7 @@ __device__ void flat_tile(FlatSmem& s, const float* __restrict__ dem, int* fd, c
 }
 
 __global__ void __launch_bounds__(kFWarps * 32, 1)
-flat_relax_kernel(const float* __restrict__ dem, int* fd, RouteWork w) {
+flat_relax_kernel(const float* __restrict__ dem, int* fd, RouteWork w, int gpu, float nodata) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   FlatSmem& s = reinterpret_cast<FlatSmem*>(smraw)[warp];
@@ -270,7 +290,7 @@ flat_relax_kernel(const float* __restrict__ dem, int* fd, RouteWork w) {
     for (int i = gwarp; i < n; i += nwarps) {
       const int t = full ? i : list[i];
       if (full && !w.tflat[t]) continue;
-      flat_tile(s, dem, fd, w, t, p, lane);
+      flat_tile(s, dem, fd, w, t, p, lane, gpu != 0, nodata);
     }
     if (!grid_barrier(gs, gridDim.x)) break;
     if (vs[R_LIST + (p + 1) % 3] == 0u) break;
@@ -313,6 +333,35 @@ __global__ void flat_dir_kernel(const float* __restrict__ dem, char2* __restrict
   }
 }
 
+// GPU order: the first neighbour in N, W, E, S, NW, NE, SW, SE order that is
+// (layer 1) a non-NODATA cell with a negative flatDist and an elevation <=
+// the cell's, or (layer d > 1) a cell of layers 1..d-1.
+__global__ void flat_dir_gpu_kernel(const float* __restrict__ dem, char2* __restrict__ dir,
+                                    int* __restrict__ fd, RouteWork w, float nodata) {
+  const int W = w.W, H = w.H;
+  const int64_t N = (int64_t)W * H;
+  constexpr int order[8] = {0, 6, 2, 4, 7, 1, 5, 3};  // N W E S NW NE SW SE as D8 indices
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < N;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int d = fd[c];
+    if (d < 1 || d == kFlatInf) continue;
+    int x = (int)(c % (uint32_t)W), y = (int)(c / (uint32_t)W);
+    const float e = dem[c];
+    int nf[8];
+    float ne[8];
+    gather8(dem, fd, W, H, x, y, nf, ne);
+    int got = -1;
+#pragma unroll
+    for (int k = 7; k >= 0; k--) {
+      const int n = order[k];
+      const bool ok = d == 1 ? (nf[n] < 0 && nf[n] != kOffGrid && ne[n] != nodata && ne[n] <= e)
+                             : (nf[n] >= 1 && nf[n] <= d - 1);
+      if (ok) got = n;
+    }
+    if (got >= 0) dir[c] = make_char2((signed char)d8_dx(got), (signed char)d8_dy(got));
+  }
+}
+
 // Unresolved flats end as flatDist 0 with no direction.
 __global__ void flat_final_kernel(int* __restrict__ fd, RouteWork w) {
   const int64_t N = (int64_t)w.W * w.H;
@@ -326,13 +375,15 @@ __global__ void route_scalars_kernel(unsigned int* s) {
 }
 
 cageo_status route_run(const float* filled, int8_t* dir, int* fd, const RouteWork& w,
-                       cudaStream_t s) {
+                       cudaStream_t s, int mode, float nodata) {
+  const bool gpu = mode == CAGEO_ROUTE_GPU_ORDER;
   const size_t nt = (size_t)w.tiles_x * w.tiles_y;
   route_scalars_kernel<<<1, 128, 0, s>>>(w.scal);
   CAGEO_CUDA(cudaMemsetAsync(w.tflat, 0, nt, s));
   CAGEO_CUDA(cudaMemsetAsync(w.queued, 0, nt * 4, s));
   dim3 b(32, 8), g((w.W + 31) / 32, (w.H + 7) / 8);
-  d8_kernel<<<g, b, 0, s>>>(filled, (char2*)dir, fd, w);
+  if (gpu) d8_kernel<true><<<g, b, 0, s>>>(filled, (char2*)dir, fd, w, nodata);
+  else d8_kernel<false><<<g, b, 0, s>>>(filled, (char2*)dir, fd, w, nodata);
   CAGEO_CUDA(cudaGetLastError());
   static int coop = 0;
   const size_t smem = sizeof(FlatSmem) * kFWarps;
@@ -348,14 +399,17 @@ cageo_status route_run(const float* filled, int8_t* dir, int* fd, const RouteWor
   const float* f = filled;
   int* fdp = fd;
   RouteWork wc = w;
-  void* params[] = {(void*)&f, (void*)&fdp, (void*)&wc};
+  int gflag = gpu ? 1 : 0;
+  float nd = nodata;
+  void* params[] = {(void*)&f, (void*)&fdp, (void*)&wc, (void*)&gflag, (void*)&nd};
   CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)flat_relax_kernel, dim3(coop),
                                          dim3(kFWarps * 32), params, smem, s));
   int sms = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const unsigned lb = (unsigned)sms * 16;
-  flat_dir_kernel<<<lb, 256, 0, s>>>(filled, (char2*)dir, fd, w);
+  if (gpu) flat_dir_gpu_kernel<<<lb, 256, 0, s>>>(filled, (char2*)dir, fd, w, nodata);
+  else flat_dir_kernel<<<lb, 256, 0, s>>>(filled, (char2*)dir, fd, w);
   flat_final_kernel<<<lb, 256, 0, s>>>(fd, w);
   CAGEO_CUDA(cudaGetLastError());
   return CAGEO_OK;
@@ -385,10 +439,12 @@ extern "C" size_t cageo_route_workspace_size(int W, int H) {
   return route_workspace_bytes(W, H) + align_up((size_t)W * H * 4, 256);
 }
 
-extern "C" cageo_status cageo_route_d8(const float* d_filled, int8_t* d_dir,
-                                       int* d_flatdist, int W, int H, void* d_workspace,
-                                       size_t workspace_bytes, cudaStream_t stream) {
+extern "C" cageo_status cageo_route_d8_mode(const float* d_filled, int8_t* d_dir,
+                                            int* d_flatdist, int W, int H, float nodata_dem,
+                                            int mode, void* d_workspace, size_t workspace_bytes,
+                                            cudaStream_t stream) {
   CAGEO_CHECK_ARG(d_filled && d_dir && valid_dims(W, H), "pointers and size");
+  CAGEO_CHECK_ARG(mode == CAGEO_ROUTE_CPU_COMPAT || mode == CAGEO_ROUTE_GPU_ORDER, "routing mode");
   Scratch ws;
   cageo_status st = ws.acquire(d_workspace, workspace_bytes,
                                cageo_route_workspace_size(W, H), stream);
@@ -396,7 +452,14 @@ extern "C" cageo_status cageo_route_d8(const float* d_filled, int8_t* d_dir,
   RouteWork w = route_carve(ws.ptr, W, H);
   int* fd = d_flatdist ? d_flatdist
                        : (int*)((char*)ws.ptr + route_workspace_bytes(W, H));
-  if ((st = route_run(d_filled, d_dir, fd, w, stream))) return st;
+  if ((st = route_run(d_filled, d_dir, fd, w, stream, mode, nodata_dem))) return st;
   CAGEO_CUDA(cudaStreamSynchronize(stream));
   return route_check_status(w, nullptr);
+}
+
+extern "C" cageo_status cageo_route_d8(const float* d_filled, int8_t* d_dir,
+                                       int* d_flatdist, int W, int H, void* d_workspace,
+                                       size_t workspace_bytes, cudaStream_t stream) {
+  return cageo_route_d8_mode(d_filled, d_dir, d_flatdist, W, H, -9999.0f,
+                             CAGEO_ROUTE_CPU_COMPAT, d_workspace, workspace_bytes, stream);
 }

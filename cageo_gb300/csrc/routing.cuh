@@ -17,8 +17,10 @@ struct RouteWork {
 };
 size_t route_workspace_bytes(int W, int H);
 RouteWork route_carve(void* base, int W, int H);
+// mode: CAGEO_ROUTE_CPU_COMPAT or CAGEO_ROUTE_GPU_ORDER (nodata is used by
+// the latter only).
 cageo_status route_run(const float* filled, int8_t* dir, int* flatdist,
-                       const RouteWork& w, cudaStream_t s);
+                       const RouteWork& w, cudaStream_t s, int mode, float nodata);
 // stats (3 entries, may be null): flat relaxation passes, flat cells,
 // microseconds of the flat relaxation.
 cageo_status route_check_status(const RouteWork& w, int64_t* stats);
@@ -32,8 +34,10 @@ size_t trace_workspace_bytes(int W, int H);
 TraceWork trace_carve(void* base, int W, int H);
 // is_stream(c) = streams[c] >= 0; the label of a stream terminal is
 // (int)(-streams[c]).
+// mode CAGEO_TRACE_DEAD_END_ERROR: cells whose path ends without an
+// outlet are ERROR instead of taking cell 0's label.
 cageo_status trace_run(const int8_t* dir, const float* streams, int* label,
-                       const TraceWork& w, cudaStream_t s);
+                       const TraceWork& w, cudaStream_t s, int mode);
 cageo_status trace_check_status(const TraceWork& w, int64_t* jumps);
 
 // count[i] += border(label) for float (stage API) or uint32 (pipeline) counts.

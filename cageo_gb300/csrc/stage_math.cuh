@@ -110,5 +110,6 @@ __host__ __device__ constexpr int d8_dy(int n) {
 // Basin labels and flat-distance codes.
 constexpr int kOutside = -9999;
 constexpr int kLake = -9998;
+constexpr int kError = -9996;
 
 }  // namespace cageo

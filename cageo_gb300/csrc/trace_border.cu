@@ -11,7 +11,9 @@
 // all are resolved: O(log path length) grid passes.  A cell without a direction
 // (0,0) is a dead end: the reference's walk never terminates there, leaves
 // the path at 0 and its connect pass then copies the label of cell 0; such
-// cells and label-0 terminals take the label of cell 0 here too.  (The
+// cells and label-0 terminals take the label of cell 0 here too (or, in the
+// dead-end-error mode used with the GPU path's semantics, dead ends and the
+// cells draining into them are ERROR).  (The
 // reference also abandons walks longer than 100000 steps; paths of that
 // length do not occur in these grids and are not modelled.)
 //
@@ -115,16 +117,17 @@ __global__ void __launch_bounds__(kJumpThreads, 8) trace_jump_kernel(int* st, Tr
   if (blockIdx.x == 0 && threadIdx.x == 0) vs[T_JUMPS] = (unsigned int)(pass + 1);
 }
 
-// Labels; dead ends and label-0 terminals take cell 0's label.
+// Labels; label-0 terminals take cell 0's label, and so do dead ends
+// (stuck = 0) unless they are reported as ERROR (stuck = kError).
 __global__ void trace_final_kernel(const int* __restrict__ st, int* __restrict__ label,
-                                   int64_t n) {
+                                   int64_t n, int stuck) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int c = st[i];
-  int l = c == kStuckCode ? 0 : c + 1;
+  int l = c == kStuckCode ? stuck : c + 1;
   if (l >= 0) {
     const int c0 = st[0];
-    const int l0 = c0 == kStuckCode ? 0 : c0 + 1;
+    const int l0 = c0 == kStuckCode ? stuck : c0 + 1;
     l = l0 >= 0 ? 0 : l0;
   }
   label[i] = l;
@@ -135,7 +138,7 @@ __global__ void trace_scalars_kernel(unsigned int* s) {
 }
 
 cageo_status trace_run(const int8_t* dir, const float* streams, int* label,
-                       const TraceWork& w, cudaStream_t s) {
+                       const TraceWork& w, cudaStream_t s, int mode) {
   const int64_t n = (int64_t)w.W * w.H;
   const unsigned blocks = (unsigned)((n + 255) / 256);
   trace_scalars_kernel<<<1, 128, 0, s>>>(w.scal);
@@ -154,7 +157,8 @@ cageo_status trace_run(const int8_t* dir, const float* streams, int* label,
   void* params[] = {(void*)&stp, (void*)&wc};
   CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)trace_jump_kernel, dim3(coop),
                                          dim3(kJumpThreads), params, 0, s));
-  trace_final_kernel<<<blocks, 256, 0, s>>>(w.state, label, n);
+  trace_final_kernel<<<blocks, 256, 0, s>>>(w.state, label, n,
+                                            mode == CAGEO_TRACE_DEAD_END_ERROR ? kError : 0);
   CAGEO_CUDA(cudaGetLastError());
   return CAGEO_OK;
 }
@@ -216,17 +220,27 @@ extern "C" size_t cageo_trace_workspace_size(int W, int H) {
   return trace_workspace_bytes(W, H);
 }
 
-extern "C" cageo_status cageo_trace(const int8_t* d_dir, const float* d_streams,
-                                    int* d_label, int W, int H, void* d_workspace,
-                                    size_t workspace_bytes, cudaStream_t stream) {
+extern "C" cageo_status cageo_trace_mode(const int8_t* d_dir, const float* d_streams,
+                                         int* d_label, int W, int H, int mode,
+                                         void* d_workspace, size_t workspace_bytes,
+                                         cudaStream_t stream) {
   CAGEO_CHECK_ARG(d_dir && d_streams && d_label && valid_dims(W, H), "pointers and size");
+  CAGEO_CHECK_ARG(mode == CAGEO_TRACE_CPU_COMPAT || mode == CAGEO_TRACE_DEAD_END_ERROR,
+                  "tracing mode");
   Scratch ws;
   cageo_status st = ws.acquire(d_workspace, workspace_bytes, trace_workspace_bytes(W, H), stream);
   if (st) return st;
   TraceWork w = trace_carve(ws.ptr, W, H);
-  if ((st = trace_run(d_dir, d_streams, d_label, w, stream))) return st;
+  if ((st = trace_run(d_dir, d_streams, d_label, w, stream, mode))) return st;
   CAGEO_CUDA(cudaStreamSynchronize(stream));
   return trace_check_status(w, nullptr);
+}
+
+extern "C" cageo_status cageo_trace(const int8_t* d_dir, const float* d_streams,
+                                    int* d_label, int W, int H, void* d_workspace,
+                                    size_t workspace_bytes, cudaStream_t stream) {
+  return cageo_trace_mode(d_dir, d_streams, d_label, W, H, CAGEO_TRACE_CPU_COMPAT, d_workspace,
+                          workspace_bytes, stream);
 }
 
 extern "C" cageo_status cageo_border_accumulate(const int* d_label, float* d_count, int W,

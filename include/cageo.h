@@ -45,13 +45,32 @@ typedef int cageo_status;
 #define CAGEO_FILTER_EXPONENTIAL 0
 #define CAGEO_FILTER_GAUSSIAN 1
 
-/* Basin label codes, src/flowtracing/FlowTracingCommon.h:18-19. */
+/* Basin label codes, src/flowtracing/FlowTracingCommon.h:18-21. */
 #define CAGEO_OUTSIDE (-9999)
 #define CAGEO_LAKE (-9998)
+#define CAGEO_ERROR (-9996)
 
 /* Pit-filling modes.  CPU_COMPAT reproduces the reference CPU path
- * (src/pitfilling/PitFillingAlgorithmCPUOpenMP.h:68-242). */
+ * (src/pitfilling/PitFillingAlgorithmCPUOpenMP.h:68-242).  EXACT is the
+ * reference GPU path's exact float fill
+ * (src/pitfilling/PitFillingAlgorithmGPUCUDA.cu:201-381): no quantization;
+ * border cells and cells equal to 0 are outlets; every other cell ends at
+ * the least, over paths from an outlet through non-NODATA cells, of the
+ * largest elevation on the path; cells no path reaches end at 99990000. */
 #define CAGEO_FILL_CPU_COMPAT 0
+#define CAGEO_FILL_EXACT 1
+
+/* Routing modes: the CPU path's flat rules, or the GPU path's
+ * (src/flowrouting/FlowRoutingAlgorithmGPUCUDAOriginal.cu:200-271,391-437:
+ * NODATA skipped, streams are first-layer outlets, first match in
+ * N, W, E, S, NW, NE, SW, SE order). */
+#define CAGEO_ROUTE_CPU_COMPAT 0
+#define CAGEO_ROUTE_GPU_ORDER 1
+
+/* Tracing modes: cells whose path ends without an outlet take cell 0's
+ * label (CPU path), or are CAGEO_ERROR (used with the GPU semantics). */
+#define CAGEO_TRACE_CPU_COMPAT 0
+#define CAGEO_TRACE_DEAD_END_ERROR 1
 
 const char* cageo_version(void);
 /* Text of the last error raised on the calling host thread. */
@@ -111,9 +130,11 @@ cageo_status cageo_stream_burn(float* d_dem, const float* d_streams, int W,
 /* ---- A6 pit filling -----------------------------------------------------
  * Replaces PitFillingAlgorithm::execute(filled, rDem)
  * (src/pitfilling/PitFillingAlgorithm.h:88-98; CPU
- * src/pitfilling/PitFillingAlgorithmCPUOpenMP.h:68-242).  Like the
- * reference, d_dem is quantized to 1/1000 m in place and d_filled receives
- * the filled surface.  W, H <= 65535 (the reference's Cell coordinates). */
+ * src/pitfilling/PitFillingAlgorithmCPUOpenMP.h:68-242; GPU
+ * src/pitfilling/PitFillingAlgorithmGPUCUDA.cu:201-381).  In CPU_COMPAT
+ * mode, like the reference, d_dem is quantized to 1/1000 m in place; in
+ * EXACT mode it is left unchanged.  d_filled receives the filled surface.
+ * W, H <= 65535 (the reference's Cell coordinates). */
 size_t cageo_pitfill_workspace_size(int W, int H);
 cageo_status cageo_pitfill(float* d_dem, float* d_filled, int W, int H,
                            float nodata_dem, int mode, void* d_workspace,
@@ -148,6 +169,14 @@ size_t cageo_route_workspace_size(int W, int H);
 cageo_status cageo_route_d8(const float* d_filled, int8_t* d_dir,
                             int* d_flatdist, int W, int H, void* d_workspace,
                             size_t workspace_bytes, cudaStream_t stream);
+/* Same with a routing mode (CAGEO_ROUTE_*); CAGEO_ROUTE_GPU_ORDER replaces
+ * the reference's FlowRoutingAlgorithm_GPU_CUDA_Original::performFlowRouting
+ * + performFlowRoutingOnFlatSurfaces and also writes flatDist -3 on NODATA
+ * cells.  nodata_dem is used by the GPU order only. */
+cageo_status cageo_route_d8_mode(const float* d_filled, int8_t* d_dir,
+                                 int* d_flatdist, int W, int H, float nodata_dem,
+                                 int mode, void* d_workspace,
+                                 size_t workspace_bytes, cudaStream_t stream);
 
 /* ---- A8 flow tracing ----------------------------------------------------
  * Replaces FlowTracingAlgorithm::execute(trace, flowDir, streams)
@@ -158,6 +187,11 @@ size_t cageo_trace_workspace_size(int W, int H);
 cageo_status cageo_trace(const int8_t* d_dir, const float* d_streams,
                          int* d_label, int W, int H, void* d_workspace,
                          size_t workspace_bytes, cudaStream_t stream);
+/* Same with a tracing mode (CAGEO_TRACE_*). */
+cageo_status cageo_trace_mode(const int8_t* d_dir, const float* d_streams,
+                              int* d_label, int W, int H, int mode,
+                              void* d_workspace, size_t workspace_bytes,
+                              cudaStream_t stream);
 
 /* ---- A9 catchment border ------------------------------------------------
  * Replaces CatchmentBorderAlgorithm::execute(mc, trace)
@@ -184,6 +218,9 @@ typedef struct {
   float nodata_dem, nodata_stream;
   uint64_t seed;
   int use_graphs;          /* capture the per-realization launches in a CUDA graph */
+  int fill_mode;           /* CAGEO_FILL_CPU_COMPAT: the CPU path throughout;
+                              CAGEO_FILL_EXACT: the GPU path's semantics (exact
+                              fill, GPU routing order, dead ends ERROR) */
 } cageo_pipeline_config;
 
 /* h_dem, h_streams: host grids (W*H floats).  The filter is built with

@@ -19,6 +19,7 @@
 #include <vector>
 #include <algorithm>
 #include <cstdio>
+#include <queue>
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -38,6 +39,7 @@ const int kD8Dy[8] = {-1, -1, 0, 1, 1, 1, 0, -1};
 
 const int kOutside = -9999;  // src/flowtracing/FlowTracingCommon.h:18
 const int kLake = -9998;     // src/flowtracing/FlowTracingCommon.h:19
+const int kError = -9996;    // src/flowtracing/FlowTracingCommon.h:21
 const float kSqrt2 = 1.41421356237309505f;  // src/flowrouting/FlowRoutingCommon.h:18
 const int kPrec = 1000;  // src/pitfilling/PitFillingAlgorithmCPUOpenMP.h:38
 
@@ -418,6 +420,213 @@ void orc_border_accumulate(const int* label, float* mc, int W, int H) {
   for (int64_t i = 0; i < N; i++) {
     if (mc[i] != -1.0f) mc[i] = mc[i] + border[i];
   }
+}
+
+// ---- The reference's GPU path semantics ("exact" mode) -------------------
+
+// Pit filling, GPU path: an exact float fill, no quantization.
+// Initialisation, src/pitfilling/PitFillingAlgorithmGPUCUDA.cu:201-231:
+// NODATA cells keep NODATA; border cells and cells equal to STREAM (0) keep
+// their elevation and are the sources; every other cell starts at 99990000.
+// Relaxation, :275-380: a source c lowers each interior neighbour n
+// (1 <= x <= W-2, 1 <= y <= H-2) whose value is not NODATA, is above c's
+// and is not its own elevation, to max(c, dem[n]), and n becomes a source.
+// The limit does not depend on the order of the updates: every reached cell
+// ends at the least, over 8-connected paths of non-NODATA cells from a
+// source, of the largest elevation along the path; unreached cells keep
+// 99990000.  It is computed here by a priority flood on that path maximum.
+int orc_pitfill_exact(const float* dem, float* filled, int W, int H, float nodata) {
+  const int64_t N = (int64_t)W * H;
+  if (W < 1 || H < 1) return -1;
+  typedef std::pair<float, int64_t> E;
+  std::priority_queue<E, std::vector<E>, std::greater<E>> pq;
+  std::vector<uint8_t> done(N, 0);
+  for (int y = 0; y < H; y++)
+    for (int x = 0; x < W; x++) {
+      const int64_t i = (int64_t)y * W + x;
+      const float v = dem[i];
+      if (v == nodata) {
+        filled[i] = v;
+        done[i] = 1;
+      } else if (v == 0.0f || x == 0 || y == 0 || x == W - 1 || y == H - 1) {
+        filled[i] = v;
+        pq.push(E(v, i));
+      } else {
+        filled[i] = 99990000.0f;
+      }
+    }
+  while (!pq.empty()) {
+    const E e = pq.top();
+    pq.pop();
+    const int64_t c = e.second;
+    if (done[c] || e.first != filled[c]) continue;
+    done[c] = 1;
+    const int cx = (int)(c % W), cy = (int)(c / W);
+    for (int n = 0; n < 8; n++) {
+      const int nx = cx + kFillDx[n], ny = cy + kFillDy[n];
+      if (nx <= 0 || nx >= W - 1 || ny <= 0 || ny >= H - 1) continue;
+      const int64_t ni = (int64_t)ny * W + nx;
+      if (done[ni]) continue;
+      const float nv = std::max(filled[c], dem[ni]);
+      if (nv < filled[ni]) {
+        filled[ni] = nv;
+        pq.push(E(nv, ni));
+      }
+    }
+  }
+  return 0;
+}
+
+// Flow routing, GPU path.  First pass,
+// src/flowrouting/FlowRoutingAlgorithmGPUCUDAOriginal.cu:200-271: border
+// cells point outward (flatDist -1, whatever their value), cells equal to 0
+// are streams (-2), NODATA cells -3; others take the steepest strictly
+// descending non-NODATA neighbour in N..NW order (diagonal drops divided by
+// sqrt 2, first maximum wins).  Flats, :391-437 with the loop at :98-121:
+// iteration k = 1, 2, ... gives each still-flat cell (flatDist 0) the first
+// neighbour, in the order N, W, E, S, NW, NE, SW, SE, that either has a
+// negative flatDist and a non-NODATA elevation <= the cell's, or was given
+// a direction in an earlier iteration (1 <= flatDist <= k-1); flatDist = k.
+// Values written in iteration k are not read in it, so applying them after
+// the scan is the same.  The reference repeats until every flat cell has a
+// direction; flats without an outlet would never finish there and are left
+// at flatDist 0 with no direction here.
+void orc_flow_route_gpu(const float* dem, int8_t* dir, int* flatdist, int W, int H,
+                        float nodata) {
+  const int64_t N = (int64_t)W * H;
+  std::memset(dir, 0, 2 * N);
+  std::memset(flatdist, 0, sizeof(int) * N);
+  std::vector<uint32_t> flats;
+  for (int y = 0; y < H; y++) {
+    for (int x = 0; x < W; x++) {
+      int dxi = 0, dyi = 0;
+      if (x == 0) dxi = -1; else if (x == W - 1) dxi = 1;
+      if (y == 0) dyi = -1; else if (y == H - 1) dyi = 1;
+      const int64_t i = (int64_t)y * W + x;
+      if (dxi != 0 || dyi != 0) {
+        dir[2 * i] = (int8_t)dxi; dir[2 * i + 1] = (int8_t)dyi;
+        flatdist[i] = -1;
+        continue;
+      }
+      if (dem[i] == 0.0f) { flatdist[i] = -2; continue; }
+      if (dem[i] == nodata) { flatdist[i] = -3; continue; }
+      float steepest = 0.0f;
+      int sdx = 0, sdy = 0;
+      for (int n = 0; n < 8; n++) {
+        const int64_t ni = (int64_t)(y + kD8Dy[n]) * W + (x + kD8Dx[n]);
+        if (dem[ni] == nodata) continue;
+        float s = dem[i] - dem[ni];
+        if (s > 0.0f) {
+          if (n % 2 == 1) s = s / kSqrt2;
+          if (s > steepest) { steepest = s; sdx = kD8Dx[n]; sdy = kD8Dy[n]; }
+        }
+      }
+      if (steepest > 0.0f) {
+        dir[2 * i] = (int8_t)sdx; dir[2 * i + 1] = (int8_t)sdy;
+        flatdist[i] = -1;
+      } else {
+        flats.push_back((uint32_t)i);
+      }
+    }
+  }
+  static const int odx[8] = {0, -1, 1, 0, -1, 1, -1, 1};
+  static const int ody[8] = {-1, 0, 0, 1, -1, -1, 1, 1};
+  std::vector<uint32_t> next;
+  std::vector<std::pair<uint32_t, int>> assign;
+  for (int k = 1; !flats.empty(); k++) {
+    next.clear();
+    assign.clear();
+    for (uint32_t c : flats) {
+      const int cx = (int)(c % (uint32_t)W), cy = (int)(c / (uint32_t)W);
+      const float e = dem[c];
+      int got = -1;
+      for (int n = 0; n < 8 && got < 0; n++) {
+        const int nx = cx + odx[n], ny = cy + ody[n];
+        if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+        const int64_t ni = (int64_t)ny * W + nx;
+        const int f = flatdist[ni];
+        if ((f < 0 && dem[ni] != nodata && e >= dem[ni]) || (f >= 1 && f + 1 <= k)) got = n;
+      }
+      if (got >= 0) assign.push_back({c, got});
+      else next.push_back(c);
+    }
+    if (assign.empty()) break;
+    for (auto& a : assign) {
+      flatdist[a.first] = k;
+      dir[2 * a.first] = (int8_t)odx[a.second];
+      dir[2 * a.first + 1] = (int8_t)ody[a.second];
+    }
+    flats.swap(next);
+  }
+}
+
+// Flow tracing with dead ends reported: stream cells (streams >= 0) are
+// LAKE; every other cell follows its direction to the grid edge (OUTSIDE) or
+// a stream cell s (label (int)(-streams[s])); a cell without a direction, and
+// every cell whose path reaches one, is ERROR.  The reference's GPU tracing
+// marks the cell without a direction ERROR
+// (src/flowtracing/FlowTracingAlgorithmGPUCUDA.cu:139-143) and leaves the
+// cells upstream of it at a value that depends on its block layout; ERROR
+// is used for them here.  A label-0 terminal takes cell 0's label, as in
+// the CPU connect pass (src/flowtracing/FlowTracingAlgorithmCPUOpenMP.h:115-134).
+void orc_flow_trace_gpu(const int8_t* dir, const float* streams, int* label, int W, int H) {
+  const int64_t N = (int64_t)W * H;
+  const int kUnset = 1;  // labels are <= 0
+  std::vector<int> lab(N, kUnset);
+  std::vector<int64_t> path;
+  for (int64_t start = 0; start < N; start++) {
+    if (lab[start] != kUnset) continue;
+    path.clear();
+    int64_t idx = start;
+    int l = kUnset;
+    while (true) {
+      if (lab[idx] != kUnset) { l = lab[idx]; break; }
+      if (streams[idx] >= 0.0f) { lab[idx] = kLake; l = kLake; break; }
+      const int dx = dir[2 * idx], dy = dir[2 * idx + 1];
+      if (dx == 0 && dy == 0) { path.push_back(idx); l = kError; break; }
+      path.push_back(idx);
+      const int cx = (int)(idx % W) + dx, cy = (int)(idx / W) + dy;
+      if (cx < 0 || cx >= W || cy < 0 || cy >= H) { l = kOutside; break; }
+      const int64_t ni = (int64_t)cy * W + cx;
+      if (streams[ni] >= 0.0f) { l = (int)(-streams[ni]); break; }
+      if ((int64_t)path.size() > N) { l = kError; break; }
+      idx = ni;
+    }
+    for (int64_t p : path) lab[p] = l;
+  }
+  const int l0 = lab[0];
+  for (int64_t i = 0; i < N; i++) label[i] = lab[i] >= 0 ? (l0 >= 0 ? 0 : l0) : lab[i];
+}
+
+// One realization of the GPU path semantics after the noise: convolution,
+// realistic DEM and burning as in the CPU path (they agree when no NODATA
+// is present), exact fill, GPU routing, tracing with dead ends reported,
+// border accumulation.
+int orc_realization_exact(const float* dem, const float* streams, float* field, int W, int H,
+                          int model, const float* filt, int r, int bevel, float nodata_dem,
+                          float nodata_stream, float* mc, float* filled_out, int8_t* dir_out,
+                          int* label_out) {
+  const int64_t N = (int64_t)W * H;
+  std::vector<float> conv(N);
+  int rc = model == 1 ? orc_convolve_separable(field, conv.data(), W, H, filt, r)
+                      : orc_convolve_2d(field, conv.data(), W, H, filt, r);
+  if (rc) return rc;
+  orc_realistic_dem(dem, conv.data(), N, nodata_dem);
+  rc = orc_stream_burn(conv.data(), streams, W, H, bevel, nodata_dem, nodata_stream);
+  if (rc) return rc;
+  std::vector<float> filled(N);
+  rc = orc_pitfill_exact(conv.data(), filled.data(), W, H, nodata_dem);
+  if (rc) return rc;
+  std::vector<int8_t> dir(2 * N);
+  std::vector<int> fd(N);
+  orc_flow_route_gpu(filled.data(), dir.data(), fd.data(), W, H, nodata_dem);
+  std::vector<int> label(N);
+  orc_flow_trace_gpu(dir.data(), streams, label.data(), W, H);
+  orc_border_accumulate(label.data(), mc, W, H);
+  if (filled_out) std::memcpy(filled_out, filled.data(), sizeof(float) * N);
+  if (dir_out) std::memcpy(dir_out, dir.data(), 2 * N);
+  if (label_out) std::memcpy(label_out, label.data(), sizeof(int) * N);
+  return 0;
 }
 
 // One realization after the noise: convolution (model 1 = Gaussian taps of

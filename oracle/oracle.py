@@ -136,6 +136,51 @@ class Oracle(_Base):
     def threads(self):
         return self.lib.orc_num_threads()
 
+    # ---- the reference's GPU path semantics (exact mode) ----
+    def pitfill_exact(self, rdem, nodata=-9999.0):
+        d = np.ascontiguousarray(rdem, np.float32)
+        H, W = d.shape
+        f = np.empty_like(d)
+        self.lib.orc_pitfill_exact(_p(d, _f32p), _p(f, _f32p), W, H, ctypes.c_float(nodata))
+        return f
+
+    def flow_route_gpu(self, filled, nodata=-9999.0, with_flatdist=False):
+        d = np.ascontiguousarray(filled, np.float32)
+        H, W = d.shape
+        dirs = np.zeros((H, W, 2), np.int8)
+        fd = np.zeros((H, W), np.int32)
+        self.lib.orc_flow_route_gpu(_p(d, _f32p), _p(dirs, _i8p), _p(fd, _i32p), W, H,
+                                    ctypes.c_float(nodata))
+        return (dirs, fd) if with_flatdist else dirs
+
+    def flow_trace_gpu(self, dirs, streams):
+        dd = np.ascontiguousarray(dirs, np.int8)
+        s = np.ascontiguousarray(streams, np.float32)
+        H, W = s.shape
+        lab = np.zeros((H, W), np.int32)
+        self.lib.orc_flow_trace_gpu(_p(dd, _i8p), _p(s, _f32p), _p(lab, _i32p), W, H)
+        return lab
+
+    def realization_exact(self, dem, streams, noise, filt, r, model, mc, bevel=2,
+                          nodata_dem=-9999.0, nodata_stream=-9999.0):
+        """Exact-mode realization (GPU path semantics); returns (mc, filled, dirs, labels)."""
+        d = np.ascontiguousarray(dem, np.float32)
+        s = np.ascontiguousarray(streams, np.float32)
+        f = np.ascontiguousarray(noise, np.float32).copy()
+        H, W = d.shape
+        m = np.ascontiguousarray(mc, np.float32).copy()
+        fl = np.ascontiguousarray(filt, np.float32)
+        filled = np.empty((H, W), np.float32)
+        dirs = np.empty((H, W, 2), np.int8)
+        lab = np.empty((H, W), np.int32)
+        rc = self.lib.orc_realization_exact(_p(d, _f32p), _p(s, _f32p), _p(f, _f32p), W, H, model,
+                                            _p(fl, _f32p), r, bevel, ctypes.c_float(nodata_dem),
+                                            ctypes.c_float(nodata_stream), _p(m, _f32p),
+                                            _p(filled, _f32p), _p(dirs, _i8p), _p(lab, _i32p))
+        if rc:
+            raise ValueError("realization rejected its arguments")
+        return m, filled, dirs, lab
+
 
 class Reference(_Base):
     prefix = "ref_"
