@@ -63,6 +63,7 @@ _SIGS = {
     "cageo_stream_burn": ([_vp, _vp, _i, _i, _i, _f, _f, _vp], _i),
     "cageo_pitfill_workspace_size": ([_i, _i], _sz),
     "cageo_pitfill": ([_vp, _vp, _i, _i, _f, _i, _vp, _sz, _vp], _i),
+    "cageo_pitfill_exact_warm": ([_vp, _vp, _vp, _i, _i, _f, _vp, _sz, _vp, _vp], _i),
     "cageo_pitfill_static_max_bytes": ([], _sz),
     "cageo_pitfill_static": ([_vp, _vp, _i, _i, _f, _i, _vp], _i),
     "cageo_route_workspace_size": ([_i, _i], _sz),
@@ -202,6 +203,27 @@ def pitfill(dem, nodata_dem=-9999.0, workspace=None, mode=FILL_CPU_COMPAT):
     _check(lib().cageo_pitfill(_ptr(dem), _ptr(filled), W, H, nodata_dem, mode, ws, wsb,
                                _stream()))
     return filled
+
+
+FILL_STATS = ("last_pass", "phases", "passes", "passes_b", "us", "us_b", "us_phases", "tiles",
+              "rounds", "tiles_b", "rounds_b", "kcyc_load", "kcyc_sweep", "kcyc_store")
+
+
+def pitfill_exact_warm(dem, warm=None, nodata_dem=-9999.0, workspace=None):
+    """Exact fill relaxed down from `warm` (None: +inf).  Returns (filled,
+    stats dict).  Exact only where warm >= the exact fill; verify otherwise."""
+    import torch
+    _grid(dem, torch.float32, "dem")
+    if warm is not None:
+        _grid(warm, torch.float32, "warm")
+    H, W = dem.shape
+    filled = torch.empty_like(dem)
+    ws, wsb = (None, 0) if workspace is None else (_ptr(workspace), workspace.numel())
+    st = (ctypes.c_int64 * 14)()
+    _check(lib().cageo_pitfill_exact_warm(_ptr(dem), _ptr(warm) if warm is not None else None,
+                                          _ptr(filled), W, H, nodata_dem, ws, wsb,
+                                          ctypes.cast(st, _vp), _stream()))
+    return filled, dict(zip(FILL_STATS, list(st)))
 
 
 def route_d8(filled, with_flatdist=False, mode=ROUTE_CPU_COMPAT, nodata_dem=-9999.0):

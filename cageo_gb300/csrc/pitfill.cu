@@ -729,6 +729,23 @@ cageo_status fill_check_status(const FillWork& w, int64_t* stats) {
 
 using namespace cageo;
 
+extern "C" cageo_status cageo_pitfill_exact_warm(const float* d_dem, const float* d_warm,
+                                                 float* d_filled, int W, int H, float nodata_dem,
+                                                 void* d_workspace, size_t workspace_bytes,
+                                                 int64_t* h_stats, cudaStream_t stream) {
+  CAGEO_CHECK_ARG(d_dem && d_filled && valid_dims(W, H), "pointers and size");
+  CAGEO_CHECK_ARG(W <= 65535 && H <= 65535, "width and height must be <= 65535");
+  CAGEO_CHECK_ARG(d_dem != d_filled && d_warm != d_filled, "the filled grid must not alias");
+  Scratch ws;
+  cageo_status st = ws.acquire(d_workspace, workspace_bytes, fill_workspace_bytes(W, H), stream);
+  if (st) return st;
+  FillWork w = fill_carve(ws.ptr, W, H);
+  if ((st = fill_reset_scalars(w, stream))) return st;
+  if ((st = fill_run_exact(d_dem, d_filled, w, nodata_dem, d_warm, stream))) return st;
+  CAGEO_CUDA(cudaStreamSynchronize(stream));
+  return fill_check_status(w, h_stats);
+}
+
 extern "C" size_t cageo_pitfill_workspace_size(int W, int H) {
   if (!valid_dims(W, H)) return 0;
   return fill_workspace_bytes(W, H);

@@ -140,6 +140,21 @@ cageo_status cageo_pitfill(float* d_dem, float* d_filled, int W, int H,
                            float nodata_dem, int mode, void* d_workspace,
                            size_t workspace_bytes, cudaStream_t stream);
 
+/* Exact fill (CAGEO_FILL_EXACT semantics) relaxed down from per-cell start
+ * values d_warm (NULL: +inf, the plain fill) instead of +inf.  No
+ * counterpart in the reference: it is the building block of the learned
+ * warm start.  The result equals the exact fill whenever every start value
+ * is >= the exact fill's value (a start of +inf always is); a start below
+ * it leaves a lower fixpoint in which some cells do not drain, so callers
+ * must verify the result (every cell drains to an outlet) and rerun cold
+ * where it fails.  h_stats (may be NULL) receives the fill's 14
+ * statistics (passes, tiles, sweep rounds ...). */
+cageo_status cageo_pitfill_exact_warm(const float* d_dem, const float* d_warm,
+                                      float* d_filled, int W, int H,
+                                      float nodata_dem, void* d_workspace,
+                                      size_t workspace_bytes, int64_t* h_stats,
+                                      cudaStream_t stream);
+
 /* Pit filling that allocates no device memory.  No counterpart in the
  * reference: it exists for callers that cannot allocate -- e.g. a host
  * application that has reserved the GPU's memory for its own allocator and
