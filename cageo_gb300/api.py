@@ -329,13 +329,14 @@ class Pipeline:
         _check(lib().cageo_pipeline_reset_counts(self._p))
 
     def stats(self):
-        s = np.zeros(19, np.int64)
-        _check(lib().cageo_pipeline_stats(self._p, s.ctypes.data_as(_vp), 19))
+        s = np.zeros(23, np.int64)
+        _check(lib().cageo_pipeline_stats(self._p, s.ctypes.data_as(_vp), 23))
         keys = ("fill_passes", "fill_phases", "flat_layers", "trace_jumps", "burn_reruns",
                 "flood_a_passes", "flood_b_passes", "flood_a_us", "flood_b_us", "phases_us",
                 "flood_a_tiles", "flood_a_rounds", "flood_b_tiles", "flood_b_rounds",
                 "flat_cells", "flat_bfs_us", "tile_kcycles_load", "tile_kcycles_sweep",
-                "tile_kcycles_store")
+                "tile_kcycles_store", "flat_tiles", "flat_kcycles_load", "flat_kcycles_bfs",
+                "flat_kcycles_store")
         return {k: int(v) for k, v in zip(keys, s)}
 
     STAGES = ("noise", "front", "fill", "route", "trace", "border")

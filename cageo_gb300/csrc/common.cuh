@@ -96,6 +96,16 @@ constexpr int kBarCountSlot = 32;
 constexpr int kBarGenSlot = 64;
 constexpr int kScalarSlots = 96;
 
+// Asynchronous 4-byte global -> shared copy (LDGSTS): many can be in flight
+// per thread without holding registers.  Complete them with cp_async_wait().
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned int sa = (unsigned int)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 __device__ inline bool grid_barrier(const GridSync& g, unsigned int nblocks) {
   __syncthreads();
   __shared__ int ok;

@@ -108,7 +108,7 @@ struct cageo_pipeline {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool graph_ok = false;
-  int64_t stats[19] = {};
+  int64_t stats[23] = {};
 };
 
 namespace {
@@ -333,7 +333,7 @@ extern "C" cageo_status cageo_pipeline_run(cageo_pipeline* p, uint32_t first, in
     }
   }
   CAGEO_CUDA(cudaStreamSynchronize(s));
-  int64_t fs[14] = {}, rs[3] = {}, jumps = 0;
+  int64_t fs[14] = {}, rs[7] = {}, jumps = 0;
   if ((st = fill_check_status(p->fw, fs))) return st;
   if ((st = route_check_status(p->rw, rs))) return st;
   if ((st = trace_check_status(p->tw, &jumps))) return st;
@@ -361,6 +361,7 @@ extern "C" cageo_status cageo_pipeline_run(cageo_pipeline* p, uint32_t first, in
   p->stats[14] = rs[1];
   p->stats[15] = rs[2];
   for (int k = 0; k < 3; k++) p->stats[16 + k] = fs[11 + k];
+  for (int k = 0; k < 4; k++) p->stats[19 + k] = rs[3 + k];
   return CAGEO_OK;
 }
 
@@ -408,7 +409,7 @@ extern "C" cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t reali
       break;
     }
     for (int i = 0; i < 6 && i < n; i++) cudaEventElapsedTime(&h_ms[i], ev[i], ev[i + 1]);
-    int64_t fs[14], rs[3];
+    int64_t fs[14], rs[7];
     if ((st = fill_check_status(p->fw, fs))) break;
     p->stats[0] = fs[0];
     p->stats[1] = fs[1];
@@ -418,6 +419,7 @@ extern "C" cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t reali
     p->stats[14] = rs[1];
     p->stats[15] = rs[2];
     for (int k = 0; k < 3; k++) p->stats[16 + k] = fs[11 + k];
+    for (int k = 0; k < 4; k++) p->stats[19 + k] = rs[3 + k];
     st = trace_check_status(p->tw, &p->stats[3]);
   } while (0);
   for (auto& e : ev) cudaEventDestroy(e);
@@ -574,7 +576,7 @@ extern "C" cudaStream_t cageo_pipeline_stream(cageo_pipeline* p) { return p ? p-
 
 extern "C" cageo_status cageo_pipeline_stats(cageo_pipeline* p, int64_t* h_stats, int n) {
   CAGEO_CHECK_ARG(p && h_stats, "null argument");
-  for (int i = 0; i < n && i < 19; i++) h_stats[i] = p->stats[i];
+  for (int i = 0; i < n && i < 23; i++) h_stats[i] = p->stats[i];
   return CAGEO_OK;
 }
 

@@ -12,10 +12,11 @@
 // whose elevation is <= theirs, taking the direction of the LAST such
 // neighbour in N..NW order.  Layer numbers are breadth-first distances, so
 // they are computed here as shortest-path distances by tile relaxation (a
-// persistent cooperative kernel: one warp sweeps a 32x32 tile of the tiles
-// that hold flat cells until stable, and queues the neighbouring tiles when
-// its border changed), and the directions by one final pass that applies
-// the last-match rule to the finished distances.
+// persistent cooperative kernel: one warp runs a bit-parallel breadth-first
+// search over a 32x32 tile of the tiles that hold flat cells, seeded from
+// its halo, and queues the neighbouring tiles when its border changed), and
+// the directions by one final pass that applies the last-match rule to the
+// finished distances.
 //
 // The GPU-order mode follows the reference's GPU routing instead
 // (src/flowrouting/FlowRoutingAlgorithmGPUCUDAOriginal.cu:200-271 and
@@ -34,13 +35,13 @@ namespace cageo {
 constexpr int kFlatInf = 0x3fffffff;
 constexpr int kOffGrid = (int)0x80000000;  // staged code of a cell outside the grid
 enum : int { R_NFLAT = 0, R_ERR = 3, R_LIST = 4, R_LAYERS = 7, R_US_BFS = 8, R_PASSES = 9,
+             R_TILES = 10, R_KCYC_LOAD = 11, R_KCYC_BFS = 12, R_KCYC_STORE = 13,
              R_BAR_COUNT = kBarCountSlot, R_BAR_GEN = kBarGenSlot, R_SIZE = kScalarSlots };
 constexpr int kFT = 32;          // flat tile size
 constexpr int kFWarps = 16;      // warps per block of the flat kernel
 constexpr int kFRS = 35;         // staged row stride
 
 size_t route_workspace_bytes(int W, int H) {
-  const size_t n = (size_t)W * H;
   const size_t nt = (size_t)((W + kFT - 1) / kFT) * ((H + kFT - 1) / kFT);
   return align_up(nt, 256) + align_up(nt * 4, 256) + align_up(2 * nt * 4, 256) + 512;
 }
@@ -150,7 +151,6 @@ __device__ __forceinline__ int flat_relay(int code, float e, bool gpu, float nod
 struct FlatSmem {
   int R[34 * kFRS];      // staged relay values (tile + halo)
   float E[34 * kFRS];    // staged elevations
-  uint8_t isflat[kFT * 36];
 };
 
 __device__ __forceinline__ void flat_enqueue(const RouteWork& w, int t, int k) {
@@ -163,92 +163,157 @@ __device__ __forceinline__ void flat_enqueue(const RouteWork& w, int t, int k) {
   }
 }
 
-// Relax flat cell (x, y): one more than the least distance among neighbours
-// whose elevation is <= its own.
-__device__ __forceinline__ bool flat_update(FlatSmem& s, int x, int y) {
-  if (!s.isflat[y * 36 + x]) return false;
-  const int b = (y + 1) * kFRS + (x + 1);
-  const float e = s.E[b];
-  int m = kFlatInf;
-#pragma unroll
-  for (int n = 0; n < 8; n++) {
-    const int o = d8_dy(n) * kFRS + d8_dx(n);
-    const int v = s.R[b + o];
-    if (s.E[b + o] <= e && v < m) m = v;
-  }
-  if (m < kFlatInf && m + 1 < s.R[b]) {
-    s.R[b] = m + 1;
-    s.isflat[y * 36 + x] = 3;  // flat and changed
-    return true;
-  }
-  return false;
-}
-
 __device__ void flat_tile(FlatSmem& s, const float* __restrict__ dem, int* fd, const RouteWork& w,
                           int t, int p, int lane, bool gpu, float nodata) {
   const int W = w.W, H = w.H;
   const int tx = t % w.tiles_x, ty = t / w.tiles_x;
   const int x0 = tx * kFT, y0 = ty * kFT;
-#pragma unroll 4
+  const long long c0 = clock64();
+  // Stage the raw codes and elevations with asynchronous copies (all of the
+  // tile's loads in flight at once), then turn codes into relay values.
   for (int idx = lane; idx < 34 * 34; idx += 32) {
     const int hy = idx / 34, hx = idx - hy * 34;
     const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
-    int code = kOffGrid;
-    float e = 0.0f;
+    int* dr = &s.R[hy * kFRS + hx];
+    float* de = &s.E[hy * kFRS + hx];
     if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
       const int64_t i = (int64_t)gy * W + gx;
-      code = ((volatile int*)fd)[i];
-      e = dem[i];
+      cp_async4(dr, fd + i);
+      cp_async4(de, dem + i);
+    } else {
+      *dr = kOffGrid;
+      *de = 0.0f;
     }
-    s.R[hy * kFRS + hx] = flat_relay(code, e, gpu, nodata);
-    s.E[hy * kFRS + hx] = e;
-    if (hx >= 1 && hx <= kFT && hy >= 1 && hy <= kFT)
-      s.isflat[(hy - 1) * 36 + hx - 1] = (code == kFlatInf || code >= 1) ? 1 : 0;
+  }
+  cp_async_wait();
+  __syncwarp();
+  // Lane y: the flat cells of row y (codes are still raw here).
+  const int y = lane;
+  unsigned int flat = 0;
+#pragma unroll
+  for (int x = 0; x < kFT; x++) {
+    const int code = s.R[(y + 1) * kFRS + (x + 1)];
+    if (code == kFlatInf || code >= 1) flat |= 1u << x;
   }
   __syncwarp();
-  auto smear = [](unsigned int m) { return m | (m << 1) | (m >> 1); };
-  bool capped = true;
-  unsigned int next_rows = 0xffffffffu;
-  for (int round = 0; round < 64; round++) {
-    unsigned int pend = next_rows, cch = 0;
-    for (int k = 0; k < kFT; k++) {
-      const int d = k, u = kFT - 1 - k;
-      unsigned int b1 = 0, b2 = 0;
-      if ((pend >> d) & 1u) b1 = __ballot_sync(0xffffffffu, flat_update(s, lane, d));
-      if ((pend >> u) & 1u) b2 = __ballot_sync(0xffffffffu, flat_update(s, lane, u));
-      if (b1) { cch |= b1; pend |= smear(1u << d); }
-      if (b2) { cch |= b2; pend |= smear(1u << u); }
-      __syncwarp();
-    }
-    unsigned int pendc = smear(cch), rch2 = 0;
-    for (int k = 0; k < kFT; k++) {
-      const int l = k, r = kFT - 1 - k;
-      unsigned int b1 = 0, b2 = 0;
-      if ((pendc >> l) & 1u) b1 = __ballot_sync(0xffffffffu, flat_update(s, l, lane));
-      if ((pendc >> r) & 1u) b2 = __ballot_sync(0xffffffffu, flat_update(s, r, lane));
-      if (b1) { rch2 |= b1; pendc |= smear(1u << l); }
-      if (b2) { rch2 |= b2; pendc |= smear(1u << r); }
-      __syncwarp();
-    }
-    if (!rch2) { capped = false; break; }
-    next_rows = smear(rch2);
+  for (int idx = lane; idx < 34 * 34; idx += 32) {
+    const int hy = idx / 34, hx = idx - hy * 34;
+    const int code = s.R[hy * kFRS + hx];
+    s.R[hy * kFRS + hx] = flat_relay(code, s.E[hy * kFRS + hx], gpu, nodata);
   }
-  unsigned int sides = 0;
-  for (int idx = lane; idx < kFT * kFT; idx += 32) {
-    const int y = idx >> 5, x = idx & 31;
-    if (s.isflat[y * 36 + x] == 3) {
-      fd[(int64_t)(y0 + y) * W + (x0 + x)] = s.R[(y + 1) * kFRS + (x + 1)];
-      if (x == 0) sides |= 1;
-      if (x == kFT - 1) sides |= 2;
-      if (y == 0) sides |= 4;
-      if (y == kFT - 1) sides |= 8;
-      if (x == 0 && y == 0) sides |= 16;
-      if (x == kFT - 1 && y == 0) sides |= 32;
-      if (x == 0 && y == kFT - 1) sides |= 64;
-      if (x == kFT - 1 && y == kFT - 1) sides |= 128;
+  __syncwarp();
+  const long long c1 = clock64();
+  // Distances inside the tile by a bit-parallel breadth-first search: lane y
+  // holds row y as a bit mask.  A flat cell is a seed at level 1 + the least
+  // relay among its neighbours that are not flat cells of this tile (halo
+  // cells, or exits inside the tile) and whose elevation is <= its own;
+  // flat cells pass levels on to their flat neighbours (which have the same
+  // elevation, so the elevation test always holds between them).  Levels are
+  // visited in increasing order, so the first level that reaches a cell is
+  // its distance; old values inside the tile came from halo values that can
+  // only have dropped since, so they are never below the new ones.
+  //
+  // Only cells on the tile's rim or next to a non-flat cell of the tile can
+  // be seeds.  Inside the rim a seed's non-flat neighbours are all inside
+  // the tile, where the least relay is 0 (an exit), so inner seeds are all
+  // at level 1.  Rim seeds are held one per lane: the top and bottom rows by
+  // column (lane = x), the left and right columns by row (lane = y, rows
+  // 1..30); each level's seed masks then come from two ballots.
+  unsigned int fup = __shfl_up_sync(0xffffffffu, flat, 1);
+  unsigned int fdn = __shfl_down_sync(0xffffffffu, flat, 1);
+  if (lane == 0) fup = 0;
+  if (lane == kFT - 1) fdn = 0;
+  const unsigned int allflat = flat & fup & fdn & (flat << 1) & (flat >> 1) & (fup << 1) &
+                               (fup >> 1) & (fdn << 1) & (fdn >> 1);
+  // Seed level of cell (cx, cy) (kFlatInf: none); fr = the flat masks of
+  // rows cy-1, cy, cy+1 (bit set = flat cell of this tile).
+  auto seed_of = [&](int cx, int cy, unsigned int fu, unsigned int fm, unsigned int fb) {
+    const int b = (cy + 1) * kFRS + (cx + 1);
+    const float e = s.E[b];
+    int best = kFlatInf;
+#pragma unroll
+    for (int n = 0; n < 8; n++) {
+      const int nx = cx + d8_dx(n), ny = cy + d8_dy(n);
+      const unsigned int row = d8_dy(n) < 0 ? fu : (d8_dy(n) > 0 ? fb : fm);
+      const bool inner = nx >= 0 && nx < kFT && ny >= 0 && ny < kFT && ((row >> nx) & 1u);
+      const int o = b + d8_dy(n) * kFRS + d8_dx(n);
+      const int v = s.R[o];
+      if (!inner && v < best && s.E[o] <= e) best = v;
+    }
+    return best < kFlatInf ? best + 1 : kFlatInf;
+  };
+  const unsigned int f0 = __shfl_sync(0xffffffffu, flat, 0);
+  const unsigned int f1 = __shfl_sync(0xffffffffu, flat, 1);
+  const unsigned int f30 = __shfl_sync(0xffffffffu, flat, kFT - 2);
+  const unsigned int f31 = __shfl_sync(0xffffffffu, flat, kFT - 1);
+  // Top row (0, x = lane) and bottom row (31, x = lane).
+  const int tseed = ((f0 >> lane) & 1u) ? seed_of(lane, 0, 0u, f0, f1) : kFlatInf;
+  const int bseed = ((f31 >> lane) & 1u) ? seed_of(lane, kFT - 1, f30, f31, 0u) : kFlatInf;
+  // Left (y, 0) and right (y, 31) columns, rows 1..30 (y = lane).
+  const bool mid = lane >= 1 && lane <= kFT - 2;
+  const int lseed = (mid && (flat & 1u)) ? seed_of(0, y, fup, flat, fdn) : kFlatInf;
+  const int rseed = (mid && (flat >> 31)) ? seed_of(kFT - 1, y, fup, flat, fdn) : kFlatInf;
+  // Inner candidates next to a non-flat cell of the tile: level 1 or none.
+  unsigned int inner1 = 0;
+  if (mid) {
+    for (unsigned int m = flat & ~allflat & 0x7ffffffeu; m; m &= m - 1) {
+      const int x = __ffs(m) - 1;
+      if (seed_of(x, y, fup, flat, fdn) == 1) inner1 |= 1u << x;
     }
   }
-  sides = __reduce_or_sync(0xffffffffu, sides);
+  auto next_level = [&](int after) {  // least seed level above `after`
+    int m = kFlatInf;
+    if (tseed > after) m = min(m, tseed);
+    if (bseed > after) m = min(m, bseed);
+    if (lseed > after) m = min(m, lseed);
+    if (rseed > after) m = min(m, rseed);
+    if (inner1 && after < 1) m = min(m, 1);
+    return __reduce_min_sync(0xffffffffu, m);
+  };
+  int L = next_level(0);
+  unsigned int visited = 0, front = 0, changed = 0;
+  for (int guard = 0; guard < 4 * kFT * kFT && L < kFlatInf; guard++) {
+    const unsigned int tb = __ballot_sync(0xffffffffu, tseed == L);
+    const unsigned int bb = __ballot_sync(0xffffffffu, bseed == L);
+    unsigned int seeds = (L == 1 ? inner1 : 0u) | (lseed == L ? 1u : 0u) |
+                         (rseed == L ? 0x80000000u : 0u);
+    if (lane == 0) seeds |= tb;
+    if (lane == kFT - 1) seeds |= bb;
+    unsigned int up = __shfl_up_sync(0xffffffffu, front, 1);
+    unsigned int dn = __shfl_down_sync(0xffffffffu, front, 1);
+    if (lane == 0) up = 0;
+    if (lane == kFT - 1) dn = 0;
+    const unsigned int v = front | up | dn;
+    const unsigned int reach = ((v | (v << 1) | (v >> 1)) | seeds) & flat & ~visited;
+    visited |= reach;
+    front = reach;
+    for (unsigned int r = reach; r; r &= r - 1) {
+      const int x = __ffs(r) - 1;
+      int* cell = &s.R[(y + 1) * kFRS + (x + 1)];
+      if (L < *cell) {
+        *cell = L;
+        changed |= 1u << x;
+      }
+    }
+    // Next level, or jump to the next seed level when the front died out.
+    L = __any_sync(0xffffffffu, front != 0) ? L + 1 : next_level(L);
+  }
+  __syncwarp();
+  const long long c2 = clock64();
+  const bool capped = false;
+  // Write back the changed distances (lane = column now); note the sides.
+  for (int yy = 0; yy < kFT; yy++) {
+    const unsigned int row = __shfl_sync(0xffffffffu, changed, yy);
+    if ((row >> lane) & 1u)
+      fd[(int64_t)(y0 + yy) * W + (x0 + lane)] = s.R[(yy + 1) * kFRS + (lane + 1)];
+  }
+  const unsigned int top = __shfl_sync(0xffffffffu, changed, 0);
+  const unsigned int bot = __shfl_sync(0xffffffffu, changed, kFT - 1);
+  const unsigned int lcol = __ballot_sync(0xffffffffu, changed & 1u);
+  const unsigned int rcol = __ballot_sync(0xffffffffu, changed >> 31);
+  unsigned int sides = (lcol ? 1u : 0u) | (rcol ? 2u : 0u) | (top ? 4u : 0u) | (bot ? 8u : 0u) |
+                       ((top & 1u) ? 16u : 0u) | ((top >> 31) ? 32u : 0u) |
+                       ((bot & 1u) ? 64u : 0u) | ((bot >> 31) ? 128u : 0u);
   if (lane < 9) {
     int dx = 0, dy = 0;
     bool want = false;
@@ -268,6 +333,13 @@ __device__ void flat_tile(FlatSmem& s, const float* __restrict__ dem, int* fd, c
       flat_enqueue(w, ny * w.tiles_x + nx, p + 1);
   }
   __syncwarp();
+  if (lane == 0) {
+    const long long c3 = clock64();
+    atomicAdd(&w.scal[R_TILES], 1u);
+    atomicAdd(&w.scal[R_KCYC_LOAD], (unsigned int)((c1 - c0) >> 10));
+    atomicAdd(&w.scal[R_KCYC_BFS], (unsigned int)((c2 - c1) >> 10));
+    atomicAdd(&w.scal[R_KCYC_STORE], (unsigned int)((c3 - c2) >> 10));
+  }
 }
 
 __global__ void __launch_bounds__(kFWarps * 32, 1)
@@ -422,6 +494,10 @@ cageo_status route_check_status(const RouteWork& w, int64_t* stats) {
     stats[0] = h[R_PASSES];
     stats[1] = h[R_NFLAT];
     stats[2] = h[R_US_BFS];
+    stats[3] = h[R_TILES];
+    stats[4] = h[R_KCYC_LOAD];
+    stats[5] = h[R_KCYC_BFS];
+    stats[6] = h[R_KCYC_STORE];
   }
   if (h[R_ERR]) {
     set_error("flow routing: flat-surface relaxation hit a wait or pass limit");

@@ -21,8 +21,9 @@ RouteWork route_carve(void* base, int W, int H);
 // the latter only).
 cageo_status route_run(const float* filled, int8_t* dir, int* flatdist,
                        const RouteWork& w, cudaStream_t s, int mode, float nodata);
-// stats (3 entries, may be null): flat relaxation passes, flat cells,
-// microseconds of the flat relaxation.
+// stats (7 entries, may be null): flat relaxation passes, flat cells,
+// microseconds of the flat relaxation, flat tile visits, and kilo-cycles
+// summed over visits spent staging, searching, storing.
 cageo_status route_check_status(const RouteWork& w, int64_t* stats);
 
 struct TraceWork {

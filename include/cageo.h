@@ -288,7 +288,9 @@ cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t realization,
  * to convergence and of the phase loop, [10..13] tiles and sweep rounds of
  * the two floods, [14] flat cells, [15] microseconds of the flat BFS,
  * [16..18] kilo-cycles summed over the fill's tile visits spent staging,
- * sweeping and storing (last realization). */
+ * sweeping and storing, [19] tile visits of the flat BFS, [20..22]
+ * kilo-cycles summed over them spent staging, searching and storing
+ * (last realization). */
 cageo_status cageo_pipeline_stats(cageo_pipeline* p, int64_t* h_stats, int n);
 void cageo_pipeline_destroy(cageo_pipeline* p);
 
