@@ -607,7 +607,13 @@ __global__ void quantize_min_kernel(float* __restrict__ d, int64_t n, float noda
   }
   unsigned int o = float_to_ordered(m);
   o = __reduce_min_sync(0xffffffffu, o);
-  if ((threadIdx.x & 31) == 0) atomicMin(minslot, o);
+  // One atomic per block (same-address atomics from every warp queue up).
+  __shared__ unsigned int bmin;
+  if (threadIdx.x == 0) bmin = 0xffffffffu;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) atomicMin(&bmin, o);
+  __syncthreads();
+  if (threadIdx.x == 0) atomicMin(minslot, bmin);
 }
 
 __global__ void fill_scalars_kernel(unsigned int* s) {

@@ -80,61 +80,75 @@ __device__ __forceinline__ void gather8(const float* __restrict__ dem, const int
 }
 
 // Steepest-descent pass.  flatdist: -1 direction, -2 stream, -3 NODATA
-// (GPU order only), kFlatInf flat.
+// (GPU order only), kFlatInf flat.  A 32x8 block covers one 32x32 flat
+// tile (4 rows per thread), so the tile's "holds a flat cell" flag and the
+// flat-cell count take one store and one atomic per block.
 template <bool GPU>
-__global__ void d8_kernel(const float* __restrict__ dem, char2* __restrict__ dir,
-                          int* __restrict__ fd, RouteWork w, float nodata) {
+__global__ void __launch_bounds__(256) d8_kernel(const float* __restrict__ dem,
+                                                 char2* __restrict__ dir,
+                                                 int* __restrict__ fd, RouteWork w, float nodata) {
   const int W = w.W, H = w.H;
-  int x = blockIdx.x * blockDim.x + threadIdx.x;
-  int y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= W || y >= H) return;
-  int64_t i = (int64_t)y * W + x;
-  int dxi = 0, dyi = 0;
-  if (x == 0) dxi = -1; else if (x == W - 1) dxi = 1;
-  if (y == 0) dyi = -1; else if (y == H - 1) dyi = 1;
-  bool flat = false;
-  if (dxi || dyi) {
-    dir[i] = make_char2((signed char)dxi, (signed char)dyi);
-    fd[i] = -1;
-  } else {
+  const int x = blockIdx.x * kFT + threadIdx.x;
+  int nflat = 0;
+#pragma unroll
+  for (int k = 0; k < kFT / 8; k++) {
+    const int y = blockIdx.y * kFT + threadIdx.y + 8 * k;
+    if (x >= W || y >= H) continue;
+    const int64_t i = (int64_t)y * W + x;
+    int dxi = 0, dyi = 0;
+    if (x == 0) dxi = -1; else if (x == W - 1) dxi = 1;
+    if (y == 0) dyi = -1; else if (y == H - 1) dyi = 1;
+    if (dxi || dyi) {
+      dir[i] = make_char2((signed char)dxi, (signed char)dyi);
+      fd[i] = -1;
+      continue;
+    }
     const float c = dem[i];
     if (c == 0.0f) {
       dir[i] = make_char2(0, 0);
       fd[i] = -2;
-    } else if (GPU && c == nodata) {
+      continue;
+    }
+    if (GPU && c == nodata) {
       dir[i] = make_char2(0, 0);
       fd[i] = -3;
-    } else {
-      float steepest = 0.0f;
-      int sdx = 0, sdy = 0;
+      continue;
+    }
+    float steepest = 0.0f;
+    int sdx = 0, sdy = 0;
 #pragma unroll
-      for (int n = 0; n < 8; n++) {
-        const int dx = d8_dx(n), dy = d8_dy(n);
-        const float e = dem[(int64_t)(y + dy) * W + (x + dx)];
-        if (GPU && e == nodata) continue;
-        float s = __fsub_rn(c, e);
-        // A diagonal drop only shrinks when divided by sqrt(2), so the
-        // (slow, correctly rounded) division is needed only when the
-        // undivided drop already beats the steepest so far.
-        if (s > 0.0f && s > steepest) {
-          if (n & 1) s = __fdiv_rn(s, 1.41421356237309505f);
-          if (s > steepest) { steepest = s; sdx = dx; sdy = dy; }
-        }
-      }
-      if (steepest > 0.0f) {
-        dir[i] = make_char2((signed char)sdx, (signed char)sdy);
-        fd[i] = -1;
-      } else {
-        dir[i] = make_char2(0, 0);
-        fd[i] = kFlatInf;
-        flat = true;
+    for (int n = 0; n < 8; n++) {
+      const int dx = d8_dx(n), dy = d8_dy(n);
+      const float e = dem[(int64_t)(y + dy) * W + (x + dx)];
+      if (GPU && e == nodata) continue;
+      float sl = __fsub_rn(c, e);
+      // A diagonal drop only shrinks when divided by sqrt(2), so the
+      // (slow, correctly rounded) division is needed only when the
+      // undivided drop already beats the steepest so far.
+      if (sl > 0.0f && sl > steepest) {
+        if (n & 1) sl = __fdiv_rn(sl, 1.41421356237309505f);
+        if (sl > steepest) { steepest = sl; sdx = dx; sdy = dy; }
       }
     }
+    if (steepest > 0.0f) {
+      dir[i] = make_char2((signed char)sdx, (signed char)sdy);
+      fd[i] = -1;
+    } else {
+      dir[i] = make_char2(0, 0);
+      fd[i] = kFlatInf;
+      nflat++;
+    }
   }
-  if (flat) w.tflat[(y / kFT) * w.tiles_x + x / kFT] = 1;
-  const unsigned int nflat = __popc(__ballot_sync(__activemask(), flat));
-  if (nflat && (threadIdx.x & 31) == __ffs(__ballot_sync(__activemask(), flat)) - 1)
-    atomicAdd(&w.scal[R_NFLAT], nflat);  // statistics only
+  __shared__ int block_flat;
+  if (threadIdx.x == 0 && threadIdx.y == 0) block_flat = 0;
+  __syncthreads();
+  nflat = __reduce_add_sync(0xffffffffu, nflat);
+  if (threadIdx.x == 0 && nflat) atomicAdd(&block_flat, nflat);
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0 && block_flat) {
+    w.tflat[blockIdx.y * w.tiles_x + blockIdx.x] = 1;
+    atomicAdd(&w.scal[R_NFLAT], (unsigned int)block_flat);  // statistics only
+  }
 }
 
 // ---- flat distances by tile relaxation ----------------------------------
@@ -453,7 +467,7 @@ cageo_status route_run(const float* filled, int8_t* dir, int* fd, const RouteWor
   route_scalars_kernel<<<1, 128, 0, s>>>(w.scal);
   CAGEO_CUDA(cudaMemsetAsync(w.tflat, 0, nt, s));
   CAGEO_CUDA(cudaMemsetAsync(w.queued, 0, nt * 4, s));
-  dim3 b(32, 8), g((w.W + 31) / 32, (w.H + 7) / 8);
+  dim3 b(32, 8), g(w.tiles_x, w.tiles_y);
   if (gpu) d8_kernel<true><<<g, b, 0, s>>>(filled, (char2*)dir, fd, w, nodata);
   else d8_kernel<false><<<g, b, 0, s>>>(filled, (char2*)dir, fd, w, nodata);
   CAGEO_CUDA(cudaGetLastError());

@@ -105,8 +105,9 @@ __global__ void __launch_bounds__(kJumpThreads, 8) trace_jump_kernel(int* st, Tr
         }
       }
     }
-    if (__any_sync(0xffffffffu, active) && (threadIdx.x & 31) == 0)
-      atomicOr(&w.scal[T_ACTIVE + pass % 3], 1u);
+    // One flag update per block: same-address atomics from every warp would
+    // queue up at the memory system.
+    if (__syncthreads_or(active) && threadIdx.x == 0) atomicOr(&w.scal[T_ACTIVE + pass % 3], 1u);
     if (!grid_barrier(gs, gridDim.x)) break;
     if (vs[T_ACTIVE + pass % 3] == 0u) break;
     if (++pass > 64) {  // 2^64 exceeds any path length: a cycle
