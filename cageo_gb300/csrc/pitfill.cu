@@ -194,7 +194,7 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
   const int tx = t % w.tiles_x, ty = t / w.tiles_x;
   const int x0 = tx * kTile, y0 = ty * kTile;
   const long long c0 = clock64();
-#pragma unroll 4
+#pragma unroll 12
   for (int idx = lane; idx < 34 * 34; idx += 32) {
     int hy = idx / 34, hx = idx - hy * 34;
     int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
