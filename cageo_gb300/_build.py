@@ -23,7 +23,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["common.cu", "noise_conv.cu", "surface.cu", "pitfill.cu", "routing.cu",
-              "trace_border.cu", "pipeline.cu", "pitfill_static.cu"]
+              "trace_border.cu", "pipeline.cu", "pitfill_static.cu", "learned.cu"]
 HOST_SOURCES = ["filter.cpp", "raster_io.cpp", "jpeg.cpp"]
 
 LIB = os.path.join(OUT, "libcageo.so")

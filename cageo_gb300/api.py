@@ -73,6 +73,13 @@ _SIGS = {
     "cageo_trace": ([_vp, _vp, _vp, _i, _i, _vp, _sz, _vp], _i),
     "cageo_trace_mode": ([_vp, _vp, _vp, _i, _i, _i, _vp, _sz, _vp], _i),
     "cageo_border_accumulate": ([_vp, _vp, _i, _i, _vp], _i),
+    "cageo_ws_param_count": ([], _i),
+    "cageo_ws_features": ([_vp, _vp, _i, _i, _i, _f, _vp], _i),
+    "cageo_ws_forward": ([_vp, _vp, _i, _i, _i, _vp, _vp, _vp, _vp], _i),
+    "cageo_ws_backward": ([_vp] * 5 + [_i, _i, _i] + [_vp] * 5, _i),
+    "cageo_ws_mse": ([_vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp], _i),
+    "cageo_ws_adam": ([_vp, _vp, _vp, _vp, _i, _f, _f, _f, _f, _i, _vp], _i),
+    "cageo_ws_infer": ([_vp, _vp, _vp, _vp, _i, _i, _f, _f, _vp], _i),
     "cageo_pipeline_create": ([ctypes.POINTER(_vp), ctypes.POINTER(PipelineConfig), _vp, _vp], _i),
     "cageo_pipeline_create_device": ([ctypes.POINTER(_vp), ctypes.POINTER(PipelineConfig), _vp,
                                       _vp], _i),
@@ -255,6 +262,66 @@ def border_accumulate(labels, counts):
     H, W = labels.shape
     _check(lib().cageo_border_accumulate(_ptr(labels), _ptr(counts), W, H, _stream()))
     return counts
+
+
+# ---- learned warm start (no counterpart in the reference) -------------------------
+def ws_features(v, nodata_dem=-9999.0):
+    """v: (B, H, W) or (H, W) float32 CUDA -> features (B, 4, H, W)."""
+    import torch
+    _grid(v, torch.float32, "v")
+    vb = v if v.dim() == 3 else v[None]
+    B, H, W = vb.shape
+    f = torch.empty((B, 4, H, W), dtype=torch.float32, device=v.device)
+    _check(lib().cageo_ws_features(_ptr(vb), _ptr(f), W, H, B, nodata_dem, _stream()))
+    return f
+
+
+def ws_forward(params, feat):
+    """Training forward pass: returns (a1, a2, out) with out (B, H, W)."""
+    import torch
+    B, _, H, W = feat.shape
+    a1 = torch.empty((B, 32, H, W), dtype=torch.float32, device=feat.device)
+    a2 = torch.empty_like(a1)
+    out = torch.empty((B, H, W), dtype=torch.float32, device=feat.device)
+    _check(lib().cageo_ws_forward(_ptr(params), _ptr(feat), W, H, B, _ptr(a1), _ptr(a2),
+                                  _ptr(out), _stream()))
+    return a1, a2, out
+
+
+def ws_backward(params, feat, a1, a2, dout, grad, tmp1=None, tmp2=None, wflip=None):
+    """Adds dL/dparams (given dL/dout) into `grad`."""
+    import torch
+    B, _, H, W = feat.shape
+    tmp1 = torch.empty_like(a1) if tmp1 is None else tmp1
+    tmp2 = torch.empty_like(a1) if tmp2 is None else tmp2
+    wflip = torch.empty(9216, dtype=torch.float32, device=feat.device) if wflip is None else wflip
+    _check(lib().cageo_ws_backward(_ptr(params), _ptr(feat), _ptr(a1), _ptr(a2), _ptr(dout), W, H,
+                                   B, _ptr(grad), _ptr(tmp1), _ptr(tmp2), _ptr(wflip), _stream()))
+    return grad
+
+
+def ws_mse(y, target, dy, loss, margin=3):
+    B, H, W = y.shape
+    _check(lib().cageo_ws_mse(_ptr(y), _ptr(target), _ptr(dy), _ptr(loss), W, H, B, margin,
+                              _stream()))
+
+
+def ws_adam(params, grad, m, v, lr, step, beta1=0.9, beta2=0.999, eps=1e-8):
+    _check(lib().cageo_ws_adam(_ptr(params), _ptr(grad), _ptr(m), _ptr(v), params.numel(), lr,
+                               beta1, beta2, eps, step, _stream()))
+
+
+def ws_infer(params, v, threshold=0.0, nodata_dem=-9999.0, want_warm=True, want_depth=False):
+    """Fused inference on one grid: returns (warm or None, depth or None)."""
+    import torch
+    _grid(v, torch.float32, "v")
+    H, W = v.shape
+    warm = torch.empty_like(v) if want_warm else None
+    depth = torch.empty_like(v) if want_depth else None
+    _check(lib().cageo_ws_infer(_ptr(params), _ptr(v), _ptr(warm) if warm is not None else None,
+                                _ptr(depth) if depth is not None else None, W, H, nodata_dem,
+                                threshold, _stream()))
+    return warm, depth
 
 
 # ---- pipeline -------------------------------------------------------------------

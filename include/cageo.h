@@ -216,6 +216,50 @@ cageo_status cageo_trace_mode(const int8_t* d_dir, const float* d_streams,
 cageo_status cageo_border_accumulate(const int* d_label, float* d_count, int W,
                                      int H, cudaStream_t stream);
 
+/* ---- Learned warm start of the exact fill ------------------------------------
+ * No counterpart in the reference.  A convolutional network (features of 4
+ * channels -> 3x3 conv, 32 channels, ReLU -> 3x3 conv, 32 channels, ReLU ->
+ * 3x3 conv, 1 channel) predicts the depth the exact fill gives each cell;
+ * cells predicted dry start cageo_pitfill_exact_warm at their elevation.
+ * Weights are rounded to bf16 where they are used, sums accumulate in fp32.
+ * Parameters: cageo_ws_param_count() floats, laid out W1[32][4][9], b1[32],
+ * W2[32][32][9], b2[32], W3[1][32][9], b3[1] (tap t = (dy+1)*3 + dx+1).
+ * Grids of a batch are stored one after another, channels planar:
+ * [batch][channel][H][W]. */
+int cageo_ws_param_count(void);
+/* Features of B grids d_v [B][H][W] into d_feat [B][4][H][W]: v minus the
+ * 3x3 minimum, v minus the 7x7 minimum, the 7x7 maximum minus v, v minus the
+ * 7x7 mean (over in-grid, non-NODATA cells; NODATA cells get zeros). */
+cageo_status cageo_ws_features(const float* d_v, float* d_feat, int W, int H, int B,
+                               float nodata_dem, cudaStream_t stream);
+/* Training forward pass (fp32 activations): d_a1, d_a2 [B][32][H][W] keep
+ * the hidden layers for the backward pass, d_out [B][H][W]. */
+cageo_status cageo_ws_forward(const float* d_params, const float* d_feat, int W, int H,
+                              int B, float* d_a1, float* d_a2, float* d_out,
+                              cudaStream_t stream);
+/* Backward pass: adds the gradient of the loss (given d_dout = dL/d out)
+ * with respect to every parameter into d_grad.  d_tmp1, d_tmp2:
+ * [B][32][H][W] scratch; d_wflip: 9216 floats of scratch. */
+cageo_status cageo_ws_backward(const float* d_params, const float* d_feat, const float* d_a1,
+                               const float* d_a2, const float* d_dout, int W, int H, int B,
+                               float* d_grad, float* d_tmp1, float* d_tmp2, float* d_wflip,
+                               cudaStream_t stream);
+/* Mean squared error over the cells at least `margin` cells inside each
+ * grid: writes dL/dy into d_dy and adds the loss into *d_loss. */
+cageo_status cageo_ws_mse(const float* d_y, const float* d_target, float* d_dy, float* d_loss,
+                          int W, int H, int B, int margin, cudaStream_t stream);
+/* One Adam step (bias-corrected, `step` counts from 1). */
+cageo_status cageo_ws_adam(float* d_params, const float* d_grad, float* d_m, float* d_v, int n,
+                           float lr, float beta1, float beta2, float eps, int step,
+                           cudaStream_t stream);
+/* Inference on one grid d_v [H][W] (burned realistic elevations, not
+ * quantized): d_depth (may be NULL) receives the predicted depths, d_warm
+ * (may be NULL) the warm start: v where the depth is below `threshold`,
+ * +inf elsewhere.  Hidden activations are bf16 here (fp32 in training). */
+cageo_status cageo_ws_infer(const float* d_params, const float* d_v, float* d_warm,
+                            float* d_depth, int W, int H, float nodata_dem, float threshold,
+                            cudaStream_t stream);
+
 /* ---- Pipeline: the whole Monte Carlo loop of src/main.cpp:180-283 -------
  * Owns its device buffers; runs realizations [first, first+count) with
  * noise Philox(seed, realization) and accumulates the border counts
