@@ -179,6 +179,54 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+WARM_THRESHOLD = 0.005  # metres: cells predicted shallower start at their elevation
+
+
+def exact_mode(dem, streams, cfg, steps, warmup, base):
+    """The reference GPU path's semantics (exact fill): plain realizations/s
+    and with the learned warm start (verified and repaired, so its counts
+    equal the plain ones), device-timed on the pipeline's stream."""
+    import torch
+    from cageo_gb300 import api, learned
+    out = {}
+    for name in ("plain", "learned"):
+        pe = api.Pipeline(dem, streams, fill_mode=api.FILL_EXACT, **cfg)
+        if name == "learned":
+            pe.set_warmstart(learned.load_params(), WARM_THRESHOLD)
+        pe.run(base, warmup)
+        if name == "learned":
+            pe.set_warmstart(learned.load_params(), WARM_THRESHOLD)  # reset its counters
+        ext = torch.cuda.ExternalStream(pe.stream)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(ext)
+        pe.run(base + 30_000, steps)
+        b.record(ext)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        row = {"value": steps / (ms / 1000.0), "unit": "realizations/s",
+               "ms_per_step": ms / steps}
+        if name == "plain":
+            st = pe.stats()
+            row["fill_rounds_last"] = st["flood_a_rounds"]
+            row["fill_us_last"] = st["flood_a_us"]
+            row["counts_sum"] = float(pe.counts().sum())
+        else:
+            ws = pe.warmstart_stats()
+            row.update(threshold_m=WARM_THRESHOLD, repaired_share=ws["repaired"] / max(1, ws["realizations"]),
+                       undrained_cells_per_step=ws["undrained_cells"] / max(1, ws["realizations"]),
+                       warm_fill_rounds_per_step=ws["warm_rounds"] / max(1, ws["realizations"]),
+                       repair_fill_rounds_per_step=ws["repair_rounds"] / max(1, ws["realizations"]),
+                       warm_fill_us_per_step=ws["warm_fill_us"] / max(1, ws["realizations"]),
+                       repair_fill_us_per_step=ws["repair_fill_us"] / max(1, ws["realizations"]),
+                       counts_sum=float(pe.counts().sum()))
+        out[name] = row
+        pe.close()
+    out["learned"]["counts_equal_plain"] = out["learned"]["counts_sum"] == out["plain"]["counts_sum"]
+    out["learned_over_plain"] = out["learned"]["value"] / out["plain"]["value"]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -187,6 +235,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-exact", action="store_true", help="skip the exact-mode measurement")
     ap.add_argument("--workload", default="eval-8192",
                     help="eval-8192 (the benchmark) or a smaller case for profiling (plain-4096)")
     args = ap.parse_args()
@@ -303,6 +352,8 @@ def main():
         "clocks": clocks.summary(),
     }
     line["gpu_launches"] = args.steps * KERNELS_PER_REALIZATION
+    if not args.no_exact:
+        line["exact_mode"] = exact_mode(dem, streams, cfg, args.steps, args.warmup, base)
     if not args.no_cpu_baseline:
         rate, threads, sec = cpu_rate(dem, streams, p, args.cpu_steps, 50_000)
         line["cpu_baseline"] = {"value": rate, "unit": "realizations/s", "cores": threads,

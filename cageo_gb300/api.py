@@ -95,6 +95,8 @@ _SIGS = {
     "cageo_pipeline_stats": ([_vp, _vp, _i], _i),
     "cageo_pipeline_profile": ([_vp, ctypes.c_uint32, _vp, _i], _i),
     "cageo_pipeline_destroy": ([_vp], None),
+    "cageo_pipeline_set_warmstart": ([_vp, _vp, _i, _f], _i),
+    "cageo_pipeline_warmstart_stats": ([_vp, _vp, _i], _i),
     "cageo_to_bytes": ([_vp, _vp, _i, _i, _vp], _i),
     "cageo_write_jpeg": ([ctypes.c_char_p, _vp, _i, _i, _i], _i),
     "cageo_pipeline_counts_bytes": ([_vp, _vp], _i),
@@ -407,6 +409,22 @@ class Pipeline:
         return {k: int(v) for k, v in zip(keys, s)}
 
     STAGES = ("noise", "front", "fill", "route", "trace", "border")
+
+    def set_warmstart(self, params, threshold):
+        """Learned warm start (exact mode); params None switches it off."""
+        if params is None:
+            _check(lib().cageo_pipeline_set_warmstart(self._p, None, 0, 0.0))
+            return
+        a = np.ascontiguousarray(params, np.float32)
+        _check(lib().cageo_pipeline_set_warmstart(self._p, a.ctypes.data_as(_vp), a.size,
+                                                  threshold))
+
+    def warmstart_stats(self):
+        s = np.zeros(8, np.int64)
+        _check(lib().cageo_pipeline_warmstart_stats(self._p, s.ctypes.data_as(_vp), 8))
+        keys = ("realizations", "repaired", "undrained_cells", "warm_tiles", "warm_rounds",
+                "repair_rounds", "warm_fill_us", "repair_fill_us")
+        return {k: int(v) for k, v in zip(keys, s)}
 
     def profile(self, realization):
         """Run one realization with per-stage CUDA event timing; returns {stage: ms}."""

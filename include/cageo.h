@@ -336,6 +336,20 @@ cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t realization,
  * kilo-cycles summed over them spent staging, searching and storing
  * (last realization). */
 cageo_status cageo_pipeline_stats(cageo_pipeline* p, int64_t* h_stats, int n);
+/* Learned warm start for an exact-mode pipeline (no counterpart in the
+ * reference): realizations then start the fill from the network's warm
+ * surface (cells predicted shallower than `threshold` metres at their
+ * elevation, the rest at +inf), verify it by tracing, and repair the cells
+ * that do not drain; the counts equal the plain exact fill's.  Each such
+ * realization synchronizes the stream once (no CUDA graph).  h_params:
+ * cageo_ws_param_count() floats, or NULL to switch the warm start off. */
+cageo_status cageo_pipeline_set_warmstart(cageo_pipeline* p, const float* h_params, int n,
+                                          float threshold);
+/* Counters since set_warmstart: [0] warm-started realizations, [1] of them
+ * repaired, [2] cells that did not drain before repair, [3] tile visits and
+ * [4] sweep rounds of the warm-started fills, [5] sweep rounds of the repair
+ * fills, [6] microseconds of the warm-started fills, [7] of the repairs. */
+cageo_status cageo_pipeline_warmstart_stats(cageo_pipeline* p, int64_t* h_stats, int n);
 void cageo_pipeline_destroy(cageo_pipeline* p);
 
 /* ---- A10 raster I/O -----------------------------------------------------

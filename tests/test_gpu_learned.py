@@ -90,3 +90,63 @@ def test_mse_and_adam(cuda):
     # First bias-corrected Adam step moves each parameter by lr * sign(g).
     ref = 1 - 0.1 * np.sign([1, -1, 2, 0, 0.5])
     assert np.allclose(p.cpu().numpy(), ref, atol=1e-6)
+
+
+@pytest.mark.parametrize("which", ["trained", "untrained"])
+def test_learned_pipeline_equals_plain_exact(cuda, which):
+    """Warm-started realizations are verified and repaired: counts, filled
+    surface, directions and labels equal the plain exact pipeline's, also
+    for an untrained network whose warm starts are mostly wrong."""
+    from cageo_gb300 import api, learned
+    dem, streams = make_case(300, 257, seed=12)
+    kw = dict(error_stddev=1.5, seed=5, fill_mode=api.FILL_EXACT)
+    plain = api.Pipeline(dem, streams, **kw)
+    plain.run(0, 4)
+    lp = api.Pipeline(dem, streams, **kw)
+    if which == "trained":
+        lp.set_warmstart(learned.load_params(), 0.005)
+    else:
+        lp.set_warmstart(learned.init_params(7), 0.5)
+    lp.run(0, 4)
+    assert np.array_equal(lp.counts(), plain.counts())
+    for a, b in zip(lp.last_stages(), plain.last_stages()):
+        assert np.array_equal(a, b)
+    st = lp.warmstart_stats()
+    assert st["realizations"] == 4
+    if which == "untrained":
+        assert st["repaired"] >= 1 and st["undrained_cells"] > 0
+    lp.set_warmstart(None, 0.0)
+    lp.run(4, 1)
+    plain.run(4, 1)
+    assert np.array_equal(lp.counts(), plain.counts())
+
+
+def test_trained_network_saves_fill_sweeps(cuda):
+    """What the trained network gains: its warm start (before verification)
+    needs fewer sweep rounds than the cold fill, and far fewer of the cells it
+    starts at their own elevation are wrong (wet cells marked dry, each of
+    which forces a repair) than with the untrained network."""
+    from cageo_gb300 import api, learned
+    import torch
+    src = learned.PairSource(size=512, tiles=2, seed=4242)
+    trained, untrained = learned.load_params(), learned.init_params(3)
+    rounds = {}
+    for name, prm in (("trained", trained), ("untrained", untrained)):
+        p = torch.from_numpy(prm).cuda()
+        tot = dict(cold=0, warm=0, dry_hits=0, false_dry=0)
+        for j in range(3):
+            v = src.realization(j % 2, 500 + j)
+            filled = api.pitfill(v, mode=api.FILL_EXACT)
+            warm, _ = api.ws_infer(p, v, threshold=0.005)
+            _, sc = api.pitfill_exact_warm(v)
+            _, sw = api.pitfill_exact_warm(v, warm)
+            marked = torch.isfinite(warm)
+            tot["cold"] += sc["rounds"]
+            tot["warm"] += sw["rounds"]
+            tot["dry_hits"] += int((marked & (filled == v)).sum())
+            tot["false_dry"] += int((marked & (filled > v)).sum())
+        rounds[name] = tot
+    print("warm-start sweep rounds:", rounds)
+    assert rounds["trained"]["warm"] < rounds["trained"]["cold"]
+    share = {k: r["false_dry"] / max(1, r["false_dry"] + r["dry_hits"]) for k, r in rounds.items()}
+    assert share["trained"] < share["untrained"] / 3
