@@ -168,7 +168,7 @@ def run_reference(args, rank, world):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 / rate, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.workload, "width": W, "height": H, "filter": "Gaussian 60 m",
+            "config": {"workload": args.workload, "width": W, "height": H, "filter": "Gaussian %g m" % p["range_m"],
                        "error_sd": p["sigma"], "pits": p["pits"], "stream_threshold": p["threshold"],
                        "parallelism": "cpu"},
             "cpu_baseline": {"value": rate, "unit": "realizations/s", "cores": threads,
@@ -326,7 +326,7 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded fBm DEM + pits, D8-accumulation streams)",
-        "config": {"workload": args.workload, "width": W, "height": H, "filter": "Gaussian 60 m",
+        "config": {"workload": args.workload, "width": W, "height": H, "filter": "Gaussian %g m" % p["range_m"],
                    "error_sd": p["sigma"], "pits": p["pits"], "stream_threshold": p["threshold"],
                    "hurst": p["hurst"], "relief_m": [p["lo"], p["hi"]],
                    "realizations_per_step": 1, "l2": "inputs larger than L2 (256 MiB grids)",

@@ -104,6 +104,11 @@ WORKLOADS = {
     "eval-8192": dict(width=8192, height=8192, hurst=0.8, seed=3, lo=0.0, hi=300.0, pits=20000,
                       threshold=2000, model="Gaussian", range_m=60.0, sigma=1.5, cell=10.0,
                       realizations=100),
+    # Stress case: 16384^2 with 20 % of the area in flat lake plateaus
+    # (constant-elevation discs of radius 50-400 cells), Gaussian 90 m.
+    "stress-16384": dict(width=16384, height=16384, hurst=0.8, seed=5, lo=0.0, hi=300.0,
+                         pits=80000, threshold=2000, model="Gaussian", range_m=90.0, sigma=1.5,
+                         cell=10.0, realizations=1000, plateaus=0.2),
 }
 
 
@@ -130,5 +135,7 @@ def workload(name, ids="ones", scale=None):
         p["pits"] = max(int(p["pits"] * scale * scale), 1)
     dem = fbm_dem(p["width"], p["height"], p["hurst"], p["seed"], p["lo"], p["hi"])
     dem = add_pits(dem, p["pits"], p["seed"])
+    if p.get("plateaus"):
+        dem = add_plateaus(dem, p["plateaus"], p["seed"], radius=(50, 400))
     streams = make_streams(dem, p["threshold"], ids=ids)
     return dem, streams, p
