@@ -77,7 +77,7 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 constexpr int kTile = 32;
-constexpr int kWarps = 16;  // one 512-thread block per SM (16 x 10 KB smem)
+constexpr int kWarps = 15;  // one 480-thread block per SM (15 x 14.5 KB smem)
 constexpr int kRS = 35;           // relay row stride (34 used)
 constexpr int kWS = 33;           // W/q row stride
 constexpr int kFS = 36;           // flag row stride (bytes)
@@ -90,6 +90,7 @@ constexpr int kMaxPasses = 1000000;
 struct WarpSmem {
   float R[34 * kRS];
   float Wv[kTile * kWS];
+  float Q[kTile * kWS];  // q of the tile's own cells
   uint8_t F[kTile * kFS];
 };
 
@@ -162,12 +163,11 @@ __device__ __forceinline__ void enqueue(const FillWork& w, int t, int k) {
 // dropped below its own q (FBELOW) is final in both floods: its value is q
 // and its relay can no longer change.
 template <int MODE>
-__device__ __forceinline__ bool update_cell(WarpSmem& s, const float* __restrict__ qt, int W,
-                                            int x, int y, float m) {
+__device__ __forceinline__ bool update_cell(WarpSmem& s, int x, int y, float m) {
   uint8_t f = s.F[y * kFS + x];
   if (f & (FNODATA | FOUTLET | FBELOW)) return false;
   float w = s.Wv[y * kWS + x];
-  float qv = __ldg(qt + (int64_t)y * W + x);
+  float qv = s.Q[y * kWS + x];
   float nw = fminf(w, fmaxf(qv, m));
   uint8_t nf = f | ((m < qv) ? FBELOW : 0);
   if (nw != w || nf != f) {
@@ -209,12 +209,12 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
     s.R[hy * kRS + hx] = relay<MODE>(wv, fv, qv);
     if (hx >= 1 && hx <= kTile && hy >= 1 && hy <= kTile) {
       s.Wv[(hy - 1) * kWS + hx - 1] = wv;
+      s.Q[(hy - 1) * kWS + hx - 1] = qv;
       s.F[(hy - 1) * kFS + hx - 1] = fv;
     }
   }
   __syncwarp();
   const long long c1 = clock64();
-  const float* qt = a.q + (int64_t)y0 * W + x0;  // q of the tile's cell (0, 0)
   // Sweeps.  A cell needs re-evaluating only after one of its 8 neighbours
   // changed, so each phase carries warp-uniform masks of the rows (vertical
   // phase) or columns (horizontal phase) to evaluate: all rows first, then
@@ -239,11 +239,11 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
       unsigned int b1 = 0, b2 = 0;
       if ((pend >> d) & 1u) {
         const float m = nbr_min(s, lane, d);
-        b1 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, qt, W, lane, d, m));
+        b1 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, lane, d, m));
       }
       if ((pend >> u) & 1u) {
         const float m = nbr_min(s, lane, u);
-        b2 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, qt, W, lane, u, m));
+        b2 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, lane, u, m));
       }
       if (b1) { cch |= b1; pend |= smear(1u << d); }
       if (b2) { cch |= b2; pend |= smear(1u << u); }
@@ -255,11 +255,11 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
       unsigned int b1 = 0, b2 = 0;
       if ((pendc >> l) & 1u) {
         const float m = nbr_min(s, l, lane);
-        b1 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, qt, W, l, lane, m));
+        b1 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, l, lane, m));
       }
       if ((pendc >> r) & 1u) {
         const float m = nbr_min(s, r, lane);
-        b2 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, qt, W, r, lane, m));
+        b2 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, r, lane, m));
       }
       if (b1) { rch2 |= b1; pendc |= smear(1u << l); }
       if (b2) { rch2 |= b2; pendc |= smear(1u << r); }
