@@ -50,10 +50,10 @@ PIPE_BYTES = 75
 # 1702 MB for 16.8 M cells), applied per cell to the benchmark grid.
 FILL_TRAFFIC_PER_CELL = 1702.2e6 / (4096 * 4096)
 # Kernels per realization on the graph path: fill 6 (scalars, init, two
-# floods, classify, final), noise 1, front 1, routing 5 (scalars, d8, flat
-# relaxation, flat directions, flat final), tracing 4 (scalars, init, jump,
+# floods, classify, final), noise 1, front 1, routing 4 (scalars, d8, flat
+# relaxation, flat directions), tracing 4 (scalars, init, jump,
 # final), border 1, realization end 1.
-KERNELS_PER_REALIZATION = 19
+KERNELS_PER_REALIZATION = 18
 
 
 def peak_hbm():

@@ -395,65 +395,56 @@ flat_relax_kernel(const float* __restrict__ dem, int* fd, RouteWork w, int gpu, 
   }
 }
 
-// Directions of flat cells: last neighbour (N..NW) in the previous layer
-// (or with flatDist -1 for layer 1) whose elevation is <= the cell's.
-__global__ void flat_dir_kernel(const float* __restrict__ dem, char2* __restrict__ dir,
-                                int* __restrict__ fd, RouteWork w) {
+// Directions of flat cells, and flatDist 0 for the flats left unresolved,
+// over the tiles that hold flat cells only (a 32x8 block per 32x32 tile, 4
+// rows per thread).  CPU rules: the LAST neighbour in N..NW order in the
+// previous layer (flatDist -1 for layer 1) whose elevation is <= the
+// cell's.  GPU order: the FIRST neighbour in N, W, E, S, NW, NE, SW, SE
+// order that is (layer 1) a non-NODATA cell with a negative flatDist and an
+// elevation <= the cell's, or (layer d > 1) a cell of layers 1..d-1.  A
+// neighbour reset from "unresolved" to 0 meanwhile matches neither rule
+// before or after, so the reset can share the pass.
+template <bool GPU>
+__global__ void __launch_bounds__(256) flat_dir_kernel(const float* __restrict__ dem,
+                                                       char2* __restrict__ dir,
+                                                       int* __restrict__ fd, RouteWork w,
+                                                       float nodata) {
+  if (!w.tflat[blockIdx.y * w.tiles_x + blockIdx.x]) return;
   const int W = w.W, H = w.H;
-  const int64_t N = (int64_t)W * H;
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < N;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    const int d = fd[c];
-    if (d < 1 || d == kFlatInf) continue;  // not a flat cell with a layer
-    int x = (int)(c % (uint32_t)W), y = (int)(c / (uint32_t)W);
-    const float e = dem[c];
-    const int want = d == 1 ? -1 : d - 1;
-    int nf[8];
-    float ne[8];
-    gather8(dem, fd, W, H, x, y, nf, ne);
-    int got = -1;
-#pragma unroll
-    for (int n = 0; n < 8; n++)
-      if (nf[n] == want && ne[n] <= e) got = n;
-    if (got >= 0) dir[c] = make_char2((signed char)d8_dx(got), (signed char)d8_dy(got));
-  }
-}
-
-// GPU order: the first neighbour in N, W, E, S, NW, NE, SW, SE order that is
-// (layer 1) a non-NODATA cell with a negative flatDist and an elevation <=
-// the cell's, or (layer d > 1) a cell of layers 1..d-1.
-__global__ void flat_dir_gpu_kernel(const float* __restrict__ dem, char2* __restrict__ dir,
-                                    int* __restrict__ fd, RouteWork w, float nodata) {
-  const int W = w.W, H = w.H;
-  const int64_t N = (int64_t)W * H;
+  const int x = blockIdx.x * kFT + threadIdx.x;
   constexpr int order[8] = {0, 6, 2, 4, 7, 1, 5, 3};  // N W E S NW NE SW SE as D8 indices
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < N;
-       c += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll 1
+  for (int k = 0; k < kFT / 8; k++) {
+    const int y = blockIdx.y * kFT + threadIdx.y + 8 * k;
+    if (x >= W || y >= H) continue;
+    const int64_t c = (int64_t)y * W + x;
     const int d = fd[c];
-    if (d < 1 || d == kFlatInf) continue;
-    int x = (int)(c % (uint32_t)W), y = (int)(c / (uint32_t)W);
+    if (d == kFlatInf) {
+      fd[c] = 0;
+      continue;
+    }
+    if (d < 1) continue;  // not a flat cell with a layer
     const float e = dem[c];
     int nf[8];
     float ne[8];
     gather8(dem, fd, W, H, x, y, nf, ne);
     int got = -1;
+    if (GPU) {
 #pragma unroll
-    for (int k = 7; k >= 0; k--) {
-      const int n = order[k];
-      const bool ok = d == 1 ? (nf[n] < 0 && nf[n] != kOffGrid && ne[n] != nodata && ne[n] <= e)
-                             : (nf[n] >= 1 && nf[n] <= d - 1);
-      if (ok) got = n;
+      for (int q = 7; q >= 0; q--) {
+        const int n = order[q];
+        const bool ok = d == 1 ? (nf[n] < 0 && nf[n] != kOffGrid && ne[n] != nodata && ne[n] <= e)
+                               : (nf[n] >= 1 && nf[n] <= d - 1);
+        if (ok) got = n;
+      }
+    } else {
+      const int want = d == 1 ? -1 : d - 1;
+#pragma unroll
+      for (int n = 0; n < 8; n++)
+        if (nf[n] == want && ne[n] <= e) got = n;
     }
     if (got >= 0) dir[c] = make_char2((signed char)d8_dx(got), (signed char)d8_dy(got));
   }
-}
-
-// Unresolved flats end as flatDist 0 with no direction.
-__global__ void flat_final_kernel(int* __restrict__ fd, RouteWork w) {
-  const int64_t N = (int64_t)w.W * w.H;
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < N;
-       c += (int64_t)gridDim.x * blockDim.x)
-    if (fd[c] == kFlatInf) fd[c] = 0;
 }
 
 __global__ void route_scalars_kernel(unsigned int* s) {
@@ -490,13 +481,8 @@ cageo_status route_run(const float* filled, int8_t* dir, int* fd, const RouteWor
   void* params[] = {(void*)&f, (void*)&fdp, (void*)&wc, (void*)&gflag, (void*)&nd};
   CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)flat_relax_kernel, dim3(coop),
                                          dim3(kFWarps * 32), params, smem, s));
-  int sms = 0, dev = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const unsigned lb = (unsigned)sms * 16;
-  if (gpu) flat_dir_gpu_kernel<<<lb, 256, 0, s>>>(filled, (char2*)dir, fd, w, nodata);
-  else flat_dir_kernel<<<lb, 256, 0, s>>>(filled, (char2*)dir, fd, w);
-  flat_final_kernel<<<lb, 256, 0, s>>>(fd, w);
+  if (gpu) flat_dir_kernel<true><<<g, b, 0, s>>>(filled, (char2*)dir, fd, w, nodata);
+  else flat_dir_kernel<false><<<g, b, 0, s>>>(filled, (char2*)dir, fd, w, nodata);
   CAGEO_CUDA(cudaGetLastError());
   return CAGEO_OK;
 }
