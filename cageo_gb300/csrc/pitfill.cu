@@ -89,8 +89,7 @@ constexpr int kMaxPasses = 1000000;
 // cache instead of being staged.
 struct WarpSmem {
   float R[34 * kRS];
-  float Wv[kTile * kWS];
-  float Q[kTile * kWS];  // q of the tile's own cells
+  float2 WQ[kTile * kWS];  // (W, q) of the tile's own cells
   uint8_t F[kTile * kFS];
 };
 
@@ -166,12 +165,12 @@ template <int MODE>
 __device__ __forceinline__ bool update_cell(WarpSmem& s, int x, int y, float m) {
   uint8_t f = s.F[y * kFS + x];
   if (f & (FNODATA | FOUTLET | FBELOW)) return false;
-  float w = s.Wv[y * kWS + x];
-  float qv = s.Q[y * kWS + x];
+  const float2 wq = s.WQ[y * kWS + x];
+  const float w = wq.x, qv = wq.y;
   float nw = fminf(w, fmaxf(qv, m));
   uint8_t nf = f | ((m < qv) ? FBELOW : 0);
   if (nw != w || nf != f) {
-    s.Wv[y * kWS + x] = nw;
+    s.WQ[y * kWS + x].x = nw;
     s.F[y * kFS + x] = nf | FDIRTY;
     s.R[(y + 1) * kRS + (x + 1)] = relay<MODE>(nw, nf, qv);
     return true;
@@ -208,8 +207,7 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
     }
     s.R[hy * kRS + hx] = relay<MODE>(wv, fv, qv);
     if (hx >= 1 && hx <= kTile && hy >= 1 && hy <= kTile) {
-      s.Wv[(hy - 1) * kWS + hx - 1] = wv;
-      s.Q[(hy - 1) * kWS + hx - 1] = qv;
+      s.WQ[(hy - 1) * kWS + hx - 1] = make_float2(wv, qv);
       s.F[(hy - 1) * kFS + hx - 1] = fv;
     }
   }
@@ -281,7 +279,7 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
     uint8_t f = s.F[y * kFS + x];
     if (f & FDIRTY) {
       int64_t i = (int64_t)(y0 + y) * W + (x0 + x);
-      a.Wg[i] = s.Wv[y * kWS + x];
+      a.Wg[i] = s.WQ[y * kWS + x].x;
       w.flags[i] = f & (uint8_t)~FDIRTY;
       if (x == 0) sides |= 1;
       if (x == kTile - 1) sides |= 2;
