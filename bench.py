@@ -264,7 +264,9 @@ def main():
     from cageo_gb300.replicas import realization_range
     # disjoint realization numbers per rank (replicas; weak scaling)
     base, _ = realization_range(rank, world, world * 1_000_000)
-    # Warm-up: graph capture + stage profile.
+    # Autotuning (sweep rounds per fill tile visit), then warm-up: graph
+    # capture + stage profile.  Neither is timed.
+    tuned, tune_ms = pipe.autotune(base + 900_000, trials=2)
     pipe.run(base, args.warmup)
     stage_ms = pipe.profile(base + args.warmup)
     stats = pipe.stats()
@@ -331,7 +333,9 @@ def main():
                    "hurst": p["hurst"], "relief_m": [p["lo"], p["hi"]],
                    "realizations_per_step": 1, "l2": "inputs larger than L2 (256 MiB grids)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "cuda_graph": True},
+                   "cuda_graph": True,
+                   "autotune": {"fill_rounds_per_visit": tuned,
+                                "ms_per_realization": {str(k): v for k, v in tune_ms.items()}}},
         "cells_per_s": value * N,
         "e2e": {"value": e2e_value, "unit": "realizations/s",
                 "h2d_bytes_per_step": int(2 * 4 * N / args.steps),

@@ -96,6 +96,7 @@ _SIGS = {
     "cageo_pipeline_profile": ([_vp, ctypes.c_uint32, _vp, _i], _i),
     "cageo_pipeline_destroy": ([_vp], None),
     "cageo_pipeline_set_warmstart": ([_vp, _vp, _i, _f], _i),
+    "cageo_pipeline_autotune": ([_vp, ctypes.c_uint32, _i, _vp, _vp], _i),
     "cageo_pipeline_warmstart_stats": ([_vp, _vp, _i], _i),
     "cageo_to_bytes": ([_vp, _vp, _i, _i, _vp], _i),
     "cageo_write_jpeg": ([ctypes.c_char_p, _vp, _i, _i, _i], _i),
@@ -409,6 +410,15 @@ class Pipeline:
         return {k: int(v) for k, v in zip(keys, s)}
 
     STAGES = ("noise", "front", "fill", "route", "trace", "border")
+
+    def autotune(self, first, trials=3):
+        """Pick the fill's sweep rounds per tile visit by timing; resets the
+        counts.  Returns (chosen rounds, {rounds: ms per realization})."""
+        best = ctypes.c_int()
+        ms = np.zeros(5, np.float32)
+        _check(lib().cageo_pipeline_autotune(self._p, first, trials, ctypes.byref(best),
+                                             ms.ctypes.data_as(_vp)))
+        return best.value, dict(zip((4, 8, 16, 32, 64), (float(v) for v in ms)))
 
     def set_warmstart(self, params, threshold):
         """Learned warm start (exact mode); params None switches it off."""

@@ -661,6 +661,65 @@ extern "C" cageo_status cageo_pipeline_reset_counts(cageo_pipeline* p) {
   return CAGEO_OK;
 }
 
+// Autotuning of the fill's sweep rounds per tile visit (the halo-sweep
+// count): each candidate runs `trials` realizations on the fast path
+// (direct launches, timed with events on the pipeline's stream); the
+// fastest is kept and the CUDA graph is captured again on the next run.
+// The counts are reset to zero afterwards.
+extern "C" cageo_status cageo_pipeline_autotune(cageo_pipeline* p, uint32_t first, int trials,
+                                                int* h_best_rounds, float* h_ms) {
+  CAGEO_CHECK_ARG(p && trials >= 1, "pipeline and trials");
+  CAGEO_CHECK_ARG(p->cfg.nodata_dem != 0.0f && !p->ws_params,
+                  "autotuning times the fused path (NODATA != 0, no warm start)");
+  static const int kCand[5] = {4, 8, 16, 32, 64};
+  cudaStream_t s = p->stream;
+  cudaEvent_t e0, e1;
+  CAGEO_CUDA(cudaEventCreate(&e0));
+  CAGEO_CUDA(cudaEventCreate(&e1));
+  cageo_status st = CAGEO_OK;
+  float best_ms = 0.0f;
+  int best = p->fw.max_rounds;
+  for (int c = 0; c < 5 && st == CAGEO_OK; c++) {
+    p->fw.max_rounds = kCand[c];
+    uint32_t r0 = first + (uint32_t)(c * (trials + 1));
+    if (cudaMemcpyAsync(p->dscal, &r0, sizeof(r0), cudaMemcpyHostToDevice, s) != cudaSuccess) {
+      st = cuda_fail(cudaGetLastError(), "cudaMemcpyAsync");
+      break;
+    }
+    if ((st = enqueue_fast(p))) break;  // warm-up
+    cudaEventRecord(e0, s);
+    for (int k = 0; k < trials && st == CAGEO_OK; k++) st = enqueue_fast(p);
+    cudaEventRecord(e1, s);
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      st = cuda_fail(cudaGetLastError(), "cudaEventSynchronize");
+      break;
+    }
+    if (st == CAGEO_OK) st = fill_check_status(p->fw, nullptr);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms /= (float)trials;
+    if (h_ms) h_ms[c] = ms;
+    if (c == 0 || ms < best_ms) {
+      best_ms = ms;
+      best = kCand[c];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  p->fw.max_rounds = best;
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  p->exec = nullptr;
+  p->graph = nullptr;
+  p->graph_ok = false;
+  if (h_best_rounds) *h_best_rounds = best;
+  CAGEO_CUDA(cudaMemsetAsync(p->counts, 0, 4 * (size_t)p->N, s));
+  CAGEO_CUDA(cudaMemsetAsync(p->dscal + 1, 0, 2 * sizeof(uint32_t), s));
+  CAGEO_CUDA(cudaStreamSynchronize(s));
+  return CAGEO_OK;
+}
+
 extern "C" cageo_status cageo_pipeline_set_warmstart(cageo_pipeline* p, const float* h_params,
                                                      int n, float threshold) {
   CAGEO_CHECK_ARG(p, "null pipeline");

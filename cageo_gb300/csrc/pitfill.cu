@@ -81,7 +81,6 @@ constexpr int kWarps = 15;  // one 480-thread block per SM (15 x 14.5 KB smem)
 constexpr int kRS = 35;           // relay row stride (34 used)
 constexpr int kWS = 33;           // W/q row stride
 constexpr int kFS = 36;           // flag row stride (bytes)
-constexpr int kMaxRounds = 64;
 constexpr int kMaxPasses = 1000000;
 
 // Per-warp staged tile: relay values with halo, W and flags of the tile's
@@ -226,10 +225,11 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
   // only its border rows and columns need evaluating first.
   const bool revisit = w.tconv[t] != 0;
   bool capped = true;
-  int rounds = kMaxRounds;
+  const int max_rounds = w.max_rounds;
+  int rounds = max_rounds;
   unsigned int next_rows = revisit ? 0x80000001u : 0xffffffffu;
   unsigned int first_cols = revisit ? 0x80000001u : 0u;
-  for (int round = 0; round < kMaxRounds; round++) {
+  for (int round = 0; round < max_rounds; round++) {
     unsigned int pend = next_rows, cch = first_cols;
     first_cols = 0;
     for (int k = 0; k < kTile; k++) {

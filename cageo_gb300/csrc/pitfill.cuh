@@ -22,6 +22,7 @@ struct FillWork {
   uint32_t* aux = nullptr;       // W*H: flood A's result, then component labels
   uint32_t* cmin = nullptr;      // W*H: per-component phase minima (at roots)
   unsigned int* scal = nullptr;  // scalar block (see pitfill.cu)
+  int max_rounds = 64;           // sweep rounds per tile visit before the tile re-queues itself
 };
 
 size_t fill_workspace_bytes(int W, int H);

@@ -336,6 +336,15 @@ cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t realization,
  * kilo-cycles summed over them spent staging, searching and storing
  * (last realization). */
 cageo_status cageo_pipeline_stats(cageo_pipeline* p, int64_t* h_stats, int n);
+/* Autotuner (no counterpart in the reference): times the fill with 4, 8,
+ * 16, 32 and 64 sweep rounds per tile visit (a tile that has not converged
+ * after that many rounds queues itself for the next pass), `trials`
+ * realizations each from `first_realization` on, and keeps the fastest.
+ * The results do not depend on the choice.  h_best_rounds (may be NULL)
+ * receives the choice, h_ms (may be NULL) 5 milliseconds per realization.
+ * Resets the counts to zero. */
+cageo_status cageo_pipeline_autotune(cageo_pipeline* p, uint32_t first_realization,
+                                     int trials, int* h_best_rounds, float* h_ms);
 /* Learned warm start for an exact-mode pipeline (no counterpart in the
  * reference): realizations then start the fill from the network's warm
  * surface (cells predicted shallower than `threshold` metres at their

@@ -89,3 +89,17 @@ def test_checkpoint_resume(cuda, tmp_path):
     other = api.Pipeline(dem, streams, seed=5)
     with pytest.raises(api.CageoError):
         other.load(str(tmp_path / "ck.bin"))
+
+
+def test_autotune_keeps_counts(cuda):
+    """The autotuner only changes how many sweep rounds a tile visit may run
+    before re-queueing itself: counts equal an untuned pipeline's."""
+    from cageo_gb300 import api
+    dem, streams = make_case(300, 200, seed=44)
+    a = api.Pipeline(dem, streams, error_stddev=1.5, seed=9)
+    best, ms = a.autotune(1000, trials=2)
+    assert best in (4, 8, 16, 32, 64) and all(v > 0 for v in ms.values())
+    a.run(0, 3)
+    b = api.Pipeline(dem, streams, error_stddev=1.5, seed=9)
+    b.run(0, 3)
+    assert np.array_equal(a.counts(), b.counts())
