@@ -69,26 +69,6 @@ __global__ void repair_start_kernel(const int* __restrict__ label,
   if (i < n) warm[i] = label[i] == kError ? kInf : filled[i];
 }
 
-// Accumulate the border mask unless the realization was flagged; a flagged
-// realization index is appended to the redo list.
-__global__ void border_gated_kernel(const int* __restrict__ label, uint32_t* __restrict__ count,
-                                    int W, int H, const int* __restrict__ anomaly) {
-  if (*anomaly) return;
-  int x = blockIdx.x * blockDim.x + threadIdx.x;
-  int y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= W || y >= H) return;
-  int64_t i = (int64_t)y * W + x;
-  const int c = label[i];
-  if (c == kLake) return;
-#pragma unroll
-  for (int n = 0; n < 8; n++) {
-    int nx = x + d8_dx(n), ny = y + d8_dy(n);
-    if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
-    int v = label[(int64_t)ny * W + nx];
-    if (c < v && v != kLake) { count[i] += 1u; return; }
-  }
-}
-
 // End of a realization: record a flagged realization, clear the flag and
 // advance the device realization counter.
 __global__ void realization_end_kernel(uint32_t* real, int* anomaly, uint32_t* redo,
@@ -192,8 +172,8 @@ cageo_status enqueue_fast(cageo_pipeline* p) {
   if ((st = enqueue_fill(p))) return st;
   if ((st = enqueue_route(p))) return st;
   if ((st = enqueue_trace(p))) return st;
-  dim3 b(32, 8), g((p->W + 31) / 32, (p->H + 7) / 8);
-  border_gated_kernel<<<g, b, 0, s>>>(p->label, p->counts, p->W, p->H, (const int*)p->dscal + 1);
+  if ((st = border_u32_gated(p->label, p->counts, p->W, p->H, (const int*)p->dscal + 1, s)))
+    return st;
   realization_end_kernel<<<1, 32, 0, s>>>(p->dscal, (int*)p->dscal + 1, p->dscal + 3,
                                           p->dscal + 2);
   CAGEO_CUDA(cudaGetLastError());
@@ -245,8 +225,8 @@ cageo_status run_learned(cageo_pipeline* p) {
     p->ws_stats[5] += fs[8];
     p->ws_stats[7] += fs[4];
   }
-  dim3 b(32, 8), g((p->W + 31) / 32, (p->H + 7) / 8);
-  border_gated_kernel<<<g, b, 0, s>>>(p->label, p->counts, p->W, p->H, (const int*)p->dscal + 1);
+  if ((st = border_u32_gated(p->label, p->counts, p->W, p->H, (const int*)p->dscal + 1, s)))
+    return st;
   realization_end_kernel<<<1, 32, 0, s>>>(p->dscal, (int*)p->dscal + 1, p->dscal + 3,
                                           p->dscal + 2);
   CAGEO_CUDA(cudaGetLastError());
@@ -487,9 +467,8 @@ extern "C" cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t reali
     cudaEventRecord(ev[4], s);
     if ((st = enqueue_trace(p))) break;
     cudaEventRecord(ev[5], s);
-    dim3 b(32, 8), g((p->W + 31) / 32, (p->H + 7) / 8);
-    border_gated_kernel<<<g, b, 0, s>>>(p->label, p->counts, p->W, p->H,
-                                        (const int*)p->dscal + 1);
+    if ((st = border_u32_gated(p->label, p->counts, p->W, p->H, (const int*)p->dscal + 1, s)))
+      break;
     realization_end_kernel<<<1, 32, 0, s>>>(p->dscal, (int*)p->dscal + 1, p->dscal + 3,
                                             p->dscal + 2);
     cudaEventRecord(ev[6], s);

@@ -46,5 +46,8 @@ cageo_status border_float(const int* label, float* count, int W, int H,
                           cudaStream_t s);
 cageo_status border_u32(const int* label, uint32_t* count, int W, int H,
                         cudaStream_t s);
+// The same, skipped entirely when *gate (device) is non-zero.
+cageo_status border_u32_gated(const int* label, uint32_t* count, int W, int H,
+                              const int* gate, cudaStream_t s);
 
 }  // namespace cageo

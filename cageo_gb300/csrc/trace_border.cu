@@ -213,40 +213,62 @@ cageo_status trace_check_status(const TraceWork& w, int64_t* jumps) {
 }
 
 // ---- A9 -------------------------------------------------------------------
+// One 32x32 tile per block: the labels of the tile and a one-cell halo are
+// staged in shared memory (cells outside the grid read as LAKE, which never
+// makes a border), then each thread tests 4 cells.  `gate` (may be null):
+// a flag that, when set, skips the accumulation for this realization.
 template <typename T>
-__global__ void border_kernel(const int* __restrict__ label, T* __restrict__ count, int W,
-                              int H) {
-  int x = blockIdx.x * blockDim.x + threadIdx.x;
-  int y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= W || y >= H) return;
-  int64_t i = (int64_t)y * W + x;
-  const int c = label[i];
-  bool border = false;
-  if (c != kLake) {
+__global__ void __launch_bounds__(256) border_kernel(const int* __restrict__ label,
+                                                     T* __restrict__ count, int W, int H,
+                                                     const int* __restrict__ gate) {
+  if (gate && *gate) return;
+  __shared__ int L[34 * 35];
+  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+  for (int k = threadIdx.y * 32 + threadIdx.x; k < 34 * 34; k += 256) {
+    const int hy = k / 34, hx = k - hy * 34;
+    const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
+    L[hy * 35 + hx] =
+        (gx >= 0 && gx < W && gy >= 0 && gy < H) ? label[(int64_t)gy * W + gx] : kLake;
+  }
+  __syncthreads();
+  const int tx = threadIdx.x, x = x0 + tx;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int ty = threadIdx.y + 8 * k, y = y0 + ty;
+    if (x >= W || y >= H) continue;
+    const int* c = &L[(ty + 1) * 35 + tx + 1];
+    if (*c == kLake) continue;
+    bool border = false;
 #pragma unroll
     for (int n = 0; n < 8; n++) {
-      int nx = x + d8_dx(n), ny = y + d8_dy(n);
-      if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
-      int v = label[(int64_t)ny * W + nx];
-      if (c < v && v != kLake) { border = true; break; }
+      const int v = c[d8_dy(n) * 35 + d8_dx(n)];
+      border |= *c < v && v != kLake;
+    }
+    if (border) {
+      const int64_t i = (int64_t)y * W + x;
+      count[i] = count[i] + (T)1;
     }
   }
-  if (border) count[i] = count[i] + (T)1;
 }
 
 template <typename T>
-static cageo_status launch_border(const int* label, T* count, int W, int H, cudaStream_t s) {
-  dim3 b(32, 8), g((W + 31) / 32, (H + 7) / 8);
-  border_kernel<T><<<g, b, 0, s>>>(label, count, W, H);
+static cageo_status launch_border(const int* label, T* count, int W, int H, const int* gate,
+                                  cudaStream_t s) {
+  dim3 b(32, 8), g((W + 31) / 32, (H + 31) / 32);
+  border_kernel<T><<<g, b, 0, s>>>(label, count, W, H, gate);
   CAGEO_CUDA(cudaGetLastError());
   return CAGEO_OK;
 }
 
 cageo_status border_float(const int* label, float* count, int W, int H, cudaStream_t s) {
-  return launch_border(label, count, W, H, s);
+  return launch_border(label, count, W, H, nullptr, s);
 }
 cageo_status border_u32(const int* label, uint32_t* count, int W, int H, cudaStream_t s) {
-  return launch_border(label, count, W, H, s);
+  return launch_border(label, count, W, H, nullptr, s);
+}
+cageo_status border_u32_gated(const int* label, uint32_t* count, int W, int H, const int* gate,
+                              cudaStream_t s) {
+  return launch_border(label, count, W, H, gate, s);
 }
 
 }  // namespace cageo
