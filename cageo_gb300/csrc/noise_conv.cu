@@ -51,7 +51,7 @@ __global__ void noise_kernel(float* __restrict__ out, int64_t n, uint32_t k0,
 }
 
 // ---- A3 separable (Gaussian) ----------------------------------------------
-constexpr int kSepTW = 64, kSepTH = 32, kSepThreads = 256;
+constexpr int kSepTW = 64, kSepTH = 64, kSepThreads = 256;
 
 __device__ inline int wrap_idx(int v, int n) {
   v %= n;
@@ -94,7 +94,10 @@ __device__ inline void block_min_out(float local_min, const FrontEpilogue& e) {
 }
 
 // 8 outputs along a line from a sliding window of 8 registers: out[j] =
-// sum_t v[j + t] * taps[t], t ascending, each sum starting at 0.
+// sum_t v[j + t] * taps[t], t ascending, each sum starting at 0.  LC > 0:
+// the tap count is a compile-time constant and the loop is fully unrolled
+// (the window shifts become register renames); LC = 0: runtime count L.
+template <int LC>
 __device__ __forceinline__ void conv_line8(const float* __restrict__ v, int stride,
                                            const float* __restrict__ taps, int L,
                                            float acc[8]) {
@@ -104,18 +107,30 @@ __device__ __forceinline__ void conv_line8(const float* __restrict__ v, int stri
     win[j] = v[j * stride];
     acc[j] = 0.0f;
   }
+  if (LC > 0) {
+#pragma unroll
+    for (int t = 0; t < LC; t++) {
+      const float tap = taps[t];
+#pragma unroll
+      for (int j = 0; j < 8; j++) acc[j] = __fadd_rn(acc[j], __fmul_rn(win[j], tap));
+#pragma unroll
+      for (int j = 0; j < 7; j++) win[j] = win[j + 1];
+      if (t + 1 < LC) win[7] = v[(t + 8) * stride];
+    }
+  } else {
 #pragma unroll 8
-  for (int t = 0; t < L; t++) {
-    const float tap = taps[t];
+    for (int t = 0; t < L; t++) {
+      const float tap = taps[t];
 #pragma unroll
-    for (int j = 0; j < 8; j++) acc[j] = __fadd_rn(acc[j], __fmul_rn(win[j], tap));
+      for (int j = 0; j < 8; j++) acc[j] = __fadd_rn(acc[j], __fmul_rn(win[j], tap));
 #pragma unroll
-    for (int j = 0; j < 7; j++) win[j] = win[j + 1];
-    win[7] = (t + 1 < L) ? v[(t + 8) * stride] : 0.0f;
+      for (int j = 0; j < 7; j++) win[j] = win[j + 1];
+      win[7] = (t + 1 < L) ? v[(t + 8) * stride] : 0.0f;
+    }
   }
 }
 
-template <class Epi>
+template <class Epi, int LC>
 __global__ void __launch_bounds__(kSepThreads)
 conv_sep_kernel(const float* __restrict__ in, int W, int H,
                 const float* __restrict__ taps, int r, Epi epi) {
@@ -137,7 +152,7 @@ conv_sep_kernel(const float* __restrict__ in, int W, int H,
   for (int item = threadIdx.x; item < IW * (kSepTH / 8); item += blockDim.x) {
     const int g = item / IW, ix = item - g * IW;
     float acc[8];
-    conv_line8(s_in + (8 * g) * IW + ix, IW, s_taps, L, acc);
+    conv_line8<LC>(s_in + (8 * g) * IW + ix, IW, s_taps, L, acc);
 #pragma unroll
     for (int j = 0; j < 8; j++) s_tmp[(8 * g + j) * IW + ix] = acc[j];
   }
@@ -147,7 +162,7 @@ conv_sep_kernel(const float* __restrict__ in, int W, int H,
   for (int item = threadIdx.x; item < kSepTH * (kSepTW / 8); item += blockDim.x) {
     const int y = item / (kSepTW / 8), g = item - y * (kSepTW / 8);
     float acc[8];
-    conv_line8(s_tmp + y * IW + 8 * g, 1, s_taps, L, acc);
+    conv_line8<LC>(s_tmp + y * IW + 8 * g, 1, s_taps, L, acc);
     const int gy = y0 + y;
     if (gy >= H) continue;
 #pragma unroll
@@ -220,10 +235,12 @@ cageo_status launch_conv(const float* in, int W, int H, int model,
     return CAGEO_ERR_ARGUMENT;
   }
   if (model == CAGEO_FILTER_GAUSSIAN) {
-    CAGEO_CUDA(cudaFuncSetAttribute(conv_sep_kernel<Epi>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // Fully unrolled kernels for the 60 m and 90 m ranges at 10 m cells.
+    auto fn = r == 15 ? conv_sep_kernel<Epi, 31> : r == 23 ? conv_sep_kernel<Epi, 47>
+                                                            : conv_sep_kernel<Epi, 0>;
+    CAGEO_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((W + kSepTW - 1) / kSepTW, (H + kSepTH - 1) / kSepTH);
-    conv_sep_kernel<Epi><<<grid, kSepThreads, smem, s>>>(in, W, H, filt, r, epi);
+    fn<<<grid, kSepThreads, smem, s>>>(in, W, H, filt, r, epi);
   } else {
     CAGEO_CUDA(cudaFuncSetAttribute(conv_2d_kernel<Epi>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
