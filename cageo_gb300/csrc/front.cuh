@@ -29,11 +29,11 @@ struct FrontParams {
   float factor[kMaxBurnClasses + 1];  // factor[0] unused
 };
 
-// Writes one output of the fused front; returns q for the min reduction.
-__device__ inline float front_epilogue(const FrontParams& p, int64_t i,
-                                       float conv) {
-  float v = realistic_value(p.dem[i], conv, p.nodata_dem);
-  uint8_t c = p.code[i];
+// Writes one output of the fused front from the convolved value and the
+// cell's DEM value and static code; returns q for the min reduction.
+__device__ inline float front_epilogue(const FrontParams& p, int64_t i, float conv, float dem,
+                                       uint8_t c) {
+  float v = realistic_value(dem, conv, p.nodata_dem);
   if (c & kCodeBurnStream) {
     // The reference tests a stream neighbour's elevation against NODATA;
     // the precomputed factors assume that test passes.

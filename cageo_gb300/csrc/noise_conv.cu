@@ -53,14 +53,27 @@ __global__ void noise_kernel(float* __restrict__ out, int64_t n, uint32_t k0,
 // ---- A3 separable (Gaussian) ----------------------------------------------
 constexpr int kSepTW = 64, kSepTH = 64, kSepThreads = 256;
 
-__device__ inline int wrap_idx(int v, int n) {
-  v %= n;
-  return v < 0 ? v + n : v;
+// Periodic index: one period either way by compare-and-add (every index a
+// valid output reads is within one period, since r < W and r < H); the
+// modulo only serves padding rows/columns of very small grids.
+__device__ __forceinline__ int wrap_idx(int v, int n) {
+  if (v < 0) v += n;
+  else if (v >= n) v -= n;
+  if ((unsigned)v >= (unsigned)n) {
+    v %= n;
+    if (v < 0) v += n;
+  }
+  return v;
 }
 
+// Epilogues: pre(i) loads what the output at i needs besides the
+// convolved value (issued before the convolution so the loads overlap it);
+// operator() writes the output.
 struct StoreEpilogue {
   float* out;
-  __device__ inline float operator()(int64_t i, float v) const {
+  struct Pre {};
+  __device__ inline Pre pre(int64_t) const { return {}; }
+  __device__ inline float operator()(int64_t i, float v, Pre) const {
     out[i] = v;
     return v;
   }
@@ -68,8 +81,13 @@ struct StoreEpilogue {
 
 struct FrontEpilogue {
   FrontParams p;
-  __device__ inline float operator()(int64_t i, float v) const {
-    return front_epilogue(p, i, v);
+  struct Pre {
+    float dem;
+    uint8_t code;
+  };
+  __device__ inline Pre pre(int64_t i) const { return {p.dem[i], p.code[i]}; }
+  __device__ inline float operator()(int64_t i, float v, Pre pr) const {
+    return front_epilogue(p, i, v, pr.dem, pr.code);
   }
 };
 
@@ -142,10 +160,21 @@ conv_sep_kernel(const float* __restrict__ in, int W, int H,
   float* s_tmp = s_in + IW * IH;
   const int x0 = blockIdx.x * kSepTW, y0 = blockIdx.y * kSepTH;
   for (int t = threadIdx.x; t < L; t += blockDim.x) s_taps[t] = taps[t];
-  for (int idx = threadIdx.x; idx < IW * IH; idx += blockDim.x) {
-    int iy = idx / IW, ix = idx - iy * IW;
-    int gy = wrap_idx(y0 - r + iy, H), gx = wrap_idx(x0 - r + ix, W);
-    s_in[idx] = in[(int64_t)gy * W + gx];
+  {
+    // Row and column of this thread's element, stepped by blockDim.x.
+    int iy = threadIdx.x / IW, ix = threadIdx.x - iy * IW;
+    const int dy = blockDim.x / IW, dx = blockDim.x - dy * IW;
+#pragma unroll 4
+    for (int idx = threadIdx.x; idx < IW * IH; idx += blockDim.x) {
+      const int gy = wrap_idx(y0 - r + iy, H), gx = wrap_idx(x0 - r + ix, W);
+      s_in[idx] = in[(int64_t)gy * W + gx];
+      iy += dy;
+      ix += dx;
+      if (ix >= IW) {
+        ix -= IW;
+        iy++;
+      }
+    }
   }
   __syncthreads();
   // Column pass: tmp[y][ix] = sum_t in[y+t][ix] * taps[t], 8 rows per item.
@@ -161,14 +190,20 @@ conv_sep_kernel(const float* __restrict__ in, int W, int H,
   float local_min = kInf;
   for (int item = threadIdx.x; item < kSepTH * (kSepTW / 8); item += blockDim.x) {
     const int y = item / (kSepTW / 8), g = item - y * (kSepTW / 8);
+    const int gy = y0 + y;
+    typename Epi::Pre pre[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const int gx = x0 + 8 * g + j;
+      if (gy < H && gx < W) pre[j] = epi.pre((int64_t)gy * W + gx);
+    }
     float acc[8];
     conv_line8<LC>(s_tmp + y * IW + 8 * g, 1, s_taps, L, acc);
-    const int gy = y0 + y;
     if (gy >= H) continue;
 #pragma unroll
     for (int j = 0; j < 8; j++) {
       const int gx = x0 + 8 * g + j;
-      if (gx < W) local_min = fminf(local_min, epi((int64_t)gy * W + gx, acc[j]));
+      if (gx < W) local_min = fminf(local_min, epi((int64_t)gy * W + gx, acc[j], pre[j]));
     }
   }
   block_min_out(local_min, epi);
@@ -210,7 +245,10 @@ conv_2d_kernel(const float* __restrict__ in, int W, int H,
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     int gy = y0 + ty + 8 * k, gx = x0 + tx;
-    if (gy < H && gx < W) local_min = fminf(local_min, epi((int64_t)gy * W + gx, sum[k]));
+    if (gy < H && gx < W) {
+      const int64_t i = (int64_t)gy * W + gx;
+      local_min = fminf(local_min, epi(i, sum[k], epi.pre(i)));
+    }
   }
   block_min_out(local_min, epi);
 }
