@@ -51,7 +51,7 @@ __global__ void noise_kernel(float* __restrict__ out, int64_t n, uint32_t k0,
 }
 
 // ---- A3 separable (Gaussian) ----------------------------------------------
-constexpr int kSepTW = 64, kSepTH = 64, kSepThreads = 256;
+constexpr int kSepTW = 64, kSepTH = 32, kSepThreads = 256;
 
 // Periodic index: one period either way by compare-and-add (every index a
 // valid output reads is within one period, since r < W and r < H); the
