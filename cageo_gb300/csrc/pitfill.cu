@@ -65,9 +65,12 @@ enum : int {
   S_KCYC_STORE = 27, // kilo-cycles writing back and queueing
   S_PASS_US_A = 36,  // 24 slots: microseconds of flood A's first passes
   S_PASS_US_B = 68,  // 24 slots: the same for flood B (phases included)
+  S_HEAD = 128,      // work-queue tickets handed out (own 128-byte line)
+  S_TAIL = 160,      // work-queue entries pushed (own line)
+  S_PENDING = 192,   // tiles queued or being processed (own line)
   S_BAR_COUNT = kBarCountSlot,
   S_BAR_GEN = kBarGenSlot,
-  S_SIZE = kScalarSlots
+  S_SIZE = 224
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -77,11 +80,11 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 constexpr int kTile = 32;
+constexpr int kRingSlack = 8192;  // work-ring room for tickets taken ahead of the pushes (> warps)
 constexpr int kWarps = 15;  // one 480-thread block per SM (15 x 14.5 KB smem)
 constexpr int kRS = 35;           // relay row stride (34 used)
 constexpr int kWS = 33;           // W/q row stride
 constexpr int kFS = 36;           // flag row stride (bytes)
-constexpr int kMaxPasses = 1000000;
 
 // Per-warp staged tile: relay values with halo, W and flags of the tile's
 // own cells.  q is static during a flood and is read through the read-only
@@ -95,8 +98,8 @@ struct WarpSmem {
 size_t fill_workspace_bytes(int W, int H) {
   size_t n = (size_t)W * H;
   size_t nt = (size_t)((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile);
-  return align_up(n, 256) + align_up(nt * 4, 256) + align_up(2 * nt * 4, 256) +
-         3 * align_up(nt, 256) + 3 * align_up(n * 4, 256) + 512;
+  return align_up(n, 256) + align_up(nt * 4, 256) + align_up((2 * nt + kRingSlack) * 4, 256) +
+         3 * align_up(nt, 256) + 3 * align_up(n * 4, 256) + 1024;
 }
 
 FillWork fill_carve(void* base, int W, int H) {
@@ -112,7 +115,7 @@ FillWork fill_carve(void* base, int W, int H) {
   w.queued = (int*)p;
   p += align_up(nt * 4, 256);
   w.lists = (int*)p;
-  p += align_up(2 * nt * 4, 256);
+  p += align_up((2 * nt + kRingSlack) * 4, 256);
   w.tdone = (uint8_t*)p;
   p += align_up(nt, 256);
   w.tseed = (uint8_t*)p;
@@ -145,13 +148,74 @@ struct FloodArgs {
   FillWork w;
 };
 
-__device__ __forceinline__ void enqueue(const FillWork& w, int t, int k) {
+// ---- asynchronous tile work queue ---------------------------------------
+// Tiles are processed as soon as they are queued, by whichever warp is free:
+// no grid-wide pass barriers.  The floods are monotone relaxations from
+// above, so the order of the updates does not change their limit; what
+// must not happen is two warps processing one tile at once (a slower
+// warp's write-back could undo a faster one's lower values).  Each tile
+// therefore has a state: 0 idle, 1 queued, 2 processing, 3 processing and
+// queued again meanwhile (re-queued when its processing ends).  `pending`
+// counts tiles in states 1-3; the queue is drained when it reaches 0.  The
+// ring (w.lists, 2 * ntiles slots, -1 = empty) holds each queued tile once.
+constexpr int kEmptySlot = -1;
+
+__device__ __forceinline__ unsigned int ring_cap(const FillWork& w) {
+  return 2u * (unsigned int)(w.tiles_x * w.tiles_y) + kRingSlack;
+}
+
+__device__ __forceinline__ void ring_push(const FillWork& w, int t) {
+  const unsigned int cap = ring_cap(w);
+  const unsigned int pos = atomicAdd(&w.scal[S_TAIL], 1u);
+  atomicExch(&w.lists[pos % cap], t);
+}
+
+__device__ __forceinline__ void enqueue(const FillWork& w, int t) {
   if (((volatile uint8_t*)w.tdone)[t]) return;  // every cell of the tile is final
-  if (atomicMax(&w.queued[t], k) < k) {
-    const unsigned int nt = (unsigned int)(w.tiles_x * w.tiles_y);
-    unsigned int pos = atomicAdd(&w.scal[S_LIST + k % 3], 1u);
-    if (pos < nt) w.lists[(k & 1) * nt + pos] = t;
-    else atomicCAS((int*)(w.scal + S_ERR), 0, 3);  // never: each tile is queued once per pass
+  for (int it = 0; it < 256; it++) {
+    const int st = ((volatile int*)w.queued)[t];
+    if (st == 0) {
+      if (atomicCAS(&w.queued[t], 0, 1) == 0) {
+        atomicAdd(&w.scal[S_PENDING], 1u);
+        ring_push(w, t);
+        return;
+      }
+    } else if (st == 2) {
+      if (atomicCAS(&w.queued[t], 2, 3) == 2) return;
+    } else {
+      return;  // already queued
+    }
+  }
+  atomicCAS((int*)(w.scal + S_ERR), 0, 3);
+}
+
+// Lane 0: take the next queued tile.  A warp takes a ticket (the next ring
+// position) when the ring looks non-empty and keeps it until the slot is
+// filled -- possibly by a later push -- so no claim ever fails.  Returns
+// the tile, or -1 while waiting; *ticket carries the ticket between calls
+// (-1: none).
+__device__ __forceinline__ int try_dequeue(const FillWork& w, long long* ticket) {
+  volatile unsigned int* vs = w.scal;
+  if (*ticket < 0) {
+    if (vs[S_HEAD] >= vs[S_TAIL]) return -1;
+    *ticket = atomicAdd(&w.scal[S_HEAD], 1u);
+  }
+  const int t = atomicExch(&w.lists[(unsigned int)*ticket % ring_cap(w)], kEmptySlot);
+  if (t == kEmptySlot) return -1;
+  *ticket = -1;
+  atomicExch(&w.queued[t], 2);
+  __threadfence();
+  return t;
+}
+
+// Lane 0, after the tile's write-back: idle again, or re-queued if a
+// neighbour queued it while it was being processed.
+__device__ __forceinline__ void finish_tile(const FillWork& w, int t) {
+  if (atomicCAS(&w.queued[t], 2, 0) == 2) {
+    atomicSub(&w.scal[S_PENDING], 1u);
+  } else {
+    atomicExch(&w.queued[t], 1);
+    ring_push(w, t);
   }
 }
 
@@ -200,9 +264,9 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
     uint8_t fv = FNODATA;
     if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
       int64_t i = (int64_t)gy * W + gx;
-      wv = a.Wg[i];
+      wv = __ldcg(a.Wg + i);  // L2: written by other SMs with no barrier in between
       qv = a.q[i];
-      fv = w.flags[i];
+      fv = __ldcg(w.flags + i);
     }
     s.R[hy * kRS + hx] = relay<MODE>(wv, fv, qv);
     if (hx >= 1 && hx <= kTile && hy >= 1 && hy <= kTile) {
@@ -223,7 +287,8 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
   auto smear = [](unsigned int m) { return m | (m << 1) | (m >> 1); };
   // A tile that converged on an earlier visit is a fixpoint for its old halo:
   // only its border rows and columns need evaluating first.
-  const bool revisit = w.tconv[t] != 0;
+  // (written by whichever warp processed the tile last, maybe on another SM)
+  const bool revisit = ((volatile uint8_t*)w.tconv)[t] != 0;
   bool capped = true;
   const int max_rounds = w.max_rounds;
   int rounds = max_rounds;
@@ -291,6 +356,7 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
       if (x == kTile - 1 && y == kTile - 1) sides |= 128;
     }
   }
+  __threadfence();  // the write-back is visible before any neighbour is queued
   sides = __reduce_or_sync(0xffffffffu, sides);
   {
     bool fin = true;
@@ -298,7 +364,6 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
       fin &= (s.F[(idx >> 5) * kFS + (idx & 31)] & (FNODATA | FOUTLET | FBELOW)) != 0;
     if (__all_sync(0xffffffffu, fin) && lane == 0) w.tdone[t] = 1;
   }
-  const int k = p + 1;
   // Lanes 0..8 queue self (if capped) and the 8 neighbours whose halo changed.
   if (lane < 9) {
     int dx = 0, dy = 0;
@@ -316,7 +381,7 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
     }
     int nx = tx + dx, ny = ty + dy;
     if (want && nx >= 0 && ny >= 0 && nx < w.tiles_x && ny < w.tiles_y)
-      enqueue(w, ny * w.tiles_x + nx, k);
+      enqueue(w, ny * w.tiles_x + nx);
   }
   __syncwarp();
   if (lane == 0) {
@@ -351,6 +416,41 @@ __device__ __forceinline__ bool uf_unite(uint32_t* lab, uint32_t a, uint32_t b) 
   return false;
 }
 
+// One warp: process queued tiles until no tile is queued or being processed
+// anywhere.  During a drain only a warp processing a tile can queue one,
+// and that tile keeps `pending` above 0, so pending == 0 means no push can
+// come: a ticket still waiting then is abandoned (head and tail are reset
+// after the drain).  False on an error or a wait limit.
+template <int MODE>
+__device__ bool drain(WarpSmem& s, const FloodArgs& a, int lane, int ntiles) {
+  const FillWork& w = a.w;
+  volatile unsigned int* vs = w.scal;
+  const unsigned int visit_cap = 1000u * (unsigned int)min(ntiles, 4000000);
+  long long ticket = -1;
+  unsigned int ns = 32;
+  for (long long idle = 0;;) {
+    int t = -1;
+    if (lane == 0) t = try_dequeue(w, &ticket);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= 0) {
+      process_tile<MODE>(s, a, t, 0, lane);
+      if (lane == 0) finish_tile(w, t);
+      __syncwarp();
+      idle = 0;
+      ns = 32;
+      continue;
+    }
+    if (vs[S_ERR]) return false;
+    if (vs[S_PENDING] == 0u) return true;
+    if (++idle > (1LL << 24) || vs[MODE == 0 ? S_TILES_A : S_TILES_B] > visit_cap) {
+      if (lane == 0) atomicCAS((int*)(w.scal + S_ERR), 0, 2);
+      return false;
+    }
+    __nanosleep(ns);
+    if (ns < 1024) ns <<= 1;
+  }
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(kWarps * 32, 1)
 fill_flood_kernel(FloodArgs a) {
@@ -366,32 +466,26 @@ fill_flood_kernel(FloodArgs a) {
   volatile unsigned int* vs = w.scal;
   const int p0 = (int)vs[S_PASS] + 2;
   int p = p0;
-  bool full = true, cand_built = false;
+  bool cand_built = false;
   int ph = 0;
   const unsigned long long t_start = global_ns();
   unsigned long long t_conv = 0;
-  while (true) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) vs[S_LIST + (p + 2) % 3] = 0u;
-    int n = full ? ntiles : (int)vs[S_LIST + p % 3];
-    const int* list = w.lists + (p & 1) * ntiles;
-    for (int i = gwarp; i < n; i += nwarps) {
-      // The first pass starts from outlets only: a tile without a relaying
-      // outlet cannot change before a neighbour does, which queues it.
-      if (full && !w.tseed[i]) continue;
-      process_tile<MODE>(s, a, full ? i : list[i], p, lane);
-    }
-    if (!grid_barrier(gs, nblocks)) break;
-    if (blockIdx.x == 0 && threadIdx.x == 0 && p - p0 < 24) {
-      static_assert(S_PASS_US_A + 24 <= kBarGenSlot && S_PASS_US_B + 24 <= kScalarSlots, "slots");
-      const unsigned long long tn = global_ns();
-      vs[(MODE == 0 ? S_PASS_US_A : S_PASS_US_B) + (p - p0)] = (unsigned int)((tn - t_start) / 1000);
-    }
-    if (p - p0 > kMaxPasses) {
-      if (threadIdx.x == 0) atomicCAS((int*)(w.scal + S_ERR), 0, 2);
-      break;
-    }
-    if (vs[S_LIST + (p + 1) % 3] == 0u) {
+  // Seed the queue with the tiles that hold a relaying outlet: a tile
+  // without one cannot change before a neighbour does, which queues it.
+  for (int i = gwarp; i < ntiles; i += nwarps)
+    if (lane == 0 && w.tseed[i]) enqueue(w, i);
+  bool go = grid_barrier(gs, nblocks);
+  while (go) {
+    const bool drained = drain<MODE>(s, a, lane, ntiles);
+    if (!grid_barrier(gs, nblocks) || !drained) break;
+    {
       if (MODE == 0) break;
+      // The queue is empty (abandoned tickets aside): restart its positions.
+      // No push comes before the next grid barrier.
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        vs[S_HEAD] = 0u;
+        vs[S_TAIL] = 0u;
+      }
       // ---- confirmation phases ----
       // Flood A gave a lower bound (W_A in aux, FBELOWA), flood B an upper
       // bound (Wg, FBELOW).  Where they agree the cell is final; the
@@ -497,13 +591,12 @@ fill_flood_kernel(FloodArgs a) {
           int tx0 = max(cx - 1, 0) / kTile, tx1 = min(cx + 1, w.W - 1) / kTile;
           int ty0 = max(cy - 1, 0) / kTile, ty1 = min(cy + 1, w.H - 1) / kTile;
           for (int ty = ty0; ty <= ty1; ty++)
-            for (int tx = tx0; tx <= tx1; tx++) enqueue(w, ty * w.tiles_x + tx, p + 1);
+            for (int tx = tx0; tx <= tx1; tx++) enqueue(w, ty * w.tiles_x + tx);
         }
       }
       ph++;
       if (!grid_barrier(gs, nblocks)) break;
     }
-    full = false;
     p++;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -575,7 +668,11 @@ __global__ void fill_final_exact_kernel(float* __restrict__ Wg, int64_t n) {
 __global__ void fill_classify_kernel(float* __restrict__ Wg, uint8_t* __restrict__ F,
                                      uint32_t* __restrict__ aux, unsigned int* scal, int64_t n) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < 3) scal[S_LIST + i] = 0u;
+  if (i == 0) {
+    scal[S_HEAD] = 0u;
+    scal[S_TAIL] = 0u;
+    scal[S_PENDING] = 0u;
+  }
   if (i >= n) return;
   uint8_t f = F[i];
   const float wa = Wg[i];
@@ -660,6 +757,7 @@ cageo_status fill_run(const float* q, float* filled, const FillWork& w, float no
   FloodArgs a{q, filled, w};
   CAGEO_CUDA(cudaMemsetAsync(w.tdone, 0, nt, s));
   CAGEO_CUDA(cudaMemsetAsync(w.tconv, 0, nt, s));
+  CAGEO_CUDA(cudaMemsetAsync(w.lists, 0xff, (2 * nt + kRingSlack) * sizeof(int), s));  // empty ring
   cageo_status st = launch_flood<0>(a, s);
   if (st) return st;
   fill_classify_kernel<<<blocks, 256, 0, s>>>(filled, w.flags, w.aux, w.scal, n);
@@ -686,6 +784,7 @@ cageo_status fill_run_exact(const float* v, float* filled, const FillWork& w, fl
   CAGEO_CUDA(cudaGetLastError());
   CAGEO_CUDA(cudaMemsetAsync(w.tdone, 0, nt, s));
   CAGEO_CUDA(cudaMemsetAsync(w.tconv, 0, nt, s));
+  CAGEO_CUDA(cudaMemsetAsync(w.lists, 0xff, (2 * nt + kRingSlack) * sizeof(int), s));  // empty ring
   FloodArgs a{v, filled, w};
   cageo_status st = launch_flood<0>(a, s);
   if (st) return st;
