@@ -45,10 +45,10 @@ FALLBACK_HBM = 6800.0
 # Algorithmic bytes per cell of each stage (unfused compulsory I/O).
 STAGE_BYTES = {"noise": 4, "front": 40, "fill": 8, "route": 5, "trace": 6, "border": 12}
 PIPE_BYTES = 75
-# DRAM bytes per cell moved by one pit fill (both flood launches), from the
-# ncu capture summarised in profiles/fill_flood_plain4096.md (4096^2 case,
-# 1702 MB for 16.8 M cells), applied per cell to the benchmark grid.
-FILL_TRAFFIC_PER_CELL = 1702.2e6 / (4096 * 4096)
+# DRAM bytes per cell moved by one pit fill (both flood launches), from an
+# ncu capture of the 4096^2 workload (1678 MB for 16.8 M cells), applied
+# per cell to the benchmark grid.
+FILL_TRAFFIC_PER_CELL = 1678.2e6 / (4096 * 4096)
 # Kernels per realization on the graph path: fill 6 (scalars, init, two
 # floods, classify, final), noise 1, front 1, routing 4 (scalars, d8, flat
 # relaxation, flat directions), tracing 4 (scalars, init, jump,
