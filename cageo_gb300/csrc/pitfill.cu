@@ -27,9 +27,10 @@
 // tile at a time, stages W, q, flags and the relay values of a one-cell
 // halo in shared memory and sweeps it down, up, right and left (Gauss-Seidel)
 // until it stops changing; a tile whose border changed queues the
-// neighbouring tiles for the next pass.  Passes end when no tile is queued.
-// Every grid-wide wait and every loop is bounded; exceeding a bound sets an
-// error flag that the host turns into CAGEO_ERR_NO_CONVERGENCE.
+// neighbouring tiles on an asynchronous work queue (no pass barriers; see
+// the queue below).  A flood ends when no tile is queued or in process.
+// Every wait and every loop is bounded; exceeding a bound sets an error
+// flag that the host turns into CAGEO_ERR_NO_CONVERGENCE.
 #include <algorithm>
 #include "common.cuh"
 #include "pitfill.cuh"
@@ -45,26 +46,25 @@ constexpr uint8_t FNODATA = 0x01, FOUTLET = 0x02, FNONPASS = 0x04, FCONF = 0x08,
 enum : int {
   S_MIN = 0,       // ordered min of q (minE)
   S_ERR = 3,       // 0 ok, 1 barrier wait limit, 2 pass limit
-  S_LIST = 4,      // 3 slots: worklist counts
   S_M = 7,         // 3 slots: ordered phase minima
   S_CAND = 10,     // number of undecided cells
-  S_PASS = 11,     // last pass number
+  S_PASS = 11,     // drains run so far in this fill (a drain empties the work queue)
   S_PHASES = 12,
-  S_PASSES_A = 13, // passes of flood A
-  S_PASSES_B = 14, // passes of flood B before the first phase
+  S_PASSES_A = 13, // drains of flood A (1)
+  S_PASSES_B = 14, // drains of flood B before the first phase (1)
   S_US_A = 15,     // microseconds of flood A
   S_US_B = 16,     // microseconds of flood B up to its first convergence
   S_US_P = 17,     // microseconds of the phase loop
   S_PEND = 18,     // 3 slots: pending cells seen by a phase
-  S_TILES_A = 21,  // tiles processed by flood A
-  S_ROUNDS_A = 22, // sweep rounds run by flood A
-  S_TILES_B = 23,  // tiles processed by flood B (phases included)
-  S_ROUNDS_B = 24, // sweep rounds run by flood B
-  S_KCYC_LOAD = 25,  // kilo-cycles (summed over tile visits) staging tiles
-  S_KCYC_SWEEP = 26, // kilo-cycles sweeping
-  S_KCYC_STORE = 27, // kilo-cycles writing back and queueing
-  S_PASS_US_A = 36,  // 24 slots: microseconds of flood A's first passes
-  S_PASS_US_B = 68,  // 24 slots: the same for flood B (phases included)
+  // Per-visit statistics, updated by every tile visit: a line of their own
+  // (96..127), away from the error flag that idle warps poll.
+  S_TILES_A = 96,   // tiles processed by flood A
+  S_ROUNDS_A = 97,  // sweep rounds run by flood A
+  S_TILES_B = 98,   // tiles processed by flood B (phases included)
+  S_ROUNDS_B = 99,  // sweep rounds run by flood B
+  S_KCYC_LOAD = 100,   // kilo-cycles (summed over tile visits) staging tiles
+  S_KCYC_SWEEP = 101,  // kilo-cycles sweeping
+  S_KCYC_STORE = 102,  // kilo-cycles writing back and queueing
   S_HEAD = 128,      // work-queue tickets handed out (own 128-byte line)
   S_TAIL = 160,      // work-queue entries pushed (own line)
   S_PENDING = 192,   // tiles queued or being processed (own line)
@@ -249,7 +249,7 @@ __device__ __forceinline__ float nbr_min(const WarpSmem& s, int x, int y) {
 }
 
 template <int MODE>
-__device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t, int p,
+__device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t,
                              int lane) {
   const FillWork& w = a.w;
   const int W = w.W, H = w.H;
@@ -433,7 +433,7 @@ __device__ bool drain(WarpSmem& s, const FloodArgs& a, int lane, int ntiles) {
     if (lane == 0) t = try_dequeue(w, &ticket);
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= 0) {
-      process_tile<MODE>(s, a, t, 0, lane);
+      process_tile<MODE>(s, a, t, lane);
       if (lane == 0) finish_tile(w, t);
       __syncwarp();
       idle = 0;

@@ -325,9 +325,9 @@ cudaStream_t cageo_pipeline_stream(cageo_pipeline* p);
  * routing, tracing, border (milliseconds). */
 cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t realization,
                                     float* h_ms, int n);
-/* Counters of the last run: [0] fill passes, [1] confirmation phases,
- * [2] flat-BFS layers, [3] trace jumps, [4] burn re-runs, [5] passes of
- * the lower-bound flood, [6] passes of the walled flood before the first
+/* Counters of the last run: [0] fill work-queue drains, [1] confirmation
+ * phases, [2] flat-BFS passes, [3] trace jumps, [4] burn re-runs, [5] drains
+ * of the lower-bound flood, [6] drains of the walled flood before the first
  * phase, [7..9] microseconds of the lower-bound flood, of the walled flood
  * to convergence and of the phase loop, [10..13] tiles and sweep rounds of
  * the two floods, [14] flat cells, [15] microseconds of the flat BFS,
@@ -338,7 +338,7 @@ cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t realization,
 cageo_status cageo_pipeline_stats(cageo_pipeline* p, int64_t* h_stats, int n);
 /* Autotuner (no counterpart in the reference): times the fill with 4, 8,
  * 16, 32 and 64 sweep rounds per tile visit (a tile that has not converged
- * after that many rounds queues itself for the next pass), `trials`
+ * after that many rounds queues itself again), `trials`
  * realizations each from `first_realization` on, and keeps the fastest.
  * The results do not depend on the choice.  h_best_rounds (may be NULL)
  * receives the choice, h_ms (may be NULL) 5 milliseconds per realization.
