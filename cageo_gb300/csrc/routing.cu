@@ -89,6 +89,17 @@ __global__ void __launch_bounds__(256) d8_kernel(const float* __restrict__ dem,
                                                  int* __restrict__ fd, RouteWork w, float nodata) {
   const int W = w.W, H = w.H;
   const int x = blockIdx.x * kFT + threadIdx.x;
+  // The tile's elevations and a one-cell halo in shared memory.
+  __shared__ float E[34 * 35];
+  {
+    const int x0 = blockIdx.x * kFT - 1, y0 = blockIdx.y * kFT - 1;
+    for (int k = threadIdx.y * 32 + threadIdx.x; k < 34 * 34; k += 256) {
+      const int hy = k / 34, hx = k - hy * 34;
+      const int gx = x0 + hx, gy = y0 + hy;
+      E[hy * 35 + hx] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? dem[(int64_t)gy * W + gx] : 0.0f;
+    }
+  }
+  __syncthreads();
   int nflat = 0;
 #pragma unroll
   for (int k = 0; k < kFT / 8; k++) {
@@ -103,7 +114,8 @@ __global__ void __launch_bounds__(256) d8_kernel(const float* __restrict__ dem,
       fd[i] = -1;
       continue;
     }
-    const float c = dem[i];
+    const float* ec = &E[(threadIdx.y + 8 * k + 1) * 35 + threadIdx.x + 1];
+    const float c = *ec;
     if (c == 0.0f) {
       dir[i] = make_char2(0, 0);
       fd[i] = -2;
@@ -119,7 +131,7 @@ __global__ void __launch_bounds__(256) d8_kernel(const float* __restrict__ dem,
 #pragma unroll
     for (int n = 0; n < 8; n++) {
       const int dx = d8_dx(n), dy = d8_dy(n);
-      const float e = dem[(int64_t)(y + dy) * W + (x + dx)];
+      const float e = ec[dy * 35 + dx];
       if (GPU && e == nodata) continue;
       float sl = __fsub_rn(c, e);
       // A diagonal drop only shrinks when divided by sqrt(2), so the

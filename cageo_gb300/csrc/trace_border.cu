@@ -60,53 +60,74 @@ TraceWork trace_carve(void* base, int W, int H) {
 // in shared memory: each cell ends resolved (a label or a dead end) or
 // pointing at the first cell of its path outside the tile, so the global
 // jumps hop from tile to tile.  One thread per cell, one block per tile.
-__global__ void __launch_bounds__(1024) trace_init_kernel(const char2* __restrict__ dir,
-                                                         const float* __restrict__ streams,
-                                                         int* __restrict__ st, int W, int H) {
+__global__ void __launch_bounds__(256) trace_init_kernel(const char2* __restrict__ dir,
+                                                        const float* __restrict__ streams,
+                                                        int* __restrict__ st, int W, int H) {
   __shared__ int gs[32 * 32];    // state once the path has left the tile (or resolved)
   __shared__ short lt[32 * 32];  // next cell of the path inside the tile, -1 otherwise
-  const int tx = threadIdx.x, ty = threadIdx.y, li = ty * 32 + tx;
-  const int x = blockIdx.x * 32 + tx, y = blockIdx.y * 32 + ty;
-  const bool in = x < W && y < H;
-  int s = kStuckCode, t = -1;
-  if (in) {
-    const int64_t i = (int64_t)y * W + x;
-    const char2 d = dir[i];
-    const int nx = x + d.x, ny = y + d.y;
-    if (streams[i] >= 0.0f) s = label_code(kLake);
-    else if (nx < 0 || nx >= W || ny < 0 || ny >= H) s = label_code(kOutside);
-    else if (d.x == 0 && d.y == 0) s = kStuckCode;
-    else {
-      const int64_t n = (int64_t)ny * W + nx;
-      const float sn = streams[n];
-      if (sn >= 0.0f) {
-        s = label_code((int)(-sn));
-      } else {
-        s = (int)n;
-        const int lx = tx + d.x, ly = ty + d.y;
-        if (lx >= 0 && lx < 32 && ly >= 0 && ly < 32) t = ly * 32 + lx;
+  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+  int s[4], t[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {  // cell li = threadIdx.x + 256 k: row li / 32, column li % 32
+    const int li = threadIdx.x + 256 * k, tx = li & 31, ty = li >> 5;
+    const int x = x0 + tx, y = y0 + ty;
+    s[k] = kStuckCode;
+    t[k] = -1;
+    if (x < W && y < H) {
+      const int64_t i = (int64_t)y * W + x;
+      const char2 d = dir[i];
+      const int nx = x + d.x, ny = y + d.y;
+      if (streams[i] >= 0.0f) s[k] = label_code(kLake);
+      else if (nx < 0 || nx >= W || ny < 0 || ny >= H) s[k] = label_code(kOutside);
+      else if (d.x == 0 && d.y == 0) s[k] = kStuckCode;
+      else {
+        const int64_t n = (int64_t)ny * W + nx;
+        const float sn = streams[n];
+        if (sn >= 0.0f) {
+          s[k] = label_code((int)(-sn));
+        } else {
+          s[k] = (int)n;
+          const int lx = tx + d.x, ly = ty + d.y;
+          if (lx >= 0 && lx < 32 && ly >= 0 && ly < 32) t[k] = ly * 32 + lx;
+        }
       }
     }
+    gs[li] = s[k];
+    lt[li] = (short)t[k];
   }
-  gs[li] = s;
-  lt[li] = (short)t;
   __syncthreads();
   for (int it = 0; it < 10; it++) {  // 2^10 cells: every path inside a tile
-    int ns = s, nt = t;
-    if (t >= 0) {
-      ns = gs[t];
-      nt = lt[t];
+    int ns[4], nt[4];
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      ns[k] = s[k];
+      nt[k] = t[k];
+      if (t[k] >= 0) {
+        ns[k] = gs[t[k]];
+        nt[k] = lt[t[k]];
+      }
     }
     __syncthreads();
-    if (t >= 0) {
-      s = ns;
-      t = nt;
-      gs[li] = s;
-      lt[li] = (short)t;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (t[k] >= 0) {
+        const int li = threadIdx.x + 256 * k;
+        s[k] = ns[k];
+        t[k] = nt[k];
+        gs[li] = s[k];
+        lt[li] = (short)t[k];
+      }
+      any |= t[k] >= 0;
     }
-    if (!__syncthreads_or(t >= 0)) break;
+    if (!__syncthreads_or(any)) break;
   }
-  if (in) st[(int64_t)y * W + x] = s;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int li = threadIdx.x + 256 * k;
+    const int x = x0 + (li & 31), y = y0 + (li >> 5);
+    if (x < W && y < H) st[(int64_t)y * W + x] = s[k];
+  }
 }
 
 // Pointer doubling in place (reading a neighbour's newer state only speeds
@@ -179,7 +200,7 @@ cageo_status trace_run(const int8_t* dir, const float* streams, int* label,
   const int64_t n = (int64_t)w.W * w.H;
   const unsigned blocks = (unsigned)((n + 255) / 256);
   trace_scalars_kernel<<<1, 128, 0, s>>>(w.scal);
-  trace_init_kernel<<<dim3((w.W + 31) / 32, (w.H + 31) / 32), dim3(32, 32), 0, s>>>(
+  trace_init_kernel<<<dim3((w.W + 31) / 32, (w.H + 31) / 32), 256, 0, s>>>(
       (const char2*)dir, streams, w.state, w.W, w.H);
   CAGEO_CUDA(cudaGetLastError());
   static int coop = 0;
