@@ -65,20 +65,6 @@ RouteWork route_carve(void* base, int W, int H) {
   return w;
 }
 
-// Loads the flat-distance code and elevation of the 8 neighbours (N..NW) of
-// cell (x, y) with independent loads; outside the grid: code INT_MIN.
-__device__ __forceinline__ void gather8(const float* __restrict__ dem, const int* __restrict__ fd,
-                                        int W, int H, int x, int y, int* nf, float* ne) {
-#pragma unroll
-  for (int n = 0; n < 8; n++) {
-    const int nx = x + d8_dx(n), ny = y + d8_dy(n);
-    const bool in = nx >= 0 && ny >= 0 && nx < W && ny < H;
-    const int64_t ni = (int64_t)ny * W + nx;
-    nf[n] = in ? ((volatile const int*)fd)[ni] : (int)0x80000000;
-    ne[n] = in ? dem[ni] : 0.0f;
-  }
-}
-
 // Steepest-descent pass.  flatdist: -1 direction, -2 stream, -3 NODATA
 // (GPU order only), kFlatInf flat.  A 32x8 block covers one 32x32 flat
 // tile (4 rows per thread), so the tile's "holds a flat cell" flag and the
@@ -425,21 +411,41 @@ __global__ void __launch_bounds__(256) flat_dir_kernel(const float* __restrict__
   const int W = w.W, H = w.H;
   const int x = blockIdx.x * kFT + threadIdx.x;
   constexpr int order[8] = {0, 6, 2, 4, 7, 1, 5, 3};  // N W E S NW NE SW SE as D8 indices
+  // Codes and elevations of the tile and a one-cell halo (outside: kOffGrid).
+  __shared__ int F[34 * 35];
+  __shared__ float E[34 * 35];
+  {
+    const int x0 = blockIdx.x * kFT - 1, y0 = blockIdx.y * kFT - 1;
+    for (int k = threadIdx.y * 32 + threadIdx.x; k < 34 * 34; k += 256) {
+      const int hy = k / 34, hx = k - hy * 34;
+      const int gx = x0 + hx, gy = y0 + hy;
+      const bool in = gx >= 0 && gx < W && gy >= 0 && gy < H;
+      const int64_t i = (int64_t)gy * W + gx;
+      F[hy * 35 + hx] = in ? fd[i] : kOffGrid;
+      E[hy * 35 + hx] = in ? dem[i] : 0.0f;
+    }
+  }
+  __syncthreads();
 #pragma unroll 1
   for (int k = 0; k < kFT / 8; k++) {
     const int y = blockIdx.y * kFT + threadIdx.y + 8 * k;
     if (x >= W || y >= H) continue;
     const int64_t c = (int64_t)y * W + x;
-    const int d = fd[c];
+    const int b = (threadIdx.y + 8 * k + 1) * 35 + threadIdx.x + 1;
+    const int d = F[b];
     if (d == kFlatInf) {
       fd[c] = 0;
       continue;
     }
     if (d < 1) continue;  // not a flat cell with a layer
-    const float e = dem[c];
+    const float e = E[b];
     int nf[8];
     float ne[8];
-    gather8(dem, fd, W, H, x, y, nf, ne);
+#pragma unroll
+    for (int n = 0; n < 8; n++) {
+      nf[n] = F[b + d8_dy(n) * 35 + d8_dx(n)];
+      ne[n] = E[b + d8_dy(n) * 35 + d8_dx(n)];
+    }
     int got = -1;
     if (GPU) {
 #pragma unroll
