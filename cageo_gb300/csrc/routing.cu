@@ -36,6 +36,7 @@ constexpr int kFlatInf = 0x3fffffff;
 constexpr int kOffGrid = (int)0x80000000;  // staged code of a cell outside the grid
 enum : int { R_NFLAT = 0, R_ERR = 3, R_LIST = 4, R_LAYERS = 7, R_US_BFS = 8, R_PASSES = 9,
              R_TILES = 10, R_KCYC_LOAD = 11, R_KCYC_BFS = 12, R_KCYC_STORE = 13,
+             R_NEXT = 40,  // 3 slots (own line): next list index of a pass
              R_BAR_COUNT = kBarCountSlot, R_BAR_GEN = kBarGenSlot, R_SIZE = kScalarSlots };
 constexpr int kFT = 32;          // flat tile size
 constexpr int kFWarps = 16;      // warps per block of the flat kernel
@@ -360,7 +361,6 @@ flat_relax_kernel(const float* __restrict__ dem, int* fd, RouteWork w, int gpu, 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   FlatSmem& s = reinterpret_cast<FlatSmem*>(smraw)[warp];
   const int ntiles = w.tiles_x * w.tiles_y;
-  const int gwarp = blockIdx.x * kFWarps + warp, nwarps = gridDim.x * kFWarps;
   GridSync gs{w.scal + R_BAR_COUNT, w.scal + R_BAR_GEN, (int*)(w.scal + R_ERR)};
   volatile unsigned int* vs = w.scal;
   unsigned long long t0;
@@ -368,10 +368,18 @@ flat_relax_kernel(const float* __restrict__ dem, int* fd, RouteWork w, int gpu, 
   int p = 2;  // queued[] starts at 0
   bool full = true;
   while (true) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) vs[R_LIST + (p + 2) % 3] = 0u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      vs[R_LIST + (p + 2) % 3] = 0u;
+      vs[R_NEXT + (p + 1) % 3] = 0u;  // used by the next pass, after the barrier
+    }
     const int n = full ? ntiles : (int)vs[R_LIST + p % 3];
     const int* list = w.lists + (p & 1) * ntiles;
-    for (int i = gwarp; i < n; i += nwarps) {
+    // Tiles are handed out one at a time, so warps that finish early take more.
+    for (;;) {
+      int i = 0;
+      if (lane == 0) i = (int)atomicAdd(&w.scal[R_NEXT + p % 3], 1u);
+      i = __shfl_sync(0xffffffffu, i, 0);
+      if (i >= n) break;
       const int t = full ? i : list[i];
       if (full && !w.tflat[t]) continue;
       flat_tile(s, dem, fd, w, t, p, lane, gpu != 0, nodata);
