@@ -733,7 +733,11 @@ static cageo_status launch_flood(const FloodArgs& a, cudaStream_t s) {
   if (!blocks[MODE]) blocks[MODE] = coop_blocks((const void*)fn, smem);
   FloodArgs args = a;
   void* params[] = {&args};
-  CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(blocks[MODE]),
+  // No more blocks than the tiles can keep busy (small grids leave the
+  // rest of the GPU idle instead of polling the work queue).
+  const int ntiles = a.w.tiles_x * a.w.tiles_y;
+  const int grid = std::max(1, std::min(blocks[MODE], (ntiles + kWarps - 1) / kWarps));
+  CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(grid),
                                          dim3(kWarps * 32), params, smem, s));
   return CAGEO_OK;
 }

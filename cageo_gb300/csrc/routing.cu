@@ -505,7 +505,8 @@ cageo_status route_run(const float* filled, int8_t* dir, int* fd, const RouteWor
   int gflag = gpu ? 1 : 0;
   float nd = nodata;
   void* params[] = {(void*)&f, (void*)&fdp, (void*)&wc, (void*)&gflag, (void*)&nd};
-  CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)flat_relax_kernel, dim3(coop),
+  const int fgrid = std::max(1, std::min(coop, (int)((nt + kFWarps - 1) / kFWarps)));
+  CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)flat_relax_kernel, dim3(fgrid),
                                          dim3(kFWarps * 32), params, smem, s));
   if (gpu) flat_dir_kernel<true><<<g, b, 0, s>>>(filled, (char2*)dir, fd, w, nodata);
   else flat_dir_kernel<false><<<g, b, 0, s>>>(filled, (char2*)dir, fd, w, nodata);

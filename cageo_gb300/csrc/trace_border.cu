@@ -214,7 +214,10 @@ cageo_status trace_run(const int8_t* dir, const float* streams, int* label,
   int* stp = w.state;
   TraceWork wc = w;
   void* params[] = {(void*)&stp, (void*)&wc};
-  CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)trace_jump_kernel, dim3(coop),
+  // Each thread takes 4 cells per iteration: no more blocks than that covers.
+  const int64_t need = (n + 4 * kJumpThreads - 1) / (4 * kJumpThreads);
+  const int jgrid = (int)std::max<int64_t>(1, std::min<int64_t>(coop, need));
+  CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)trace_jump_kernel, dim3(jgrid),
                                          dim3(kJumpThreads), params, 0, s));
   trace_final_kernel<<<blocks, 256, 0, s>>>(w.state, label, n,
                                             mode == CAGEO_TRACE_DEAD_END_ERROR ? kError : 0);
