@@ -51,9 +51,9 @@ PIPE_BYTES = 75
 FILL_TRAFFIC_PER_CELL = 1678.2e6 / (4096 * 4096)
 # Kernels per realization on the graph path: fill 6 (scalars, init, two
 # floods, classify, final), noise 1, front 1, routing 4 (scalars, d8, flat
-# relaxation, flat directions), tracing 4 (scalars, init, jump,
-# final), border 1, realization end 1.
-KERNELS_PER_REALIZATION = 18
+# relaxation, flat directions), tracing 3 (scalars, init, jump), border
+# (which also writes the labels) 1, realization end 1.
+KERNELS_PER_REALIZATION = 17
 
 
 def peak_hbm():

@@ -153,9 +153,23 @@ cageo_status enqueue_route(cageo_pipeline* p) {
                    p->cfg.nodata_dem);
 }
 
+int trace_mode(const cageo_pipeline* p) {
+  return exact_mode(p) ? CAGEO_TRACE_DEAD_END_ERROR : CAGEO_TRACE_CPU_COMPAT;
+}
+
+// Tracing with labels (the learned path reads them before the border).
 cageo_status enqueue_trace(cageo_pipeline* p) {
-  return trace_run(p->dir, p->streams, p->label, p->tw, p->stream,
-                   exact_mode(p) ? CAGEO_TRACE_DEAD_END_ERROR : CAGEO_TRACE_CPU_COMPAT);
+  return trace_run(p->dir, p->streams, p->label, p->tw, p->stream, trace_mode(p), true);
+}
+
+// Tracing whose labels are decoded by the border pass (one pass fewer);
+// gate: skip the accumulation when set (null: always accumulate).
+cageo_status enqueue_trace_border(cageo_pipeline* p, const int* gate) {
+  cageo_status st = trace_run(p->dir, p->streams, p->label, p->tw, p->stream, trace_mode(p),
+                              false);
+  if (st) return st;
+  return border_u32_from_state(p->tw.state, p->label, p->counts, p->W, p->H, gate,
+                               trace_mode(p), p->stream);
 }
 
 // Launch sequence of one realization on the fast path.  The realization
@@ -171,9 +185,7 @@ cageo_status enqueue_fast(cageo_pipeline* p) {
     return st;
   if ((st = enqueue_fill(p))) return st;
   if ((st = enqueue_route(p))) return st;
-  if ((st = enqueue_trace(p))) return st;
-  if ((st = border_u32_gated(p->label, p->counts, p->W, p->H, (const int*)p->dscal + 1, s)))
-    return st;
+  if ((st = enqueue_trace_border(p, (const int*)p->dscal + 1))) return st;
   realization_end_kernel<<<1, 32, 0, s>>>(p->dscal, (int*)p->dscal + 1, p->dscal + 3,
                                           p->dscal + 2);
   CAGEO_CUDA(cudaGetLastError());
@@ -250,8 +262,7 @@ cageo_status run_stage_path(cageo_pipeline* p, uint32_t r) {
   if (!exact_mode(p) && (st = fill_quantize_min(p->q, p->fw, c.nodata_dem, s))) return st;
   if ((st = enqueue_fill(p))) return st;
   if ((st = enqueue_route(p))) return st;
-  if ((st = enqueue_trace(p))) return st;
-  if ((st = border_u32(p->label, p->counts, p->W, p->H, s))) return st;
+  if ((st = enqueue_trace_border(p, nullptr))) return st;
   return CAGEO_OK;
 }
 
@@ -465,9 +476,10 @@ extern "C" cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t reali
     cudaEventRecord(ev[3], s);
     if ((st = enqueue_route(p))) break;
     cudaEventRecord(ev[4], s);
-    if ((st = enqueue_trace(p))) break;
-    cudaEventRecord(ev[5], s);
-    if ((st = border_u32_gated(p->label, p->counts, p->W, p->H, (const int*)p->dscal + 1, s)))
+    if ((st = trace_run(p->dir, p->streams, p->label, p->tw, s, trace_mode(p), false))) break;
+    cudaEventRecord(ev[5], s);  // the border stage decodes the labels
+    if ((st = border_u32_from_state(p->tw.state, p->label, p->counts, p->W, p->H,
+                                    (const int*)p->dscal + 1, trace_mode(p), s)))
       break;
     realization_end_kernel<<<1, 32, 0, s>>>(p->dscal, (int*)p->dscal + 1, p->dscal + 3,
                                             p->dscal + 2);

@@ -37,8 +37,9 @@ TraceWork trace_carve(void* base, int W, int H);
 // (int)(-streams[c]).
 // mode CAGEO_TRACE_DEAD_END_ERROR: cells whose path ends without an
 // outlet are ERROR instead of taking cell 0's label.
+// write_labels = false leaves the labels to border_u32_from_state.
 cageo_status trace_run(const int8_t* dir, const float* streams, int* label,
-                       const TraceWork& w, cudaStream_t s, int mode);
+                       const TraceWork& w, cudaStream_t s, int mode, bool write_labels);
 cageo_status trace_check_status(const TraceWork& w, int64_t* jumps);
 
 // count[i] += border(label) for float (stage API) or uint32 (pipeline) counts.
@@ -46,6 +47,10 @@ cageo_status border_float(const int* label, float* count, int W, int H,
                           cudaStream_t s);
 cageo_status border_u32(const int* label, uint32_t* count, int W, int H,
                         cudaStream_t s);
+// From the resolved trace states of a trace_run without labels: writes the
+// labels (mode as for tracing) and adds the border mask unless *gate is set.
+cageo_status border_u32_from_state(const int* state, int* label, uint32_t* count, int W,
+                                   int H, const int* gate, int mode, cudaStream_t s);
 // The same, skipped entirely when *gate (device) is non-zero.
 cageo_status border_u32_gated(const int* label, uint32_t* count, int W, int H,
                               const int* gate, cudaStream_t s);

@@ -175,20 +175,23 @@ __global__ void __launch_bounds__(kJumpThreads, 8) trace_jump_kernel(int* st, Tr
   if (blockIdx.x == 0 && threadIdx.x == 0) vs[T_JUMPS] = (unsigned int)(pass + 1);
 }
 
-// Labels; label-0 terminals take cell 0's label, and so do dead ends
-// (stuck = 0) unless they are reported as ERROR (stuck = kError).
+// Label of a resolved state c (cell 0's state c0): label-0 terminals take
+// cell 0's label, and so do dead ends (stuck = 0) unless they are reported
+// as ERROR (stuck = kError).
+__device__ __forceinline__ int decode_label(int c, int c0, int stuck) {
+  int l = c == kStuckCode ? stuck : c + 1;
+  if (l >= 0) {
+    const int l0 = c0 == kStuckCode ? stuck : c0 + 1;
+    l = l0 >= 0 ? 0 : l0;
+  }
+  return l;
+}
+
 __global__ void trace_final_kernel(const int* __restrict__ st, int* __restrict__ label,
                                    int64_t n, int stuck) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int c = st[i];
-  int l = c == kStuckCode ? stuck : c + 1;
-  if (l >= 0) {
-    const int c0 = st[0];
-    const int l0 = c0 == kStuckCode ? stuck : c0 + 1;
-    l = l0 >= 0 ? 0 : l0;
-  }
-  label[i] = l;
+  label[i] = decode_label(st[i], st[0], stuck);
 }
 
 __global__ void trace_scalars_kernel(unsigned int* s) {
@@ -196,7 +199,7 @@ __global__ void trace_scalars_kernel(unsigned int* s) {
 }
 
 cageo_status trace_run(const int8_t* dir, const float* streams, int* label,
-                       const TraceWork& w, cudaStream_t s, int mode) {
+                       const TraceWork& w, cudaStream_t s, int mode, bool write_labels) {
   const int64_t n = (int64_t)w.W * w.H;
   const unsigned blocks = (unsigned)((n + 255) / 256);
   trace_scalars_kernel<<<1, 128, 0, s>>>(w.scal);
@@ -219,8 +222,9 @@ cageo_status trace_run(const int8_t* dir, const float* streams, int* label,
   const int jgrid = (int)std::max<int64_t>(1, std::min<int64_t>(coop, need));
   CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)trace_jump_kernel, dim3(jgrid),
                                          dim3(kJumpThreads), params, 0, s));
-  trace_final_kernel<<<blocks, 256, 0, s>>>(w.state, label, n,
-                                            mode == CAGEO_TRACE_DEAD_END_ERROR ? kError : 0);
+  if (write_labels)
+    trace_final_kernel<<<blocks, 256, 0, s>>>(w.state, label, n,
+                                              mode == CAGEO_TRACE_DEAD_END_ERROR ? kError : 0);
   CAGEO_CUDA(cudaGetLastError());
   return CAGEO_OK;
 }
@@ -275,6 +279,55 @@ __global__ void __launch_bounds__(256) border_kernel(const int* __restrict__ lab
   }
 }
 
+// The same from the resolved trace states: decodes the labels of the tile
+// and halo (writing the tile's own into `label`), so the labels need no
+// pass of their own.  The labels are written even when `gate` skips the
+// accumulation.
+__global__ void __launch_bounds__(256) border_state_kernel(const int* __restrict__ st,
+                                                           int* __restrict__ label,
+                                                           uint32_t* __restrict__ count, int W,
+                                                           int H, const int* __restrict__ gate,
+                                                           int stuck) {
+  __shared__ int L[34 * 35];
+  const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+  const int c0 = st[0];
+  for (int k = threadIdx.y * 32 + threadIdx.x; k < 34 * 34; k += 256) {
+    const int hy = k / 34, hx = k - hy * 34;
+    const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
+    L[hy * 35 + hx] = (gx >= 0 && gx < W && gy >= 0 && gy < H)
+                          ? decode_label(st[(int64_t)gy * W + gx], c0, stuck)
+                          : kLake;
+  }
+  __syncthreads();
+  const bool skip = gate && *gate;
+  const int tx = threadIdx.x, x = x0 + tx;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int ty = threadIdx.y + 8 * k, y = y0 + ty;
+    if (x >= W || y >= H) continue;
+    const int64_t i = (int64_t)y * W + x;
+    const int* c = &L[(ty + 1) * 35 + tx + 1];
+    label[i] = *c;
+    if (skip || *c == kLake) continue;
+    bool border = false;
+#pragma unroll
+    for (int n = 0; n < 8; n++) {
+      const int v = c[d8_dy(n) * 35 + d8_dx(n)];
+      border |= *c < v && v != kLake;
+    }
+    if (border) count[i] += 1u;
+  }
+}
+
+cageo_status border_u32_from_state(const int* state, int* label, uint32_t* count, int W, int H,
+                                   const int* gate, int mode, cudaStream_t s) {
+  dim3 b(32, 8), g((W + 31) / 32, (H + 31) / 32);
+  border_state_kernel<<<g, b, 0, s>>>(state, label, count, W, H, gate,
+                                      mode == CAGEO_TRACE_DEAD_END_ERROR ? kError : 0);
+  CAGEO_CUDA(cudaGetLastError());
+  return CAGEO_OK;
+}
+
 template <typename T>
 static cageo_status launch_border(const int* label, T* count, int W, int H, const int* gate,
                                   cudaStream_t s) {
@@ -315,7 +368,7 @@ extern "C" cageo_status cageo_trace_mode(const int8_t* d_dir, const float* d_str
   cageo_status st = ws.acquire(d_workspace, workspace_bytes, trace_workspace_bytes(W, H), stream);
   if (st) return st;
   TraceWork w = trace_carve(ws.ptr, W, H);
-  if ((st = trace_run(d_dir, d_streams, d_label, w, stream, mode))) return st;
+  if ((st = trace_run(d_dir, d_streams, d_label, w, stream, mode, true))) return st;
   CAGEO_CUDA(cudaStreamSynchronize(stream));
   return trace_check_status(w, nullptr);
 }
