@@ -40,7 +40,7 @@ namespace cageo {
 
 // Per-cell flag bits.
 constexpr uint8_t FNODATA = 0x01, FOUTLET = 0x02, FNONPASS = 0x04, FCONF = 0x08,
-                  FBELOW = 0x10, FBELOWA = 0x20, FDIRTY = 0x40, FUNSURE = 0x80;
+                  FBELOW = 0x10, FBELOWA = 0x20, FUNSURE = 0x80;
 
 // Scalar block layout (unsigned ints).
 enum : int {
@@ -219,33 +219,47 @@ __device__ __forceinline__ void finish_tile(const FillWork& w, int t) {
   }
 }
 
-// Relax cell (x, y) of the staged tile; returns true if it changed.
-// Update cell (x, y) of the staged tile given m, the least relay among its
-// 8 neighbours; returns true if it changed.  A cell whose incoming level has
-// dropped below its own q (FBELOW) is final in both floods: its value is q
-// and its relay can no longer change.
-template <int MODE>
-__device__ __forceinline__ bool update_cell(WarpSmem& s, int x, int y, float m) {
-  uint8_t f = s.F[y * kFS + x];
-  if (f & (FNODATA | FOUTLET | FBELOW)) return false;
+// Relaxation of staged cell (x, y) given m, the least relay among the
+// neighbours it reads, split into its loads (cell_load) and its update
+// (cell_store, true if the cell changed) so that the two cells of a sweep
+// step are both loaded before either is written.  A cell whose incoming
+// level has dropped below its own q (FBELOW) is final in both floods: its
+// value is q and its relay can no longer change.
+struct CellEval {
+  float w, q, m;
+  uint8_t f;
+};
+
+__device__ __forceinline__ CellEval cell_load(const WarpSmem& s, int x, int y, float m) {
   const float2 wq = s.WQ[y * kWS + x];
-  const float w = wq.x, qv = wq.y;
-  float nw = fminf(w, fmaxf(qv, m));
-  uint8_t nf = f | ((m < qv) ? FBELOW : 0);
-  if (nw != w || nf != f) {
-    s.WQ[y * kWS + x].x = nw;
-    s.F[y * kFS + x] = nf | FDIRTY;
-    s.R[(y + 1) * kRS + (x + 1)] = relay<MODE>(nw, nf, qv);
-    return true;
-  }
-  return false;
+  return CellEval{wq.x, wq.y, m, s.F[y * kFS + x]};
 }
 
-// Least relay among the 8 neighbours of staged cell (x, y).
-__device__ __forceinline__ float nbr_min(const WarpSmem& s, int x, int y) {
-  const float* r = &s.R[(y + 1) * kRS + (x + 1)];
-  return fminf(fminf(fminf(r[-kRS - 1], r[-kRS]), fminf(r[-kRS + 1], r[-1])),
-               fminf(fminf(r[1], r[kRS - 1]), fminf(r[kRS], r[kRS + 1])));
+template <int MODE>
+__device__ __forceinline__ bool cell_store(WarpSmem& s, int x, int y, const CellEval& e) {
+  if (e.f & (FNODATA | FOUTLET | FBELOW)) return false;
+  const float nw = fminf(e.w, fmaxf(e.q, e.m));
+  const uint8_t nf = e.f | ((e.m < e.q) ? FBELOW : 0);
+  if (nw == e.w && nf == e.f) return false;
+  s.WQ[y * kWS + x].x = nw;
+  s.F[y * kFS + x] = nf;
+  s.R[(y + 1) * kRS + (x + 1)] = relay<MODE>(nw, nf, e.q);
+  return true;
+}
+
+// Least relay of the three staged cells in relay row ry (tile row ry - 1),
+// tile columns x-1..x+1: the neighbours of (x, ry - 2) below it or of
+// (x, ry) above it.
+__device__ __forceinline__ float row3_min(const WarpSmem& s, int x, int ry) {
+  const float* r = &s.R[ry * kRS + x];
+  return fminf(fminf(r[0], r[1]), r[2]);
+}
+
+// Least relay of the three staged cells in relay column rx (tile column
+// rx - 1), tile rows y-1..y+1.
+__device__ __forceinline__ float col3_min(const WarpSmem& s, int rx, int y) {
+  const float* r = &s.R[y * kRS + rx];
+  return fminf(fminf(r[0], r[kRS]), r[2 * kRS]);
 }
 
 template <int MODE>
@@ -276,89 +290,105 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t,
   }
   __syncwarp();
   const long long c1 = clock64();
-  // Sweeps.  A cell needs re-evaluating only after one of its 8 neighbours
-  // changed, so each phase carries warp-uniform masks of the rows (vertical
-  // phase) or columns (horizontal phase) to evaluate: all rows first, then
-  // the rows/columns next to a change.  A change also marks its neighbours
-  // for the rest of the current sweep.  Changes of a vertical phase select
-  // the columns of the following horizontal phase (which re-evaluates every
-  // neighbour of those changes) and vice versa, so a horizontal phase
-  // without a change leaves a fixpoint.
-  auto smear = [](unsigned int m) { return m | (m << 1) | (m >> 1); };
+  // Sweeps.  Each of the four directions reads only the three neighbours on
+  // the side it comes from: down (row by row from the top) the row above,
+  // up the row below, right the column to the left, left the column to the
+  // right; a round is a vertical phase (down and up interleaved) and a
+  // horizontal phase (right and left interleaved).  Together the four read
+  // all 8 neighbours.  Warp-uniform masks hold the rows (pd, pu) and
+  // columns (pr, pl) each direction still has to evaluate; a bit is cleared
+  // when its row or column is evaluated.  A change at (x, y) sets the
+  // directions that read it: row y+1 down, y-1 up, column x+1 right, x-1
+  // left.  A bit set for a row or column its sweep has already passed stays
+  // set into the next round.  When all four masks are empty, every cell has
+  // been evaluated against each neighbour since that neighbour last changed:
+  // the tile is at a fixpoint for its halo.
   // A tile that converged on an earlier visit is a fixpoint for its old halo:
-  // only its border rows and columns need evaluating first.
+  // only the rows and columns that read the halo need evaluating first.
   // (written by whichever warp processed the tile last, maybe on another SM)
   const bool revisit = ((volatile uint8_t*)w.tconv)[t] != 0;
-  bool capped = true;
   const int max_rounds = w.max_rounds;
-  int rounds = max_rounds;
-  unsigned int next_rows = revisit ? 0x80000001u : 0xffffffffu;
-  unsigned int first_cols = revisit ? 0x80000001u : 0u;
-  for (int round = 0; round < max_rounds; round++) {
-    unsigned int pend = next_rows, cch = first_cols;
-    first_cols = 0;
+  unsigned int pd = revisit ? 1u : ~0u, pu = revisit ? 0x80000000u : ~0u;
+  unsigned int pr = pd, pl = pu;
+  unsigned int dc = 0;  // this lane's column: rows of the cells changed on this visit
+  int rounds = 0;
+  // A step evaluates both of its rows (columns) when either is pending: the
+  // two cells are loaded before either is stored, so their dependency chains
+  // overlap.  Extra evaluations are harmless (any relaxation step is), and
+  // at the crossing (k = 16) a cell that reads the other's old value is
+  // re-evaluated through the masks like any other.
+  for (; rounds < max_rounds && (pd | pu | pr | pl); rounds++) {
     for (int k = 0; k < kTile; k++) {
       const int d = k, u = kTile - 1 - k;
-      unsigned int b1 = 0, b2 = 0;
-      if ((pend >> d) & 1u) {
-        const float m = nbr_min(s, lane, d);
-        b1 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, lane, d, m));
+      const unsigned int bd = 1u << d, bu = 1u << u;
+      if (!((pd & bd) | (pu & bu))) continue;
+      pd &= ~bd;
+      pu &= ~bu;
+      const CellEval ed = cell_load(s, lane, d, row3_min(s, lane, d));
+      const CellEval eu = cell_load(s, lane, u, row3_min(s, lane, u + 2));
+      const bool cd = cell_store<MODE>(s, lane, d, ed);
+      const bool cu = cell_store<MODE>(s, lane, u, eu);
+      dc |= (cd ? bd : 0u) | (cu ? bu : 0u);
+      const unsigned int b1 = __ballot_sync(0xffffffffu, cd), b2 = __ballot_sync(0xffffffffu, cu);
+      if (b1 | b2) {
+        const unsigned int rows = (b1 ? bd : 0u) | (b2 ? bu : 0u), cols = b1 | b2;
+        pd |= rows << 1;
+        pu |= rows >> 1;
+        pr |= cols << 1;
+        pl |= cols >> 1;
       }
-      if ((pend >> u) & 1u) {
-        const float m = nbr_min(s, lane, u);
-        b2 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, lane, u, m));
-      }
-      if (b1) { cch |= b1; pend |= smear(1u << d); }
-      if (b2) { cch |= b2; pend |= smear(1u << u); }
       __syncwarp();
     }
-    unsigned int pendc = smear(cch) | cch, rch2 = 0;
     for (int k = 0; k < kTile; k++) {
       const int l = k, r = kTile - 1 - k;
-      unsigned int b1 = 0, b2 = 0;
-      if ((pendc >> l) & 1u) {
-        const float m = nbr_min(s, l, lane);
-        b1 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, l, lane, m));
+      const unsigned int bl = 1u << l, br = 1u << r;
+      if (!((pr & bl) | (pl & br))) continue;
+      pr &= ~bl;
+      pl &= ~br;
+      const CellEval el = cell_load(s, l, lane, col3_min(s, l, lane));
+      const CellEval er = cell_load(s, r, lane, col3_min(s, r + 2, lane));
+      const bool cl = cell_store<MODE>(s, l, lane, el);
+      const bool cr = cell_store<MODE>(s, r, lane, er);
+      const unsigned int b1 = __ballot_sync(0xffffffffu, cl), b2 = __ballot_sync(0xffffffffu, cr);
+      if (b1 | b2) {
+        const unsigned int cols = (b1 ? bl : 0u) | (b2 ? br : 0u), rows = b1 | b2;
+        pr |= cols << 1;
+        pl |= cols >> 1;
+        pd |= rows << 1;
+        pu |= rows >> 1;
+        dc |= (lane == l ? b1 : 0u) | (lane == r ? b2 : 0u);
       }
-      if ((pendc >> r) & 1u) {
-        const float m = nbr_min(s, r, lane);
-        b2 = __ballot_sync(0xffffffffu, update_cell<MODE>(s, r, lane, m));
-      }
-      if (b1) { rch2 |= b1; pendc |= smear(1u << l); }
-      if (b2) { rch2 |= b2; pendc |= smear(1u << r); }
       __syncwarp();
     }
-    if (!rch2) { capped = false; rounds = round + 1; break; }
-    next_rows = smear(rch2);
   }
+  const bool capped = (pd | pu | pr | pl) != 0;
   const long long c2 = clock64();
   if (lane == 0) {
     w.tconv[t] = capped ? 0 : 1;
     atomicAdd(&w.scal[MODE == 0 ? S_TILES_A : S_TILES_B], 1u);
     atomicAdd(&w.scal[MODE == 0 ? S_ROUNDS_A : S_ROUNDS_B], (unsigned int)rounds);
   }
-  // Write back changed cells; note which borders changed.
-  unsigned int sides = 0;  // 1 L, 2 R, 4 T, 8 B, 16 TL, 32 TR, 64 BL, 128 BR
-  for (int idx = lane; idx < kTile * kTile; idx += 32) {
-    int y = idx >> 5, x = idx & 31;
-    uint8_t f = s.F[y * kFS + x];
-    if (f & FDIRTY) {
-      int64_t i = (int64_t)(y0 + y) * W + (x0 + x);
-      a.Wg[i] = s.WQ[y * kWS + x].x;
-      w.flags[i] = f & (uint8_t)~FDIRTY;
-      if (x == 0) sides |= 1;
-      if (x == kTile - 1) sides |= 2;
-      if (y == 0) sides |= 4;
-      if (y == kTile - 1) sides |= 8;
-      if (x == 0 && y == 0) sides |= 16;
-      if (x == kTile - 1 && y == 0) sides |= 32;
-      if (x == 0 && y == kTile - 1) sides |= 64;
-      if (x == kTile - 1 && y == kTile - 1) sides |= 128;
+  // Write back the changed cells, row by row (coalesced); note which
+  // borders changed.  Cells outside the grid are NODATA and never change.
+  const unsigned int rows_changed = __reduce_or_sync(0xffffffffu, dc);
+  for (unsigned int rows = rows_changed; rows; rows &= rows - 1) {
+    const int y = __ffs(rows) - 1;
+    if ((dc >> y) & 1u) {
+      const int64_t i = (int64_t)(y0 + y) * W + (x0 + lane);
+      a.Wg[i] = s.WQ[y * kWS + lane].x;
+      w.flags[i] = s.F[y * kFS + lane];
     }
   }
   __threadfence();  // the write-back is visible before any neighbour is queued
-  sides = __reduce_or_sync(0xffffffffu, sides);
-  {
+  const unsigned int dl = __shfl_sync(0xffffffffu, dc, 0), dr = __shfl_sync(0xffffffffu, dc, 31);
+  // 1 L, 2 R, 4 T, 8 B, 16 TL, 32 TR, 64 BL, 128 BR
+  const unsigned int sides = (dl ? 1u : 0u) | (dr ? 2u : 0u) | ((rows_changed & 1u) ? 4u : 0u) |
+                             ((rows_changed >> 31) ? 8u : 0u) | ((dl & 1u) ? 16u : 0u) |
+                             ((dr & 1u) ? 32u : 0u) | ((dl >> 31) ? 64u : 0u) |
+                             ((dr >> 31) ? 128u : 0u);
+  // Every cell final?  Only a change can make it so: a visit that changed
+  // nothing leaves the answer of the visit before.
+  if (rows_changed) {
     bool fin = true;
     for (int idx = lane; idx < kTile * kTile; idx += 32)
       fin &= (s.F[(idx >> 5) * kFS + (idx & 31)] & (FNODATA | FOUTLET | FBELOW)) != 0;
