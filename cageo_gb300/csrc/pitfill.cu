@@ -239,11 +239,13 @@ template <int MODE>
 __device__ __forceinline__ bool cell_store(WarpSmem& s, int x, int y, const CellEval& e) {
   if (e.f & (FNODATA | FOUTLET | FBELOW)) return false;
   const float nw = fminf(e.w, fmaxf(e.q, e.m));
-  const uint8_t nf = e.f | ((e.m < e.q) ? FBELOW : 0);
-  if (nw == e.w && nf == e.f) return false;
+  const bool below = e.m < e.q;  // sets FBELOW, which the cell does not have yet
+  if (nw == e.w && !below) return false;
   s.WQ[y * kWS + x].x = nw;
-  s.F[y * kFS + x] = nf;
-  s.R[(y + 1) * kRS + (x + 1)] = relay<MODE>(nw, nf, e.q);
+  if (below) s.F[y * kFS + x] = e.f | FBELOW;
+  // relay<MODE>() of a cell that is neither NODATA nor an outlet
+  const bool wall = MODE == 1 && (e.f & FNONPASS) && (below || !(e.f & FCONF));
+  s.R[(y + 1) * kRS + (x + 1)] = wall ? kInf : nw;
   return true;
 }
 
@@ -318,6 +320,7 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t,
   // at the crossing (k = 16) a cell that reads the other's old value is
   // re-evaluated through the masks like any other.
   for (; rounds < max_rounds && (pd | pu | pr | pl); rounds++) {
+#pragma unroll 4
     for (int k = 0; k < kTile; k++) {
       const int d = k, u = kTile - 1 - k;
       const unsigned int bd = 1u << d, bu = 1u << u;
@@ -339,6 +342,7 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t,
       }
       __syncwarp();
     }
+#pragma unroll 4
     for (int k = 0; k < kTile; k++) {
       const int l = k, r = kTile - 1 - k;
       const unsigned int bl = 1u << l, br = 1u << r;
