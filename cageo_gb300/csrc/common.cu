@@ -28,6 +28,10 @@ cageo_status Scratch::acquire(void* given, size_t given_bytes, size_t need,
                 given_bytes, need);
       return CAGEO_ERR_ARGUMENT;
     }
+    if ((uintptr_t)given % 256 != 0) {
+      set_error("workspace must start on a 256-byte boundary (as cudaMalloc returns)");
+      return CAGEO_ERR_ARGUMENT;
+    }
     ptr = given;
     owned = false;
     return CAGEO_OK;

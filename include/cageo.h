@@ -19,8 +19,9 @@
  *  - Basin labels are int32: -(int)streams[terminal stream cell],
  *    CAGEO_OUTSIDE or CAGEO_LAKE (src/flowtracing/FlowTracingCommon.h:18-21).
  *  - Stages that need scratch memory take (d_workspace, workspace_bytes);
- *    query the size with the matching *_workspace_size().  Passing NULL lets
- *    the call allocate and free it stream-ordered (cudaMallocAsync).
+ *    query the size with the matching *_workspace_size().  A workspace must
+ *    start on a 256-byte boundary (CAGEO_ERR_ARGUMENT otherwise).  Passing
+ *    NULL lets the call allocate and free it stream-ordered (cudaMallocAsync).
  */
 #ifndef CAGEO_H_
 #define CAGEO_H_

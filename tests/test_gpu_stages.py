@@ -58,6 +58,30 @@ def test_pitfill(cuda, oracle, W, H, seed):
     assert np.array_equal(bits(filled.cpu().numpy()), bits(f_ref)), "filled DEM"
 
 
+def test_pitfill_unaligned_grids(cuda, oracle):
+    """A grid that starts 4 bytes past a 16-byte boundary (a tensor view)
+    fills the same.  A workspace off its 256-byte boundary is refused before
+    any launch."""
+    import torch
+    from cageo_gb300 import api
+    W, H = 512, 96
+    dem, streams = make_case(W, H, seed=5)
+    rdem = oracle.stream_burn(oracle.realistic_dem(dem, gaussian_noise(W, H, 12)), streams)
+    q_ref, f_ref = oracle.pitfill(rdem)
+    buf = torch.empty(W * H + 1, dtype=torch.float32, device=cuda)
+    d = buf[1:].view(H, W)
+    d.copy_(_t(rdem, cuda))
+    assert d.data_ptr() % 16 == 4
+    filled = api.pitfill(d)
+    assert np.array_equal(bits(d.cpu().numpy()), bits(q_ref)), "quantized DEM"
+    assert np.array_equal(bits(filled.cpu().numpy()), bits(f_ref)), "filled DEM"
+    need = api.lib().cageo_pitfill_workspace_size(W, H)
+    ws = torch.empty(need + 256, dtype=torch.uint8, device=cuda)[4:]
+    with pytest.raises(api.CageoError) as e:
+        api.pitfill(_t(rdem, cuda), workspace=ws)
+    assert e.value.status == 1 and "256-byte" in str(e.value)  # CAGEO_ERR_ARGUMENT
+
+
 @pytest.mark.parametrize("realization", range(4))
 def test_pitfill_philox_noise(cuda, oracle, realization):
     """Fill of realistic DEMs made from the library's own Philox noise (the
