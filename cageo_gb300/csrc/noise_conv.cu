@@ -111,6 +111,27 @@ __device__ inline void block_min_out(float local_min, const FrontEpilogue& e) {
   }
 }
 
+// a0 += w0 * t and a1 += w1 * t, each product and each sum rounded to
+// nearest on its own (as __fmul_rn / __fadd_rn, no contraction): the two
+// products as one packed single-precision multiply, the sums as scalar
+// __fadd_rn.  (A packed multiply feeding a packed add is contracted into a
+// fused multiply-add by the assembler, .rn notwithstanding: one rounding
+// fewer, different last bits.  A packed multiply feeding scalar adds, or
+// scalar multiplies feeding a packed add, keep both roundings; both were
+// checked against __fmul_rn + __fadd_rn over 4 M random operand pairs.)
+__device__ __forceinline__ void muladd2_rn(float& a0, float& a1, float w0, float w1, float t) {
+  float p0, p1;
+  asm("{\n\t.reg .b64 wa, tt;\n\t"
+      "mov.b64 wa, {%2, %3};\n\t"
+      "mov.b64 tt, {%4, %4};\n\t"
+      "mul.rn.f32x2 wa, wa, tt;\n\t"
+      "mov.b64 {%0, %1}, wa;\n\t}"
+      : "=f"(p0), "=f"(p1)
+      : "f"(w0), "f"(w1), "f"(t));
+  a0 = __fadd_rn(a0, p0);
+  a1 = __fadd_rn(a1, p1);
+}
+
 // 8 outputs along a line from a sliding window of 8 registers: out[j] =
 // sum_t v[j + t] * taps[t], t ascending, each sum starting at 0.  LC > 0:
 // the tap count is a compile-time constant and the loop is fully unrolled
@@ -130,7 +151,7 @@ __device__ __forceinline__ void conv_line8(const float* __restrict__ v, int stri
     for (int t = 0; t < LC; t++) {
       const float tap = taps[t];
 #pragma unroll
-      for (int j = 0; j < 8; j++) acc[j] = __fadd_rn(acc[j], __fmul_rn(win[j], tap));
+      for (int j = 0; j < 8; j += 2) muladd2_rn(acc[j], acc[j + 1], win[j], win[j + 1], tap);
 #pragma unroll
       for (int j = 0; j < 7; j++) win[j] = win[j + 1];
       if (t + 1 < LC) win[7] = v[(t + 8) * stride];
@@ -140,7 +161,7 @@ __device__ __forceinline__ void conv_line8(const float* __restrict__ v, int stri
     for (int t = 0; t < L; t++) {
       const float tap = taps[t];
 #pragma unroll
-      for (int j = 0; j < 8; j++) acc[j] = __fadd_rn(acc[j], __fmul_rn(win[j], tap));
+      for (int j = 0; j < 8; j += 2) muladd2_rn(acc[j], acc[j + 1], win[j], win[j + 1], tap);
 #pragma unroll
       for (int j = 0; j < 7; j++) win[j] = win[j + 1];
       win[7] = (t + 1 < L) ? v[(t + 8) * stride] : 0.0f;
@@ -236,9 +257,9 @@ conv_2d_kernel(const float* __restrict__ in, int W, int H,
     const float* frow = s_f + fy * L;
     for (int fx = 0; fx < L; fx++) {
       float f = frow[fx];
-#pragma unroll
-      for (int k = 0; k < 4; k++)
-        sum[k] = __fadd_rn(sum[k], __fmul_rn(s_in[(ty + 8 * k + fy) * IW + tx + fx], f));
+      const float* c = s_in + (ty + fy) * IW + tx + fx;
+      muladd2_rn(sum[0], sum[1], c[0], c[8 * IW], f);
+      muladd2_rn(sum[2], sum[3], c[16 * IW], c[24 * IW], f);
     }
   }
   float local_min = kInf;
