@@ -231,7 +231,12 @@ conv_sep_kernel(const float* __restrict__ in, int W, int H,
 }
 
 // ---- A3 full 2D (exponential) -----------------------------------------------
-constexpr int kTwoDT = 32, kTwoDThreads = 256;
+// A block computes a 64 x 32 tile; a thread 8 consecutive outputs of one row
+// from a sliding window of 8 registers, so each tap costs one shared-memory
+// load of input (and a broadcast load of the tap) per 8 outputs.  Each
+// output's sum runs over the filter rows, and inside a row over its taps,
+// in ascending order, as the reference's 2D loop does.
+constexpr int kTwoDTW = 64, kTwoDTH = 32, kTwoDThreads = 256;
 
 template <class Epi>
 __global__ void __launch_bounds__(kTwoDThreads)
@@ -239,36 +244,60 @@ conv_2d_kernel(const float* __restrict__ in, int W, int H,
                const float* __restrict__ filt, int r, Epi epi) {
   extern __shared__ float sm[];
   const int L = 2 * r + 1;
-  const int IW = kTwoDT + 2 * r;
+  const int IW = kTwoDTW + 2 * r, IH = kTwoDTH + 2 * r;
   float* s_f = sm;
   float* s_in = sm + ((L * L + 3) & ~3);
-  const int x0 = blockIdx.x * kTwoDT, y0 = blockIdx.y * kTwoDT;
+  const int x0 = blockIdx.x * kTwoDTW, y0 = blockIdx.y * kTwoDTH;
   for (int t = threadIdx.x; t < L * L; t += blockDim.x) s_f[t] = filt[t];
-  for (int idx = threadIdx.x; idx < IW * IW; idx += blockDim.x) {
-    int iy = idx / IW, ix = idx - iy * IW;
-    int gy = wrap_idx(y0 - r + iy, H), gx = wrap_idx(x0 - r + ix, W);
-    s_in[idx] = in[(int64_t)gy * W + gx];
+  {
+    int iy = threadIdx.x / IW, ix = threadIdx.x - iy * IW;
+    const int dy = blockDim.x / IW, dx = blockDim.x - dy * IW;
+#pragma unroll 4
+    for (int idx = threadIdx.x; idx < IW * IH; idx += blockDim.x) {
+      const int gy = wrap_idx(y0 - r + iy, H), gx = wrap_idx(x0 - r + ix, W);
+      s_in[idx] = in[(int64_t)gy * W + gx];
+      iy += dy;
+      ix += dx;
+      if (ix >= IW) {
+        ix -= IW;
+        iy++;
+      }
+    }
   }
   __syncthreads();
-  // Each thread: column tx, rows ty, ty+8, ty+16, ty+24 (4 independent sums).
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  float sum[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  const int ox = 8 * (threadIdx.x & 7), ty = threadIdx.x >> 3;
+  const int gy = y0 + ty;
+  typename Epi::Pre pre[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    const int gx = x0 + ox + j;
+    if (gy < H && gx < W) pre[j] = epi.pre((int64_t)gy * W + gx);
+  }
+  float acc[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) acc[j] = 0.0f;
   for (int fy = 0; fy < L; fy++) {
+    const float* row = s_in + (ty + fy) * IW + ox;
     const float* frow = s_f + fy * L;
+    float win[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) win[j] = row[j];
+#pragma unroll 8
     for (int fx = 0; fx < L; fx++) {
-      float f = frow[fx];
-      const float* c = s_in + (ty + fy) * IW + tx + fx;
-      muladd2_rn(sum[0], sum[1], c[0], c[8 * IW], f);
-      muladd2_rn(sum[2], sum[3], c[16 * IW], c[24 * IW], f);
+      const float f = frow[fx];
+#pragma unroll
+      for (int j = 0; j < 8; j += 2) muladd2_rn(acc[j], acc[j + 1], win[j], win[j + 1], f);
+#pragma unroll
+      for (int j = 0; j < 7; j++) win[j] = win[j + 1];
+      win[7] = (fx + 1 < L) ? row[fx + 8] : 0.0f;
     }
   }
   float local_min = kInf;
+  if (gy < H) {
 #pragma unroll
-  for (int k = 0; k < 4; k++) {
-    int gy = y0 + ty + 8 * k, gx = x0 + tx;
-    if (gy < H && gx < W) {
-      const int64_t i = (int64_t)gy * W + gx;
-      local_min = fminf(local_min, epi(i, sum[k], epi.pre(i)));
+    for (int j = 0; j < 8; j++) {
+      const int gx = x0 + ox + j;
+      if (gx < W) local_min = fminf(local_min, epi((int64_t)gy * W + gx, acc[j], pre[j]));
     }
   }
   block_min_out(local_min, epi);
@@ -280,8 +309,8 @@ size_t conv_smem_bytes(int model, int r) {
     int IW = kSepTW + 2 * r, IH = kSepTH + 2 * r;
     return sizeof(float) * (((L + 3) & ~3) + (size_t)IW * IH + (size_t)IW * kSepTH);
   }
-  int IW = kTwoDT + 2 * r;
-  return sizeof(float) * (((L * L + 3) & ~3) + (size_t)IW * IW);
+  int IW = kTwoDTW + 2 * r, IH = kTwoDTH + 2 * r;
+  return sizeof(float) * (((L * L + 3) & ~3) + (size_t)IW * IH);
 }
 
 template <class Epi>
@@ -303,7 +332,7 @@ cageo_status launch_conv(const float* in, int W, int H, int model,
   } else {
     CAGEO_CUDA(cudaFuncSetAttribute(conv_2d_kernel<Epi>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 grid((W + kTwoDT - 1) / kTwoDT, (H + kTwoDT - 1) / kTwoDT);
+    dim3 grid((W + kTwoDTW - 1) / kTwoDTW, (H + kTwoDTH - 1) / kTwoDTH);
     conv_2d_kernel<Epi><<<grid, kTwoDThreads, smem, s>>>(in, W, H, filt, r, epi);
   }
   CAGEO_CUDA(cudaGetLastError());
