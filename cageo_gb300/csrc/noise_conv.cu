@@ -188,7 +188,7 @@ conv_sep_kernel(const float* __restrict__ in, int W, int H,
 #pragma unroll 4
     for (int idx = threadIdx.x; idx < IW * IH; idx += blockDim.x) {
       const int gy = wrap_idx(y0 - r + iy, H), gx = wrap_idx(x0 - r + ix, W);
-      s_in[idx] = in[(int64_t)gy * W + gx];
+      cp_async4(&s_in[idx], &in[(int64_t)gy * W + gx]);  // all of them in flight at once
       iy += dy;
       ix += dx;
       if (ix >= IW) {
@@ -196,6 +196,7 @@ conv_sep_kernel(const float* __restrict__ in, int W, int H,
         iy++;
       }
     }
+    cp_async_wait();
   }
   __syncthreads();
   // Column pass: tmp[y][ix] = sum_t in[y+t][ix] * taps[t], 8 rows per item.
@@ -255,7 +256,7 @@ conv_2d_kernel(const float* __restrict__ in, int W, int H,
 #pragma unroll 4
     for (int idx = threadIdx.x; idx < IW * IH; idx += blockDim.x) {
       const int gy = wrap_idx(y0 - r + iy, H), gx = wrap_idx(x0 - r + ix, W);
-      s_in[idx] = in[(int64_t)gy * W + gx];
+      cp_async4(&s_in[idx], &in[(int64_t)gy * W + gx]);  // all of them in flight at once
       iy += dy;
       ix += dx;
       if (ix >= IW) {
@@ -263,6 +264,7 @@ conv_2d_kernel(const float* __restrict__ in, int W, int H,
         iy++;
       }
     }
+    cp_async_wait();
   }
   __syncthreads();
   const int ox = 8 * (threadIdx.x & 7), ty = threadIdx.x >> 3;
