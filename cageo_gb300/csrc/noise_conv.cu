@@ -319,21 +319,44 @@ template <class Epi>
 cageo_status launch_conv(const float* in, int W, int H, int model,
                          const float* filt, int r, const Epi& epi,
                          cudaStream_t s) {
-  size_t smem = conv_smem_bytes(model, r);
-  if (smem > 227 * 1024) {
-    set_error("filter radius %d needs %zu bytes of shared memory", r, smem);
-    return CAGEO_ERR_ARGUMENT;
-  }
+  // The kernels' dynamic shared-memory limit is raised to the most the
+  // device allows (its opt-in maximum less the kernel's static shared
+  // memory), the same value on every call: pipelines on other host threads
+  // launch the same kernels with other radii, and a per-call limit set by
+  // one thread could fall below another thread's launch between its set
+  // and launch.  (Occupancy follows each launch's own size, not the limit.)
+  int optin = 0, dev = 0;
+  CAGEO_CUDA(cudaGetDevice(&dev));
+  CAGEO_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  auto raise_limit = [&](const void* fn, int* limit) -> cageo_status {
+    cudaFuncAttributes fa;
+    CAGEO_CUDA(cudaFuncGetAttributes(&fa, fn));
+    *limit = optin - (int)fa.sharedSizeBytes;
+    CAGEO_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, *limit));
+    return CAGEO_OK;
+  };
+  const size_t smem = conv_smem_bytes(model, r);
   if (model == CAGEO_FILTER_GAUSSIAN) {
     // Fully unrolled kernels for the 60 m and 90 m ranges at 10 m cells.
     auto fn = r == 15 ? conv_sep_kernel<Epi, 31> : r == 23 ? conv_sep_kernel<Epi, 47>
                                                             : conv_sep_kernel<Epi, 0>;
-    CAGEO_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int limit = 0;
+    cageo_status st = raise_limit((const void*)fn, &limit);
+    if (st) return st;
+    if (smem > (size_t)limit) {
+      set_error("filter radius %d needs %zu bytes of shared memory (%d available)", r, smem, limit);
+      return CAGEO_ERR_ARGUMENT;
+    }
     dim3 grid((W + kSepTW - 1) / kSepTW, (H + kSepTH - 1) / kSepTH);
     fn<<<grid, kSepThreads, smem, s>>>(in, W, H, filt, r, epi);
   } else {
-    CAGEO_CUDA(cudaFuncSetAttribute(conv_2d_kernel<Epi>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int limit = 0;
+    cageo_status st = raise_limit((const void*)conv_2d_kernel<Epi>, &limit);
+    if (st) return st;
+    if (smem > (size_t)limit) {
+      set_error("filter radius %d needs %zu bytes of shared memory (%d available)", r, smem, limit);
+      return CAGEO_ERR_ARGUMENT;
+    }
     dim3 grid((W + kTwoDTW - 1) / kTwoDTW, (H + kTwoDTH - 1) / kTwoDTH);
     conv_2d_kernel<Epi><<<grid, kTwoDThreads, smem, s>>>(in, W, H, filt, r, epi);
   }

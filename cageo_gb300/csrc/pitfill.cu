@@ -652,10 +652,11 @@ __global__ void fill_init_kernel(const float* __restrict__ q, float* __restrict_
                                  uint8_t* __restrict__ F, const unsigned int* minslot,
                                  uint8_t* __restrict__ tseed, int tiles_x, int W, int H,
                                  float nodata) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (int64_t)W * H) return;
+  // One block row per grid row: no division to find the cell's x and y.
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if (x >= W) return;
+  const int64_t i = (int64_t)y * W + x;
   const float minE = ordered_to_float(*minslot);
-  int x = (int)(i % W), y = (int)(i / W);
   float qv = q[i];
   uint8_t f = 0;
   if (qv == nodata) {
@@ -677,9 +678,9 @@ __global__ void fill_init_exact_kernel(const float* __restrict__ v, float* __res
                                        uint8_t* __restrict__ F, const float* __restrict__ warm,
                                        uint8_t* __restrict__ tseed, int tiles_x, int W, int H,
                                        float nodata) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (int64_t)W * H) return;
-  int x = (int)(i % W), y = (int)(i / W);
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if (x >= W) return;
+  const int64_t i = (int64_t)y * W + x;
   const float e = v[i];
   uint8_t f = 0;
   if (e == nodata) f = FNODATA;
@@ -789,8 +790,9 @@ cageo_status fill_run(const float* q, float* filled, const FillWork& w, float no
   const unsigned blocks = (unsigned)((n + 255) / 256);
   const size_t nt = (size_t)w.tiles_x * w.tiles_y;
   CAGEO_CUDA(cudaMemsetAsync(w.tseed, 0, nt, s));
-  fill_init_kernel<<<blocks, 256, 0, s>>>(q, filled, w.flags, w.scal + S_MIN, w.tseed,
-                                          w.tiles_x, w.W, w.H, nodata);
+  const dim3 rows((unsigned)((w.W + 255) / 256), (unsigned)w.H);
+  fill_init_kernel<<<rows, 256, 0, s>>>(q, filled, w.flags, w.scal + S_MIN, w.tseed, w.tiles_x,
+                                        w.W, w.H, nodata);
   CAGEO_CUDA(cudaGetLastError());
   FloodArgs a{q, filled, w};
   CAGEO_CUDA(cudaMemsetAsync(w.tdone, 0, nt, s));
@@ -817,8 +819,9 @@ cageo_status fill_run_exact(const float* v, float* filled, const FillWork& w, fl
   // A warm start may hold values above the answer anywhere: every tile is
   // visited on the first pass.
   CAGEO_CUDA(cudaMemsetAsync(w.tseed, warm ? 1 : 0, nt, s));
-  fill_init_exact_kernel<<<blocks, 256, 0, s>>>(v, filled, w.flags, warm, w.tseed, w.tiles_x,
-                                                w.W, w.H, nodata);
+  const dim3 rows((unsigned)((w.W + 255) / 256), (unsigned)w.H);
+  fill_init_exact_kernel<<<rows, 256, 0, s>>>(v, filled, w.flags, warm, w.tseed, w.tiles_x, w.W,
+                                              w.H, nodata);
   CAGEO_CUDA(cudaGetLastError());
   CAGEO_CUDA(cudaMemsetAsync(w.tdone, 0, nt, s));
   CAGEO_CUDA(cudaMemsetAsync(w.tconv, 0, nt, s));

@@ -80,11 +80,16 @@ __global__ void __launch_bounds__(256) d8_kernel(const float* __restrict__ dem,
   __shared__ float E[34 * 35];
   {
     const int x0 = blockIdx.x * kFT - 1, y0 = blockIdx.y * kFT - 1;
+#pragma unroll
     for (int k = threadIdx.y * 32 + threadIdx.x; k < 34 * 34; k += 256) {
       const int hy = k / 34, hx = k - hy * 34;
       const int gx = x0 + hx, gy = y0 + hy;
-      E[hy * 35 + hx] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? dem[(int64_t)gy * W + gx] : 0.0f;
+      if (gx >= 0 && gx < W && gy >= 0 && gy < H)
+        cp_async4(&E[hy * 35 + hx], dem + (int64_t)gy * W + gx);  // all in flight at once
+      else
+        E[hy * 35 + hx] = 0.0f;
     }
+    cp_async_wait();
   }
   __syncthreads();
   int nflat = 0;
@@ -424,14 +429,20 @@ __global__ void __launch_bounds__(256) flat_dir_kernel(const float* __restrict__
   __shared__ float E[34 * 35];
   {
     const int x0 = blockIdx.x * kFT - 1, y0 = blockIdx.y * kFT - 1;
+#pragma unroll
     for (int k = threadIdx.y * 32 + threadIdx.x; k < 34 * 34; k += 256) {
       const int hy = k / 34, hx = k - hy * 34;
       const int gx = x0 + hx, gy = y0 + hy;
-      const bool in = gx >= 0 && gx < W && gy >= 0 && gy < H;
-      const int64_t i = (int64_t)gy * W + gx;
-      F[hy * 35 + hx] = in ? fd[i] : kOffGrid;
-      E[hy * 35 + hx] = in ? dem[i] : 0.0f;
+      if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+        const int64_t i = (int64_t)gy * W + gx;
+        cp_async4(&F[hy * 35 + hx], fd + i);  // all in flight at once
+        cp_async4(&E[hy * 35 + hx], dem + i);
+      } else {
+        F[hy * 35 + hx] = kOffGrid;
+        E[hy * 35 + hx] = 0.0f;
+      }
     }
+    cp_async_wait();
   }
   __syncthreads();
 #pragma unroll 1
