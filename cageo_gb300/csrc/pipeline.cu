@@ -168,7 +168,7 @@ cageo_status enqueue_trace_border(cageo_pipeline* p, const int* gate) {
   cageo_status st = trace_run(p->dir, p->streams, p->label, p->tw, p->stream, trace_mode(p),
                               false);
   if (st) return st;
-  return border_u32_from_state(p->tw.state, p->label, p->counts, p->W, p->H, gate,
+  return border_u32_from_state(p->tw, p->label, p->counts, gate,
                                trace_mode(p), p->stream);
 }
 
@@ -478,7 +478,7 @@ extern "C" cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t reali
     cudaEventRecord(ev[4], s);
     if ((st = trace_run(p->dir, p->streams, p->label, p->tw, s, trace_mode(p), false))) break;
     cudaEventRecord(ev[5], s);  // the border stage decodes the labels
-    if ((st = border_u32_from_state(p->tw.state, p->label, p->counts, p->W, p->H,
+    if ((st = border_u32_from_state(p->tw, p->label, p->counts,
                                     (const int*)p->dscal + 1, trace_mode(p), s)))
       break;
     realization_end_kernel<<<1, 32, 0, s>>>(p->dscal, (int*)p->dscal + 1, p->dscal + 3,

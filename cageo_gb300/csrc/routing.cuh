@@ -27,8 +27,9 @@ cageo_status route_run(const float* filled, int8_t* dir, int* flatdist,
 cageo_status route_check_status(const RouteWork& w, int64_t* stats);
 
 struct TraceWork {
-  int W = 0, H = 0;
-  int* state = nullptr;          // W*H: packed pointer / label
+  int W = 0, H = 0, tiles_x = 0, tiles_y = 0;
+  int* state = nullptr;          // W*H: label, or the tile-border cell the path leaves by
+  int* bstate = nullptr;         // 124 per 32x32 tile: the same for the tiles' border cells
   unsigned int* scal = nullptr;
 };
 size_t trace_workspace_bytes(int W, int H);
@@ -47,10 +48,10 @@ cageo_status border_float(const int* label, float* count, int W, int H,
                           cudaStream_t s);
 cageo_status border_u32(const int* label, uint32_t* count, int W, int H,
                         cudaStream_t s);
-// From the resolved trace states of a trace_run without labels: writes the
-// labels (mode as for tracing) and adds the border mask unless *gate is set.
-cageo_status border_u32_from_state(const int* state, int* label, uint32_t* count, int W,
-                                   int H, const int* gate, int mode, cudaStream_t s);
+// From the trace states of a trace_run without labels: writes the labels
+// (mode as for tracing) and adds the border mask unless *gate is set.
+cageo_status border_u32_from_state(const TraceWork& w, int* label, uint32_t* count,
+                                   const int* gate, int mode, cudaStream_t s);
 // The same, skipped entirely when *gate (device) is non-zero.
 cageo_status border_u32_gated(const int* label, uint32_t* count, int W, int H,
                               const int* gate, cudaStream_t s);

@@ -7,8 +7,13 @@
 // (int)(-streams[s])).  The reference walks each path serially with caching;
 // the label of a cell depends only on where its path ends, so here every
 // cell holds a packed 32-bit state -- "points to cell p" or "resolved to
-// label l" -- and repeatedly jumps p <- state[p] (pointer doubling) until
-// all are resolved: O(log path length) grid passes.  A cell without a direction
+// label l".  Paths are first followed inside each 32x32 tile; a path that
+// leaves its tile then points at the border cell of the next tile it
+// enters, and those border cells (124 per tile, kept in a compact array)
+// point only at border cells of other tiles.  Pointer doubling
+// (p <- state[p]) over the compact array resolves them in O(log path
+// length) passes over 12% of the cells; every other cell then needs one
+// lookup.  A cell without a direction
 // (0,0) is a dead end: the reference's walk never terminates there, leaves
 // the path at 0 and its connect pass then copies the label of cell 0; such
 // cells and label-0 terminals take the label of cell 0 here too (or, in the
@@ -39,21 +44,38 @@ enum : int { T_ERR = 2, T_ACTIVE = 3, T_JUMPS = 6, T_BAR_COUNT = kBarCountSlot,
 
 __device__ __forceinline__ int label_code(int label) { return label - 1; }
 
+constexpr int kBorderCells = 124;  // cells on the rim of a 32x32 tile
+
 size_t trace_workspace_bytes(int W, int H) {
   const size_t n = (size_t)W * H;
-  return align_up(n * 4, 256) + 512;
+  const size_t nt = (size_t)((W + 31) / 32) * ((H + 31) / 32);
+  return align_up(n * 4, 256) + align_up(nt * kBorderCells * 4, 256) + 512;
 }
 
 TraceWork trace_carve(void* base, int W, int H) {
   TraceWork w;
   w.W = W;
   w.H = H;
+  w.tiles_x = (W + 31) / 32;
+  w.tiles_y = (H + 31) / 32;
   const size_t n = (size_t)W * H;
+  const size_t nt = (size_t)w.tiles_x * w.tiles_y;
   char* p = (char*)base;
   w.state = (int*)p;
   p += align_up(n * 4, 256);
+  w.bstate = (int*)p;
+  p += align_up(nt * kBorderCells * 4, 256);
   w.scal = (unsigned int*)p;
   return w;
+}
+
+// Compact index of cell (x, y) on the rim of its 32x32 tile (x % 32 or
+// y % 32 is 0 or 31): top row 0..31, bottom row 32..63, left column rows
+// 1..30 at 64..93, right column rows 1..30 at 94..123.
+__device__ __forceinline__ int border_index(int x, int y, int tiles_x) {
+  const int lx = x & 31, ly = y & 31;
+  const int b = ly == 0 ? lx : ly == 31 ? 32 + lx : lx == 0 ? 63 + ly : 93 + ly;
+  return ((y >> 5) * tiles_x + (x >> 5)) * kBorderCells + b;
 }
 
 // Initial state of every cell, then pointer jumping inside its 32x32 tile
@@ -62,7 +84,9 @@ TraceWork trace_carve(void* base, int W, int H) {
 // jumps hop from tile to tile.  One thread per cell, one block per tile.
 __global__ void __launch_bounds__(256) trace_init_kernel(const char2* __restrict__ dir,
                                                         const float* __restrict__ streams,
-                                                        int* __restrict__ st, int W, int H) {
+                                                        int* __restrict__ st,
+                                                        int* __restrict__ bst, int W, int H,
+                                                        unsigned int* scal) {
   __shared__ int gs[32 * 32];    // state once the path has left the tile (or resolved)
   __shared__ short lt[32 * 32];  // next cell of the path inside the tile, -1 otherwise
   const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
@@ -86,9 +110,13 @@ __global__ void __launch_bounds__(256) trace_init_kernel(const char2* __restrict
         if (sn >= 0.0f) {
           s[k] = label_code((int)(-sn));
         } else {
-          s[k] = (int)n;
           const int lx = tx + d.x, ly = ty + d.y;
-          if (lx >= 0 && lx < 32 && ly >= 0 && ly < 32) t[k] = ly * 32 + lx;
+          if (lx >= 0 && lx < 32 && ly >= 0 && ly < 32) {
+            t[k] = ly * 32 + lx;  // inside the tile: followed below
+            s[k] = 0;
+          } else {
+            s[k] = border_index(nx, ny, gridDim.x);  // on the rim of the next tile
+          }
         }
       }
     }
@@ -122,19 +150,29 @@ __global__ void __launch_bounds__(256) trace_init_kernel(const char2* __restrict
     }
     if (!__syncthreads_or(any)) break;
   }
+  // A path of a 32x32 tile has at most 1024 cells: one still inside after
+  // 2^10 hops is on a cycle, which never resolves (reported as an error).
 #pragma unroll
   for (int k = 0; k < 4; k++) {
-    const int li = threadIdx.x + 256 * k;
-    const int x = x0 + (li & 31), y = y0 + (li >> 5);
+    if (t[k] >= 0) {
+      s[k] = kStuckCode;
+      atomicCAS((int*)(scal + T_ERR), 0, 2);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int li = threadIdx.x + 256 * k, lx = li & 31, ly = li >> 5;
+    const int x = x0 + lx, y = y0 + ly;
     if (x < W && y < H) st[(int64_t)y * W + x] = s[k];
+    if (lx == 0 || lx == 31 || ly == 0 || ly == 31) bst[border_index(x, y, gridDim.x)] = s[k];
   }
 }
 
-// Pointer doubling in place (reading a neighbour's newer state only speeds
-// convergence).  Each thread takes 4 cells per iteration so their dependent
+// Pointer doubling in place over the tiles' border cells (reading a
+// neighbour's newer state only speeds convergence).  Each thread takes 4 cells per iteration so their dependent
 // load pairs overlap.  Persistent; one bounded grid barrier per pass.
 __global__ void __launch_bounds__(kJumpThreads, 8) trace_jump_kernel(int* st, TraceWork w) {
-  const int64_t N = (int64_t)w.W * w.H;
+  const int64_t N = (int64_t)w.tiles_x * w.tiles_y * kBorderCells;
   GridSync gs{w.scal + T_BAR_COUNT, w.scal + T_BAR_GEN, (int*)(w.scal + T_ERR)};
   volatile unsigned int* vs = w.scal;
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
@@ -187,11 +225,17 @@ __device__ __forceinline__ int decode_label(int c, int c0, int stuck) {
   return l;
 }
 
-__global__ void trace_final_kernel(const int* __restrict__ st, int* __restrict__ label,
-                                   int64_t n, int stuck) {
+// Resolved state of a cell from its own state: a path that left the cell's
+// tile takes the (resolved) state of the border cell it entered next.
+__device__ __forceinline__ int resolve(int c, const int* __restrict__ bst) {
+  return c >= 0 ? bst[c] : c;
+}
+
+__global__ void trace_final_kernel(const int* __restrict__ st, const int* __restrict__ bst,
+                                   int* __restrict__ label, int64_t n, int stuck) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  label[i] = decode_label(st[i], st[0], stuck);
+  label[i] = decode_label(resolve(st[i], bst), resolve(st[0], bst), stuck);
 }
 
 __global__ void trace_scalars_kernel(unsigned int* s) {
@@ -203,8 +247,8 @@ cageo_status trace_run(const int8_t* dir, const float* streams, int* label,
   const int64_t n = (int64_t)w.W * w.H;
   const unsigned blocks = (unsigned)((n + 255) / 256);
   trace_scalars_kernel<<<1, 128, 0, s>>>(w.scal);
-  trace_init_kernel<<<dim3((w.W + 31) / 32, (w.H + 31) / 32), 256, 0, s>>>(
-      (const char2*)dir, streams, w.state, w.W, w.H);
+  trace_init_kernel<<<dim3(w.tiles_x, w.tiles_y), 256, 0, s>>>(
+      (const char2*)dir, streams, w.state, w.bstate, w.W, w.H, w.scal);
   CAGEO_CUDA(cudaGetLastError());
   static int coop = 0;
   if (!coop) {
@@ -214,16 +258,18 @@ cageo_status trace_run(const int8_t* dir, const float* streams, int* label,
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trace_jump_kernel, kJumpThreads, 0);
     coop = std::max(1, per) * sms;
   }
-  int* stp = w.state;
+  int* stp = w.bstate;
   TraceWork wc = w;
   void* params[] = {(void*)&stp, (void*)&wc};
-  // Each thread takes 4 cells per iteration: no more blocks than that covers.
-  const int64_t need = (n + 4 * kJumpThreads - 1) / (4 * kJumpThreads);
+  // Each thread takes 4 border cells per iteration: no more blocks than
+  // that covers.
+  const int64_t nb = (int64_t)w.tiles_x * w.tiles_y * kBorderCells;
+  const int64_t need = (nb + 4 * kJumpThreads - 1) / (4 * kJumpThreads);
   const int jgrid = (int)std::max<int64_t>(1, std::min<int64_t>(coop, need));
   CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)trace_jump_kernel, dim3(jgrid),
                                          dim3(kJumpThreads), params, 0, s));
   if (write_labels)
-    trace_final_kernel<<<blocks, 256, 0, s>>>(w.state, label, n,
+    trace_final_kernel<<<blocks, 256, 0, s>>>(w.state, w.bstate, label, n,
                                               mode == CAGEO_TRACE_DEAD_END_ERROR ? kError : 0);
   CAGEO_CUDA(cudaGetLastError());
   return CAGEO_OK;
@@ -284,18 +330,19 @@ __global__ void __launch_bounds__(256) border_kernel(const int* __restrict__ lab
 // pass of their own.  The labels are written even when `gate` skips the
 // accumulation.
 __global__ void __launch_bounds__(256) border_state_kernel(const int* __restrict__ st,
+                                                           const int* __restrict__ bst,
                                                            int* __restrict__ label,
                                                            uint32_t* __restrict__ count, int W,
                                                            int H, const int* __restrict__ gate,
                                                            int stuck) {
   __shared__ int L[34 * 35];
   const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
-  const int c0 = st[0];
+  const int c0 = resolve(st[0], bst);
   for (int k = threadIdx.y * 32 + threadIdx.x; k < 34 * 34; k += 256) {
     const int hy = k / 34, hx = k - hy * 34;
     const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
     L[hy * 35 + hx] = (gx >= 0 && gx < W && gy >= 0 && gy < H)
-                          ? decode_label(st[(int64_t)gy * W + gx], c0, stuck)
+                          ? decode_label(resolve(st[(int64_t)gy * W + gx], bst), c0, stuck)
                           : kLake;
   }
   __syncthreads();
@@ -319,10 +366,10 @@ __global__ void __launch_bounds__(256) border_state_kernel(const int* __restrict
   }
 }
 
-cageo_status border_u32_from_state(const int* state, int* label, uint32_t* count, int W, int H,
+cageo_status border_u32_from_state(const TraceWork& w, int* label, uint32_t* count,
                                    const int* gate, int mode, cudaStream_t s) {
-  dim3 b(32, 8), g((W + 31) / 32, (H + 31) / 32);
-  border_state_kernel<<<g, b, 0, s>>>(state, label, count, W, H, gate,
+  dim3 b(32, 8), g(w.tiles_x, w.tiles_y);
+  border_state_kernel<<<g, b, 0, s>>>(w.state, w.bstate, label, count, w.W, w.H, gate,
                                       mode == CAGEO_TRACE_DEAD_END_ERROR ? kError : 0);
   CAGEO_CUDA(cudaGetLastError());
   return CAGEO_OK;

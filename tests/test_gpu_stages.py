@@ -148,6 +148,23 @@ def test_trace_and_border(cuda, oracle, W, H):
     assert np.array_equal(mc.cpu().numpy(), oracle.border_accumulate(ref, np.full((H, W), 3.0, np.float32)))
 
 
+@pytest.mark.parametrize("x0", [5, 31])
+def test_trace_cycle_is_an_error(cuda, x0):
+    """Directions that form a cycle never reach an outlet: tracing reports
+    CAGEO_ERR_NO_CONVERGENCE, whether the cycle stays inside a 32x32 tile
+    (x0 = 5) or crosses into the next one (x0 = 31)."""
+    from cageo_gb300 import api
+    H, W = 40, 70
+    dirs = np.zeros((H, W, 2), np.int8)
+    dirs[..., 1] = -1  # everything flows north, out of the grid
+    dirs[10, x0] = (1, 0)      # (x0, 10) -> (x0 + 1, 10)
+    dirs[10, x0 + 1] = (-1, 0)  # and back
+    streams = np.full((H, W), -9999.0, np.float32)
+    with pytest.raises(api.CageoError) as e:
+        api.trace(_t(dirs, cuda), _t(streams, cuda))
+    assert e.value.status == 3  # CAGEO_ERR_NO_CONVERGENCE
+
+
 def test_trace_dead_ends(cuda, oracle):
     """Cells without a direction never terminate in the reference; they and
     label-0 streams take cell 0's label in its connect pass."""
