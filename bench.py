@@ -46,9 +46,9 @@ FALLBACK_HBM = 6800.0
 STAGE_BYTES = {"noise": 4, "front": 40, "fill": 8, "route": 5, "trace": 6, "border": 12}
 PIPE_BYTES = 75
 # DRAM bytes per cell moved by one pit fill (both flood launches), from an
-# ncu capture of the 4096^2 workload (1678 MB for 16.8 M cells), applied
+# ncu capture of the 4096^2 workload (1674 MB for 16.8 M cells), applied
 # per cell to the benchmark grid.
-FILL_TRAFFIC_PER_CELL = 1678.2e6 / (4096 * 4096)
+FILL_TRAFFIC_PER_CELL = 1673.6e6 / (4096 * 4096)
 # Kernels per realization on the graph path: fill 6 (scalars, init, two
 # floods, classify, final), noise 1, front 1, routing 4 (scalars, d8, flat
 # relaxation, flat directions), tracing 3 (scalars, init, jump), border
@@ -248,6 +248,21 @@ def exact_mode(dem, streams, cfg, steps, warmup, base):
         pe.close()
     out["learned"]["counts_equal_plain"] = out["learned"]["counts_sum"] == out["plain"]["counts_sum"]
     out["learned_over_plain"] = out["learned"]["value"] / out["plain"]["value"]
+    # The fused network inference alone (features + 3 layers + warm surface)
+    # on a grid of the workload's size, device-timed on torch's stream.
+    params = torch.from_numpy(learned.load_params()).cuda()
+    v = torch.from_numpy(np.ascontiguousarray(dem)).cuda()
+    warm = None
+    for _ in range(2):
+        warm, _ = api.ws_infer(params, v, WARM_THRESHOLD)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(3):
+        api.ws_infer(params, v, WARM_THRESHOLD)
+    b.record()
+    torch.cuda.synchronize()
+    out["learned"]["inference_ms"] = a.elapsed_time(b) / 3
+    del warm
     return out
 
 

@@ -188,7 +188,7 @@ __device__ void flat_tile(FlatSmem& s, const float* __restrict__ dem, int* fd, c
   const int x0 = tx * kFT, y0 = ty * kFT;
   const long long c0 = clock64();
   // Stage the raw codes and elevations with asynchronous copies (all of the
-  // tile's loads in flight at once), then turn codes into relay values.
+  // tile's loads in flight at once).
   for (int idx = lane; idx < 34 * 34; idx += 32) {
     const int hy = idx / 34, hx = idx - hy * 34;
     const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
@@ -205,19 +205,20 @@ __device__ void flat_tile(FlatSmem& s, const float* __restrict__ dem, int* fd, c
   }
   cp_async_wait();
   __syncwarp();
-  // Lane y: the flat cells of row y (codes are still raw here).
+  // Lane y: the flat cells of row y, and its exits (cells with a direction
+  // that a first-layer flat cell may drain into: relay 0).  The staged codes
+  // stay raw; the seeds below turn the few they read into relay values.
   const int y = lane;
-  unsigned int flat = 0;
+  unsigned int flat = 0, exitm = 0;
 #pragma unroll
   for (int x = 0; x < kFT; x++) {
-    const int code = s.R[(y + 1) * kFRS + (x + 1)];
+    const int b = (y + 1) * kFRS + (x + 1);
+    const int code = s.R[b];
     if (code == kFlatInf || code >= 1) flat |= 1u << x;
-  }
-  __syncwarp();
-  for (int idx = lane; idx < 34 * 34; idx += 32) {
-    const int hy = idx / 34, hx = idx - hy * 34;
-    const int code = s.R[hy * kFRS + hx];
-    s.R[hy * kFRS + hx] = flat_relay(code, s.E[hy * kFRS + hx], gpu, nodata);
+    // flat_relay(code) == 0 for a non-flat cell; the elevation matters in
+    // GPU order only.
+    const bool ex = gpu ? ((code == -1 || code == -2) && s.E[b] != nodata) : code == -1;
+    if (ex) exitm |= 1u << x;
   }
   __syncwarp();
   const long long c1 = clock64();
@@ -241,8 +242,6 @@ __device__ void flat_tile(FlatSmem& s, const float* __restrict__ dem, int* fd, c
   unsigned int fdn = __shfl_down_sync(0xffffffffu, flat, 1);
   if (lane == 0) fup = 0;
   if (lane == kFT - 1) fdn = 0;
-  const unsigned int allflat = flat & fup & fdn & (flat << 1) & (flat >> 1) & (fup << 1) &
-                               (fup >> 1) & (fdn << 1) & (fdn >> 1);
   // Seed level of cell (cx, cy) (kFlatInf: none); fr = the flat masks of
   // rows cy-1, cy, cy+1 (bit set = flat cell of this tile).
   auto seed_of = [&](int cx, int cy, unsigned int fu, unsigned int fm, unsigned int fb) {
@@ -255,8 +254,9 @@ __device__ void flat_tile(FlatSmem& s, const float* __restrict__ dem, int* fd, c
       const unsigned int row = d8_dy(n) < 0 ? fu : (d8_dy(n) > 0 ? fb : fm);
       const bool inner = nx >= 0 && nx < kFT && ny >= 0 && ny < kFT && ((row >> nx) & 1u);
       const int o = b + d8_dy(n) * kFRS + d8_dx(n);
-      const int v = s.R[o];
-      if (!inner && v < best && s.E[o] <= e) best = v;
+      const float eo = s.E[o];
+      const int v = flat_relay(s.R[o], eo, gpu, nodata);  // the staged codes are raw
+      if (!inner && v < best && eo <= e) best = v;
     }
     return best < kFlatInf ? best + 1 : kFlatInf;
   };
@@ -271,10 +271,15 @@ __device__ void flat_tile(FlatSmem& s, const float* __restrict__ dem, int* fd, c
   const bool mid = lane >= 1 && lane <= kFT - 2;
   const int lseed = (mid && (flat & 1u)) ? seed_of(0, y, fup, flat, fdn) : kFlatInf;
   const int rseed = (mid && (flat >> 31)) ? seed_of(kFT - 1, y, fup, flat, fdn) : kFlatInf;
-  // Inner candidates next to a non-flat cell of the tile: level 1 or none.
+  // Inner candidates next to an exit of the tile: level 1 or none (an inner
+  // cell's other non-flat neighbours relay nothing).
+  unsigned int exu = __shfl_up_sync(0xffffffffu, exitm, 1);
+  unsigned int exd = __shfl_down_sync(0xffffffffu, exitm, 1);
+  const unsigned int ex3 = exitm | exu | exd;
+  const unsigned int near_exit = ex3 | (ex3 << 1) | (ex3 >> 1);
   unsigned int inner1 = 0;
   if (mid) {
-    for (unsigned int m = flat & ~allflat & 0x7ffffffeu; m; m &= m - 1) {
+    for (unsigned int m = flat & near_exit & 0x7ffffffeu; m; m &= m - 1) {
       const int x = __ffs(m) - 1;
       if (seed_of(x, y, fup, flat, fdn) == 1) inner1 |= 1u << x;
     }
@@ -290,6 +295,27 @@ __device__ void flat_tile(FlatSmem& s, const float* __restrict__ dem, int* fd, c
   };
   int L = next_level(0);
   unsigned int visited = 0, front = 0, changed = 0;
+  // The level of each reached cell is kept as an offset from Lb in 6 bit
+  // planes (lane = row, bit = column) and written to the staged tile in one
+  // pass per segment of at most 64 consecutive levels (when the front dies
+  // out, or after 64 levels), so the level loop itself does no shared-memory
+  // traffic.
+  int Lb = L;
+  unsigned int seg = 0, pl0 = 0, pl1 = 0, pl2 = 0, pl3 = 0, pl4 = 0, pl5 = 0;
+  auto flush = [&]() {
+    for (unsigned int r = seg; r; r &= r - 1) {
+      const int x = __ffs(r) - 1;
+      const int off = ((pl0 >> x) & 1) | (((pl1 >> x) & 1) << 1) | (((pl2 >> x) & 1) << 2) |
+                      (((pl3 >> x) & 1) << 3) | (((pl4 >> x) & 1) << 4) |
+                      (((pl5 >> x) & 1) << 5);
+      int* cell = &s.R[(y + 1) * kFRS + (x + 1)];
+      if (Lb + off < *cell) {
+        *cell = Lb + off;
+        changed |= 1u << x;
+      }
+    }
+    seg = pl0 = pl1 = pl2 = pl3 = pl4 = pl5 = 0;
+  };
   for (int guard = 0; guard < 4 * kFT * kFT && L < kFlatInf; guard++) {
     const unsigned int tb = __ballot_sync(0xffffffffu, tseed == L);
     const unsigned int bb = __ballot_sync(0xffffffffu, bseed == L);
@@ -305,17 +331,27 @@ __device__ void flat_tile(FlatSmem& s, const float* __restrict__ dem, int* fd, c
     const unsigned int reach = ((v | (v << 1) | (v >> 1)) | seeds) & flat & ~visited;
     visited |= reach;
     front = reach;
-    for (unsigned int r = reach; r; r &= r - 1) {
-      const int x = __ffs(r) - 1;
-      int* cell = &s.R[(y + 1) * kFRS + (x + 1)];
-      if (L < *cell) {
-        *cell = L;
-        changed |= 1u << x;
-      }
-    }
+    const int off = L - Lb;  // 0..63
+    seg |= reach;
+    if (off & 1) pl0 |= reach;
+    if (off & 2) pl1 |= reach;
+    if (off & 4) pl2 |= reach;
+    if (off & 8) pl3 |= reach;
+    if (off & 16) pl4 |= reach;
+    if (off & 32) pl5 |= reach;
     // Next level, or jump to the next seed level when the front died out.
-    L = __any_sync(0xffffffffu, front != 0) ? L + 1 : next_level(L);
+    if (__any_sync(0xffffffffu, front != 0)) {
+      if (++L - Lb == 64) {
+        flush();
+        Lb = L;
+      }
+    } else {
+      flush();
+      L = next_level(L);
+      Lb = L;
+    }
   }
+  flush();
   __syncwarp();
   const long long c2 = clock64();
   const bool capped = false;
