@@ -169,6 +169,75 @@ __device__ __forceinline__ void conv_line8(const float* __restrict__ v, int stri
   }
 }
 
+// p0 = w0 * t and p1 = w1 * t, each rounded to nearest, as one packed
+// single-precision multiply.
+__device__ __forceinline__ void mul2_rn(float& p0, float& p1, float w0, float w1, float t) {
+  asm("{\n\t.reg .b64 wa, tt;\n\t"
+      "mov.b64 wa, {%2, %3};\n\t"
+      "mov.b64 tt, {%4, %4};\n\t"
+      "mul.rn.f32x2 wa, wa, tt;\n\t"
+      "mov.b64 {%0, %1}, wa;\n\t}"
+      : "=f"(p0), "=f"(p1)
+      : "f"(w0), "f"(w1), "f"(t));
+}
+
+// conv_line8 for two lines at once (v0, v1; same stride and taps): the
+// window values of the two lines at one position are multiplied as one
+// packed pair, and the two windows shift together, so the pairs stay put
+// in registers.  ADJ: the lines are adjacent columns (v1 = v0 + 1, v0
+// 8-byte aligned), loaded as one float2.  Each sum runs over t ascending,
+// as in conv_line8.
+template <int LC, bool ADJ>
+__device__ __forceinline__ void conv_line8x2(const float* __restrict__ v0,
+                                             const float* __restrict__ v1, int stride,
+                                             const float* __restrict__ taps, int L,
+                                             float a0[8], float a1[8]) {
+  float w0[8], w1[8];
+  auto load = [&](int k, float& x0, float& x1) {
+    if (ADJ) {
+      const float2 p = *reinterpret_cast<const float2*>(v0 + k * stride);
+      x0 = p.x;
+      x1 = p.y;
+    } else {
+      x0 = v0[k * stride];
+      x1 = v1[k * stride];
+    }
+  };
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    load(j, w0[j], w1[j]);
+    a0[j] = 0.0f;
+    a1[j] = 0.0f;
+  }
+  auto tap_step = [&](float tap) {
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      float p0, p1;
+      mul2_rn(p0, p1, w0[j], w1[j], tap);
+      a0[j] = __fadd_rn(a0[j], p0);
+      a1[j] = __fadd_rn(a1[j], p1);
+    }
+#pragma unroll
+    for (int j = 0; j < 7; j++) {
+      w0[j] = w0[j + 1];
+      w1[j] = w1[j + 1];
+    }
+  };
+  if (LC > 0) {
+#pragma unroll
+    for (int t = 0; t < LC; t++) {
+      tap_step(taps[t]);
+      if (t + 1 < LC) load(t + 8, w0[7], w1[7]);
+    }
+  } else {
+#pragma unroll 4
+    for (int t = 0; t < L; t++) {
+      tap_step(taps[t]);
+      if (t + 1 < L) load(t + 8, w0[7], w1[7]);
+    }
+  }
+}
+
 template <class Epi, int LC>
 __global__ void __launch_bounds__(kSepThreads)
 conv_sep_kernel(const float* __restrict__ in, int W, int H,
@@ -199,13 +268,16 @@ conv_sep_kernel(const float* __restrict__ in, int W, int H,
     cp_async_wait();
   }
   __syncthreads();
-  // Column pass: tmp[y][ix] = sum_t in[y+t][ix] * taps[t], 8 rows per item.
-  for (int item = threadIdx.x; item < IW * (kSepTH / 8); item += blockDim.x) {
-    const int g = item / IW, ix = item - g * IW;
-    float acc[8];
-    conv_line8<LC>(s_in + (8 * g) * IW + ix, IW, s_taps, L, acc);
+  // Column pass: tmp[y][ix] = sum_t in[y+t][ix] * taps[t]; an item is 8
+  // rows of two adjacent columns (IW is even).
+  const int IW2 = IW / 2;
+  for (int item = threadIdx.x; item < IW2 * (kSepTH / 8); item += blockDim.x) {
+    const int g = item / IW2, ix = 2 * (item - g * IW2);
+    float a0[8], a1[8];
+    conv_line8x2<LC, true>(s_in + (8 * g) * IW + ix, nullptr, IW, s_taps, L, a0, a1);
 #pragma unroll
-    for (int j = 0; j < 8; j++) s_tmp[(8 * g + j) * IW + ix] = acc[j];
+    for (int j = 0; j < 8; j++)
+      *reinterpret_cast<float2*>(&s_tmp[(8 * g + j) * IW + ix]) = make_float2(a0[j], a1[j]);
   }
   __syncthreads();
   // Row pass (8 consecutive outputs per item) and store.
