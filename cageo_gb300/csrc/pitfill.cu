@@ -99,7 +99,7 @@ size_t fill_workspace_bytes(int W, int H) {
   size_t n = (size_t)W * H;
   size_t nt = (size_t)((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile);
   return align_up(n, 256) + align_up(nt * 4, 256) + align_up((2 * nt + kRingSlack) * 4, 256) +
-         3 * align_up(nt, 256) + 3 * align_up(n * 4, 256) + 1024;
+         2 * align_up(nt, 256) + 3 * align_up(n * 4, 256) + 1024;
 }
 
 FillWork fill_carve(void* base, int W, int H) {
@@ -116,8 +116,6 @@ FillWork fill_carve(void* base, int W, int H) {
   p += align_up(nt * 4, 256);
   w.lists = (int*)p;
   p += align_up((2 * nt + kRingSlack) * 4, 256);
-  w.tdone = (uint8_t*)p;
-  p += align_up(nt, 256);
   w.tseed = (uint8_t*)p;
   p += align_up(nt, 256);
   w.tconv = (uint8_t*)p;
@@ -154,10 +152,13 @@ struct FloodArgs {
 // above, so the order of the updates does not change their limit; what
 // must not happen is two warps processing one tile at once (a slower
 // warp's write-back could undo a faster one's lower values).  Each tile
-// therefore has a state: 0 idle, 1 queued, 2 processing, 3 processing and
-// queued again meanwhile (re-queued when its processing ends).  `pending`
-// counts tiles in states 1-3; the queue is drained when it reaches 0.  The
-// ring (w.lists, 2 * ntiles slots, -1 = empty) holds each queued tile once.
+// therefore has a state: idle, queued, processing, processing and queued
+// again meanwhile (re-queued when its processing ends), or done (every
+// cell final: never queued again in this flood).  `pending` counts tiles
+// that are queued or processing; the queue is drained when it reaches 0.
+// The ring (w.lists, 2 * ntiles slots, -1 = empty) holds each queued tile
+// once.
+enum : int { kIdle = 0, kQueued = 1, kBusy = 2, kBusyQueued = 3, kDone = 4 };
 constexpr int kEmptySlot = -1;
 
 __device__ __forceinline__ unsigned int ring_cap(const FillWork& w) {
@@ -167,24 +168,27 @@ __device__ __forceinline__ unsigned int ring_cap(const FillWork& w) {
 __device__ __forceinline__ void ring_push(const FillWork& w, int t) {
   const unsigned int cap = ring_cap(w);
   const unsigned int pos = atomicAdd(&w.scal[S_TAIL], 1u);
-  atomicExch(&w.lists[pos % cap], t);
+  // A plain store: the taker swaps the slot for "empty" and retries while
+  // it reads empty.
+  ((volatile int*)w.lists)[pos % cap] = t;
 }
 
+// Queue tile t unless it is queued already or done: idle -> queued,
+// processing -> processing and queued again.  A single compare-and-swap
+// when the state is the one expected.
 __device__ __forceinline__ void enqueue(const FillWork& w, int t) {
-  if (((volatile uint8_t*)w.tdone)[t]) return;  // every cell of the tile is final
+  int expect = kIdle;
   for (int it = 0; it < 256; it++) {
-    const int st = ((volatile int*)w.queued)[t];
-    if (st == 0) {
-      if (atomicCAS(&w.queued[t], 0, 1) == 0) {
+    const int old = atomicCAS(&w.queued[t], expect, expect == kIdle ? kQueued : kBusyQueued);
+    if (old == expect) {
+      if (expect == kIdle) {
         atomicAdd(&w.scal[S_PENDING], 1u);
         ring_push(w, t);
-        return;
       }
-    } else if (st == 2) {
-      if (atomicCAS(&w.queued[t], 2, 3) == 2) return;
-    } else {
-      return;  // already queued
+      return;
     }
+    if (old != kIdle && old != kBusy) return;  // queued already, or done
+    expect = old;
   }
   atomicCAS((int*)(w.scal + S_ERR), 0, 3);
 }
@@ -203,18 +207,24 @@ __device__ __forceinline__ int try_dequeue(const FillWork& w, long long* ticket)
   const int t = atomicExch(&w.lists[(unsigned int)*ticket % ring_cap(w)], kEmptySlot);
   if (t == kEmptySlot) return -1;
   *ticket = -1;
-  atomicExch(&w.queued[t], 2);
+  // Queued -> processing: only the taker changes a queued tile's state.
+  // The fence puts the change before the staging loads, so a neighbour
+  // that writes the halo later sees "processing" and queues the tile again.
+  ((volatile int*)w.queued)[t] = kBusy;
   __threadfence();
   return t;
 }
 
-// Lane 0, after the tile's write-back: idle again, or re-queued if a
-// neighbour queued it while it was being processed.
-__device__ __forceinline__ void finish_tile(const FillWork& w, int t) {
-  if (atomicCAS(&w.queued[t], 2, 0) == 2) {
+// Lane 0, after the tile's write-back: idle again (done if every cell is
+// final), or queued again if a neighbour queued it while it was processed.
+__device__ __forceinline__ void finish_tile(const FillWork& w, int t, bool done) {
+  if (atomicCAS(&w.queued[t], kBusy, done ? kDone : kIdle) == kBusy) {
+    atomicSub(&w.scal[S_PENDING], 1u);
+  } else if (done) {  // processing and queued again: only the owner changes that state
+    ((volatile int*)w.queued)[t] = kDone;
     atomicSub(&w.scal[S_PENDING], 1u);
   } else {
-    atomicExch(&w.queued[t], 1);
+    ((volatile int*)w.queued)[t] = kQueued;
     ring_push(w, t);
   }
 }
@@ -264,8 +274,9 @@ __device__ __forceinline__ float col3_min(const WarpSmem& s, int rx, int y) {
   return fminf(fminf(r[0], r[kRS]), r[2 * kRS]);
 }
 
+// Returns whether every cell of the tile is final (NODATA, outlet or FBELOW).
 template <int MODE>
-__device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t,
+__device__ bool process_tile(WarpSmem& s, const FloodArgs& a, int t,
                              int lane) {
   const FillWork& w = a.w;
   const int W = w.W, H = w.H;
@@ -390,13 +401,14 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t,
                              ((rows_changed >> 31) ? 8u : 0u) | ((dl & 1u) ? 16u : 0u) |
                              ((dr & 1u) ? 32u : 0u) | ((dl >> 31) ? 64u : 0u) |
                              ((dr >> 31) ? 128u : 0u);
-  // Every cell final?  Only a change can make it so: a visit that changed
-  // nothing leaves the answer of the visit before.
-  if (rows_changed) {
+  // Every cell final?  Only a change can make it so after the first visit: a
+  // later visit that changed nothing leaves the answer of the visit before.
+  bool done = false;
+  if (rows_changed || !revisit) {
     bool fin = true;
     for (int idx = lane; idx < kTile * kTile; idx += 32)
       fin &= (s.F[(idx >> 5) * kFS + (idx & 31)] & (FNODATA | FOUTLET | FBELOW)) != 0;
-    if (__all_sync(0xffffffffu, fin) && lane == 0) w.tdone[t] = 1;
+    done = __all_sync(0xffffffffu, fin);
   }
   // Lanes 0..8 queue self (if capped) and the 8 neighbours whose halo changed.
   if (lane < 9) {
@@ -424,6 +436,7 @@ __device__ void process_tile(WarpSmem& s, const FloodArgs& a, int t,
     atomicAdd(&w.scal[S_KCYC_SWEEP], (unsigned int)((c2 - c1) >> 10));
     atomicAdd(&w.scal[S_KCYC_STORE], (unsigned int)((c3 - c2) >> 10));
   }
+  return done;
 }
 
 // Lock-free union-find over the undecided cells (labels in w.aux): links
@@ -467,8 +480,8 @@ __device__ bool drain(WarpSmem& s, const FloodArgs& a, int lane, int ntiles) {
     if (lane == 0) t = try_dequeue(w, &ticket);
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= 0) {
-      process_tile<MODE>(s, a, t, lane);
-      if (lane == 0) finish_tile(w, t);
+      const bool done = process_tile<MODE>(s, a, t, lane);
+      if (lane == 0) finish_tile(w, t, done);
       __syncwarp();
       idle = 0;
       ns = 32;
@@ -795,14 +808,14 @@ cageo_status fill_run(const float* q, float* filled, const FillWork& w, float no
                                         w.W, w.H, nodata);
   CAGEO_CUDA(cudaGetLastError());
   FloodArgs a{q, filled, w};
-  CAGEO_CUDA(cudaMemsetAsync(w.tdone, 0, nt, s));
+  CAGEO_CUDA(cudaMemsetAsync(w.queued, 0, sizeof(int) * nt, s));  // all idle
   CAGEO_CUDA(cudaMemsetAsync(w.tconv, 0, nt, s));
   CAGEO_CUDA(cudaMemsetAsync(w.lists, 0xff, (2 * nt + kRingSlack) * sizeof(int), s));  // empty ring
   cageo_status st = launch_flood<0>(a, s);
   if (st) return st;
   fill_classify_kernel<<<blocks, 256, 0, s>>>(filled, w.flags, w.aux, w.scal, n);
   CAGEO_CUDA(cudaGetLastError());
-  CAGEO_CUDA(cudaMemsetAsync(w.tdone, 0, nt, s));
+  CAGEO_CUDA(cudaMemsetAsync(w.queued, 0, sizeof(int) * nt, s));  // all idle
   CAGEO_CUDA(cudaMemsetAsync(w.tconv, 0, nt, s));
   st = launch_flood<1>(a, s);
   if (st) return st;
@@ -823,7 +836,7 @@ cageo_status fill_run_exact(const float* v, float* filled, const FillWork& w, fl
   fill_init_exact_kernel<<<rows, 256, 0, s>>>(v, filled, w.flags, warm, w.tseed, w.tiles_x, w.W,
                                               w.H, nodata);
   CAGEO_CUDA(cudaGetLastError());
-  CAGEO_CUDA(cudaMemsetAsync(w.tdone, 0, nt, s));
+  CAGEO_CUDA(cudaMemsetAsync(w.queued, 0, sizeof(int) * nt, s));  // all idle
   CAGEO_CUDA(cudaMemsetAsync(w.tconv, 0, nt, s));
   CAGEO_CUDA(cudaMemsetAsync(w.lists, 0xff, (2 * nt + kRingSlack) * sizeof(int), s));  // empty ring
   FloodArgs a{v, filled, w};

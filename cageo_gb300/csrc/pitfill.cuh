@@ -13,9 +13,8 @@ struct FillWork {
   int W = 0, H = 0;
   int tiles_x = 0, tiles_y = 0;
   uint8_t* flags = nullptr;      // W*H
-  int* queued = nullptr;         // ntiles: last pass a tile was queued for
+  int* queued = nullptr;         // ntiles: tile state in the work queue (idle, queued, processing, re-queued, done)
   int* lists = nullptr;          // 2 * ntiles: tile worklists (double buffer)
-  uint8_t* tdone = nullptr;      // ntiles: 1 once every cell of the tile is final
   uint8_t* tseed = nullptr;      // ntiles: tile holds a relaying outlet
   uint8_t* tconv = nullptr;      // ntiles: tile converged on its last visit
   uint32_t* cand = nullptr;      // W*H: list of undecided cells of the phases
