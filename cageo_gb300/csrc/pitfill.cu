@@ -331,11 +331,14 @@ __device__ bool process_tile(WarpSmem& s, const FloodArgs& a, int t,
   // at the crossing (k = 16) a cell that reads the other's old value is
   // re-evaluated through the masks like any other.
   for (; rounds < max_rounds && (pd | pu | pr | pl); rounds++) {
-#pragma unroll 4
+    // Step k evaluates row k (down) and row 31 - k (up); steps with neither
+    // pending are skipped by a find-first-set over both masks.
     for (int k = 0; k < kTile; k++) {
+      const unsigned int m = (pd | __brev(pu)) >> k;
+      if (!m) break;
+      k += __ffs(m) - 1;
       const int d = k, u = kTile - 1 - k;
       const unsigned int bd = 1u << d, bu = 1u << u;
-      if (!((pd & bd) | (pu & bu))) continue;
       pd &= ~bd;
       pu &= ~bu;
       const CellEval ed = cell_load(s, lane, d, row3_min(s, lane, d));
@@ -353,11 +356,12 @@ __device__ bool process_tile(WarpSmem& s, const FloodArgs& a, int t,
       }
       __syncwarp();
     }
-#pragma unroll 4
     for (int k = 0; k < kTile; k++) {
+      const unsigned int m = (pr | __brev(pl)) >> k;
+      if (!m) break;
+      k += __ffs(m) - 1;
       const int l = k, r = kTile - 1 - k;
       const unsigned int bl = 1u << l, br = 1u << r;
-      if (!((pr & bl) | (pl & br))) continue;
       pr &= ~bl;
       pl &= ~br;
       const CellEval el = cell_load(s, l, lane, col3_min(s, l, lane));
