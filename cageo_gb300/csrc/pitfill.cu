@@ -274,10 +274,27 @@ __device__ __forceinline__ float col3_min(const WarpSmem& s, int rx, int y) {
   return fminf(fminf(r[0], r[kRS]), r[2 * kRS]);
 }
 
+// Per-warp visit statistics (lane 0), added to the scalar block every 64
+// visits and when a drain ends: one atomic per counter and flush instead of
+// five atomics on one cache line per visit.
+struct VisitStats {
+  unsigned int tiles = 0, rounds = 0, kload = 0, ksweep = 0, kstore = 0;
+};
+
+template <int MODE>
+__device__ __forceinline__ void flush_stats(const FillWork& w, VisitStats& st) {
+  if (!st.tiles) return;
+  atomicAdd(&w.scal[MODE == 0 ? S_TILES_A : S_TILES_B], st.tiles);
+  atomicAdd(&w.scal[MODE == 0 ? S_ROUNDS_A : S_ROUNDS_B], st.rounds);
+  atomicAdd(&w.scal[S_KCYC_LOAD], st.kload);
+  atomicAdd(&w.scal[S_KCYC_SWEEP], st.ksweep);
+  atomicAdd(&w.scal[S_KCYC_STORE], st.kstore);
+  st = VisitStats{};
+}
+
 // Returns whether every cell of the tile is final (NODATA, outlet or FBELOW).
 template <int MODE>
-__device__ bool process_tile(WarpSmem& s, const FloodArgs& a, int t,
-                             int lane) {
+__device__ bool process_tile(WarpSmem& s, const FloodArgs& a, int t, int lane, VisitStats& st) {
   const FillWork& w = a.w;
   const int W = w.W, H = w.H;
   const int tx = t % w.tiles_x, ty = t / w.tiles_x;
@@ -384,8 +401,8 @@ __device__ bool process_tile(WarpSmem& s, const FloodArgs& a, int t,
   const long long c2 = clock64();
   if (lane == 0) {
     w.tconv[t] = capped ? 0 : 1;
-    atomicAdd(&w.scal[MODE == 0 ? S_TILES_A : S_TILES_B], 1u);
-    atomicAdd(&w.scal[MODE == 0 ? S_ROUNDS_A : S_ROUNDS_B], (unsigned int)rounds);
+    st.tiles++;
+    st.rounds += (unsigned int)rounds;
   }
   // Write back the changed cells, row by row (coalesced); note which
   // borders changed.  Cells outside the grid are NODATA and never change.
@@ -398,7 +415,10 @@ __device__ bool process_tile(WarpSmem& s, const FloodArgs& a, int t,
       w.flags[i] = s.F[y * kFS + lane];
     }
   }
-  __threadfence();  // the write-back is visible before any neighbour is queued
+  // The write-back (and a "not converged" mark) is visible before any
+  // neighbour is queued or the tile's state changes.  A visit that changed
+  // nothing wrote nothing and queues no one.
+  if (rows_changed) __threadfence();
   const unsigned int dl = __shfl_sync(0xffffffffu, dc, 0), dr = __shfl_sync(0xffffffffu, dc, 31);
   // 1 L, 2 R, 4 T, 8 B, 16 TL, 32 TR, 64 BL, 128 BR
   const unsigned int sides = (dl ? 1u : 0u) | (dr ? 2u : 0u) | ((rows_changed & 1u) ? 4u : 0u) |
@@ -436,9 +456,9 @@ __device__ bool process_tile(WarpSmem& s, const FloodArgs& a, int t,
   __syncwarp();
   if (lane == 0) {
     const long long c3 = clock64();
-    atomicAdd(&w.scal[S_KCYC_LOAD], (unsigned int)((c1 - c0) >> 10));
-    atomicAdd(&w.scal[S_KCYC_SWEEP], (unsigned int)((c2 - c1) >> 10));
-    atomicAdd(&w.scal[S_KCYC_STORE], (unsigned int)((c3 - c2) >> 10));
+    st.kload += (unsigned int)((c1 - c0) >> 10);
+    st.ksweep += (unsigned int)((c2 - c1) >> 10);
+    st.kstore += (unsigned int)((c3 - c2) >> 10);
   }
   return done;
 }
@@ -479,27 +499,39 @@ __device__ bool drain(WarpSmem& s, const FloodArgs& a, int lane, int ntiles) {
   const unsigned int visit_cap = 1000u * (unsigned int)min(ntiles, 4000000);
   long long ticket = -1;
   unsigned int ns = 32;
+  VisitStats st;
+  bool ok = true;
   for (long long idle = 0;;) {
     int t = -1;
     if (lane == 0) t = try_dequeue(w, &ticket);
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= 0) {
-      const bool done = process_tile<MODE>(s, a, t, lane);
-      if (lane == 0) finish_tile(w, t, done);
+      const bool done = process_tile<MODE>(s, a, t, lane, st);
+      if (lane == 0) {
+        finish_tile(w, t, done);
+        if (st.tiles >= 64) flush_stats<MODE>(w, st);
+      }
       __syncwarp();
       idle = 0;
       ns = 32;
       continue;
     }
-    if (vs[S_ERR]) return false;
-    if (vs[S_PENDING] == 0u) return true;
+    if (vs[S_ERR]) {
+      ok = false;
+      break;
+    }
+    if (vs[S_PENDING] == 0u) break;
     if (++idle > (1LL << 24) || vs[MODE == 0 ? S_TILES_A : S_TILES_B] > visit_cap) {
       if (lane == 0) atomicCAS((int*)(w.scal + S_ERR), 0, 2);
-      return false;
+      ok = false;
+      break;
     }
     __nanosleep(ns);
     if (ns < 1024) ns <<= 1;
   }
+  if (lane == 0) flush_stats<MODE>(w, st);
+  __syncwarp();
+  return ok;
 }
 
 template <int MODE>
