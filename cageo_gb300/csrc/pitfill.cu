@@ -697,26 +697,34 @@ fill_flood_kernel(FloodArgs a) {
   }
 }
 
+// Cells per thread of the elementwise fill kernels (fewer, longer blocks).
+constexpr int kCellsPerThread = 4;
+
 __global__ void fill_init_kernel(const float* __restrict__ q, float* __restrict__ Wg,
                                  uint8_t* __restrict__ F, const unsigned int* minslot,
                                  uint8_t* __restrict__ tseed, int tiles_x, int W, int H,
                                  float nodata) {
-  // One block row per grid row: no division to find the cell's x and y.
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
-  if (x >= W) return;
-  const int64_t i = (int64_t)y * W + x;
+  // One block row per grid row (no division to find a cell's x and y);
+  // kCellsPerThread cells a block-width apart per thread (coalesced).
+  const int y = blockIdx.y;
   const float minE = ordered_to_float(*minslot);
-  float qv = q[i];
-  uint8_t f = 0;
-  if (qv == nodata) {
-    f = FNODATA;
-  } else {
-    if (!fill_passable(qv, minE)) f |= FNONPASS;
-    if (x == 0 || y == 0 || x == W - 1 || y == H - 1 || qv == 0.0f) f |= FOUTLET;
+#pragma unroll
+  for (int k = 0; k < kCellsPerThread; k++) {
+    const int x = (blockIdx.x * kCellsPerThread + k) * blockDim.x + threadIdx.x;
+    if (x >= W) break;
+    const int64_t i = (int64_t)y * W + x;
+    const float qv = q[i];
+    uint8_t f = 0;
+    if (qv == nodata) {
+      f = FNODATA;
+    } else {
+      if (!fill_passable(qv, minE)) f |= FNONPASS;
+      if (x == 0 || y == 0 || x == W - 1 || y == H - 1 || qv == 0.0f) f |= FOUTLET;
+    }
+    F[i] = f;
+    Wg[i] = (f & (FNODATA | FOUTLET)) ? qv : kInf;
+    if ((f & FOUTLET) && !(f & FNONPASS)) tseed[(y / kTile) * tiles_x + x / kTile] = 1;
   }
-  F[i] = f;
-  Wg[i] = (f & (FNODATA | FOUTLET)) ? qv : kInf;
-  if ((f & FOUTLET) && !(f & FNONPASS)) tseed[(y / kTile) * tiles_x + x / kTile] = 1;
 }
 
 // Exact mode (the reference's GPU fill, src/pitfilling/PitFillingAlgorithmGPUCUDA.cu:201-231):
@@ -727,22 +735,29 @@ __global__ void fill_init_exact_kernel(const float* __restrict__ v, float* __res
                                        uint8_t* __restrict__ F, const float* __restrict__ warm,
                                        uint8_t* __restrict__ tseed, int tiles_x, int W, int H,
                                        float nodata) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
-  if (x >= W) return;
-  const int64_t i = (int64_t)y * W + x;
-  const float e = v[i];
-  uint8_t f = 0;
-  if (e == nodata) f = FNODATA;
-  else if (x == 0 || y == 0 || x == W - 1 || y == H - 1 || e == 0.0f) f = FOUTLET;
-  F[i] = f;
-  Wg[i] = f ? e : (warm ? fmaxf(warm[i], e) : kInf);
-  if (f == FOUTLET) tseed[(y / kTile) * tiles_x + x / kTile] = 1;
+  const int y = blockIdx.y;
+#pragma unroll
+  for (int k = 0; k < kCellsPerThread; k++) {
+    const int x = (blockIdx.x * kCellsPerThread + k) * blockDim.x + threadIdx.x;
+    if (x >= W) break;
+    const int64_t i = (int64_t)y * W + x;
+    const float e = v[i];
+    uint8_t f = 0;
+    if (e == nodata) f = FNODATA;
+    else if (x == 0 || y == 0 || x == W - 1 || y == H - 1 || e == 0.0f) f = FOUTLET;
+    F[i] = f;
+    Wg[i] = f ? e : (warm ? fmaxf(warm[i], e) : kInf);
+    if (f == FOUTLET) tseed[(y / kTile) * tiles_x + x / kTile] = 1;
+  }
 }
 
 // Cells no outlet reaches keep the reference's initial value.
 __global__ void fill_final_exact_kernel(float* __restrict__ Wg, int64_t n) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n && Wg[i] == kInf) Wg[i] = 99990000.0f;
+#pragma unroll
+  for (int k = 0; k < kCellsPerThread; k++) {
+    const int64_t i = ((int64_t)blockIdx.x * kCellsPerThread + k) * blockDim.x + threadIdx.x;
+    if (i < n && Wg[i] == kInf) Wg[i] = 99990000.0f;
+  }
 }
 
 // Between the floods: keep flood A's result (lower bound) in aux and
@@ -751,28 +766,34 @@ __global__ void fill_final_exact_kernel(float* __restrict__ Wg, int64_t n) {
 // flood B's first pass appends to.
 __global__ void fill_classify_kernel(float* __restrict__ Wg, uint8_t* __restrict__ F,
                                      uint32_t* __restrict__ aux, unsigned int* scal, int64_t n) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
     scal[S_HEAD] = 0u;
     scal[S_TAIL] = 0u;
     scal[S_PENDING] = 0u;
   }
-  if (i >= n) return;
-  uint8_t f = F[i];
-  const float wa = Wg[i];
-  aux[i] = __float_as_uint(wa);
-  if (f & (FNODATA | FOUTLET)) return;
-  if ((f & FNONPASS) && !(f & FBELOW) && wa < kInf) f |= FCONF;
-  if (f & FBELOW) f |= FBELOWA;
-  F[i] = f & (uint8_t)~FBELOW;
-  Wg[i] = kInf;
+#pragma unroll
+  for (int k = 0; k < kCellsPerThread; k++) {
+    const int64_t i = ((int64_t)blockIdx.x * kCellsPerThread + k) * blockDim.x + threadIdx.x;
+    if (i >= n) break;
+    uint8_t f = F[i];
+    const float wa = Wg[i];
+    aux[i] = __float_as_uint(wa);
+    if (f & (FNODATA | FOUTLET)) continue;
+    if ((f & FNONPASS) && !(f & FBELOW) && wa < kInf) f |= FCONF;
+    if (f & FBELOW) f |= FBELOWA;
+    F[i] = f & (uint8_t)~FBELOW;
+    Wg[i] = kInf;
+  }
 }
 
 __global__ void fill_final_kernel(const float* __restrict__ q, float* __restrict__ Wg,
                                   int64_t n) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  if (Wg[i] == kInf) Wg[i] = q[i];
+#pragma unroll
+  for (int k = 0; k < kCellsPerThread; k++) {
+    const int64_t i = ((int64_t)blockIdx.x * kCellsPerThread + k) * blockDim.x + threadIdx.x;
+    if (i >= n) break;
+    if (Wg[i] == kInf) Wg[i] = q[i];
+  }
 }
 
 __global__ void quantize_min_kernel(float* __restrict__ d, int64_t n, float nodata,
@@ -836,10 +857,11 @@ cageo_status fill_reset_scalars(const FillWork& w, cudaStream_t s) {
 cageo_status fill_run(const float* q, float* filled, const FillWork& w, float nodata,
                       cudaStream_t s) {
   const int64_t n = (int64_t)w.W * w.H;
-  const unsigned blocks = (unsigned)((n + 255) / 256);
+  const unsigned blocks = (unsigned)((n + 256 * kCellsPerThread - 1) / (256 * kCellsPerThread));
   const size_t nt = (size_t)w.tiles_x * w.tiles_y;
   CAGEO_CUDA(cudaMemsetAsync(w.tseed, 0, nt, s));
-  const dim3 rows((unsigned)((w.W + 255) / 256), (unsigned)w.H);
+  const dim3 rows((unsigned)((w.W + 256 * kCellsPerThread - 1) / (256 * kCellsPerThread)),
+                   (unsigned)w.H);
   fill_init_kernel<<<rows, 256, 0, s>>>(q, filled, w.flags, w.scal + S_MIN, w.tseed, w.tiles_x,
                                         w.W, w.H, nodata);
   CAGEO_CUDA(cudaGetLastError());
@@ -863,12 +885,13 @@ cageo_status fill_run(const float* q, float* filled, const FillWork& w, float no
 cageo_status fill_run_exact(const float* v, float* filled, const FillWork& w, float nodata,
                             const float* warm, cudaStream_t s) {
   const int64_t n = (int64_t)w.W * w.H;
-  const unsigned blocks = (unsigned)((n + 255) / 256);
+  const unsigned blocks = (unsigned)((n + 256 * kCellsPerThread - 1) / (256 * kCellsPerThread));
   const size_t nt = (size_t)w.tiles_x * w.tiles_y;
   // A warm start may hold values above the answer anywhere: every tile is
   // visited on the first pass.
   CAGEO_CUDA(cudaMemsetAsync(w.tseed, warm ? 1 : 0, nt, s));
-  const dim3 rows((unsigned)((w.W + 255) / 256), (unsigned)w.H);
+  const dim3 rows((unsigned)((w.W + 256 * kCellsPerThread - 1) / (256 * kCellsPerThread)),
+                   (unsigned)w.H);
   fill_init_exact_kernel<<<rows, 256, 0, s>>>(v, filled, w.flags, warm, w.tseed, w.tiles_x, w.W,
                                               w.H, nodata);
   CAGEO_CUDA(cudaGetLastError());
