@@ -81,7 +81,7 @@ __device__ __forceinline__ unsigned long long global_ns() {
 
 constexpr int kTile = 32;
 constexpr int kRingSlack = 8192;  // work-ring room for tickets taken ahead of the pushes (> warps)
-constexpr int kWarps = 15;  // one 480-thread block per SM (15 x 14.5 KB smem)
+constexpr int kWarps = 16;  // one 512-thread block per SM (16 x 14.0 KB smem, 128 registers)
 constexpr int kRS = 35;           // relay row stride (34 used)
 constexpr int kWS = 33;           // W/q row stride
 constexpr int kFS = 36;           // flag row stride (bytes)
