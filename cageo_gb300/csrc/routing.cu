@@ -39,7 +39,7 @@ enum : int { R_NFLAT = 0, R_ERR = 3, R_LIST = 4, R_LAYERS = 7, R_US_BFS = 8, R_P
              R_NEXT = 40,  // 3 slots (own line): next list index of a pass
              R_BAR_COUNT = kBarCountSlot, R_BAR_GEN = kBarGenSlot, R_SIZE = kScalarSlots };
 constexpr int kFT = 32;          // flat tile size
-constexpr int kFWarps = 16;      // warps per block of the flat kernel
+constexpr int kFWarps = 20;      // warps per block of the flat kernel (20 x 9.5 KB smem)
 constexpr int kFRS = 35;         // staged row stride
 
 size_t route_workspace_bytes(int W, int H) {
