@@ -37,6 +37,7 @@ constexpr int kOffGrid = (int)0x80000000;  // staged code of a cell outside the 
 enum : int { R_NFLAT = 0, R_ERR = 3, R_LIST = 4, R_LAYERS = 7, R_US_BFS = 8, R_PASSES = 9,
              R_TILES = 10, R_KCYC_LOAD = 11, R_KCYC_BFS = 12, R_KCYC_STORE = 13,
              R_NEXT = 40,  // 3 slots (own line): next list index of a pass
+             R_CLS = 44,   // 4 slots: next tile of each parity class in the first pass
              R_BAR_COUNT = kBarCountSlot, R_BAR_GEN = kBarGenSlot, R_SIZE = kScalarSlots };
 constexpr int kFT = 32;          // flat tile size
 constexpr int kFWarps = 20;      // warps per block of the flat kernel (20 x 9.5 KB smem)
@@ -413,17 +414,39 @@ flat_relax_kernel(const float* __restrict__ dem, int* fd, RouteWork w, int gpu, 
       vs[R_LIST + (p + 2) % 3] = 0u;
       vs[R_NEXT + (p + 1) % 3] = 0u;  // used by the next pass, after the barrier
     }
-    const int n = full ? ntiles : (int)vs[R_LIST + p % 3];
-    const int* list = w.lists + (p & 1) * ntiles;
     // Tiles are handed out one at a time, so warps that finish early take more.
-    for (;;) {
-      int i = 0;
-      if (lane == 0) i = (int)atomicAdd(&w.scal[R_NEXT + p % 3], 1u);
-      i = __shfl_sync(0xffffffffu, i, 0);
-      if (i >= n) break;
-      const int t = full ? i : list[i];
-      if (full && !w.tflat[t]) continue;
-      flat_tile(s, dem, fd, w, t, p, lane, gpu != 0, nodata);
+    if (full) {
+      // First pass: every tile with a flat cell, one 2x2 parity class of
+      // tiles after another (grid barrier between), so a tile is never
+      // searched while its neighbours are and each class starts from the
+      // finished borders of the classes before it.
+      const int hx = (w.tiles_x + 1) / 2, hy = (w.tiles_y + 1) / 2;
+      bool ok = true;
+      for (int c = 0; c < 4 && ok; c++) {
+        for (;;) {
+          int i = 0;
+          if (lane == 0) i = (int)atomicAdd(&w.scal[R_CLS + c], 1u);
+          i = __shfl_sync(0xffffffffu, i, 0);
+          if (i >= hx * hy) break;
+          const int tx = 2 * (i % hx) + (c & 1), ty = 2 * (i / hx) + (c >> 1);
+          if (tx >= w.tiles_x || ty >= w.tiles_y) continue;
+          const int t = ty * w.tiles_x + tx;
+          if (!w.tflat[t]) continue;
+          flat_tile(s, dem, fd, w, t, p, lane, gpu != 0, nodata);
+        }
+        if (c < 3) ok = grid_barrier(gs, gridDim.x);
+      }
+      if (!ok) break;
+    } else {
+      const int n = (int)vs[R_LIST + p % 3];
+      const int* list = w.lists + (p & 1) * ntiles;
+      for (;;) {
+        int i = 0;
+        if (lane == 0) i = (int)atomicAdd(&w.scal[R_NEXT + p % 3], 1u);
+        i = __shfl_sync(0xffffffffu, i, 0);
+        if (i >= n) break;
+        flat_tile(s, dem, fd, w, list[i], p, lane, gpu != 0, nodata);
+      }
     }
     if (!grid_barrier(gs, gridDim.x)) break;
     if (vs[R_LIST + (p + 1) % 3] == 0u) break;
