@@ -45,6 +45,28 @@ def test_pipeline_counts(cuda, oracle, W, H, model, graphs):
     p.close()
 
 
+@pytest.mark.parametrize("W,H,rng_m", [(2, 2, 4.0), (3, 40, 4.0), (40, 3, 4.0), (33, 33, 30.0),
+                                       (31, 65, 30.0), (65, 31, 10.0)])
+def test_pipeline_small_and_thin_grids(cuda, oracle, W, H, rng_m):
+    """Grids smaller than a 32x32 tile, a tile and one cell, or a few cells
+    thin: partial tiles on every side, the whole grid a border."""
+    from cageo_gb300 import api, synth
+    dem = synth.fbm_dem(W, H, 0.8, 7 * W + H, 80.0, 180.0)
+    streams = np.full((H, W), -9999.0, np.float32)
+    streams[H // 2, W // 2] = 1.0  # one stream cell
+    p = api.Pipeline(dem, streams, filter_model=1, practical_range=rng_m, error_stddev=1.5,
+                     seed=5, use_graphs=True)
+    p.run(0, 3)
+    got = p.counts()
+    f, d, lab = p.last_stages()
+    ref, (rf, rd, rl) = _oracle_counts(oracle, dem, streams, 5, range(3), 1, rng_m, 1.5)
+    assert np.array_equal(got, ref)
+    assert np.array_equal(bits(f), bits(rf))
+    assert np.array_equal(d, rd)
+    assert np.array_equal(lab, rl)
+    p.close()
+
+
 def test_pipeline_nodata_zero_uses_stage_path(cuda, oracle):
     from cageo_gb300 import api
     dem, streams = make_case(96, 80, seed=5)
