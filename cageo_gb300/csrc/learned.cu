@@ -269,6 +269,27 @@ __device__ __forceinline__ void mma_bf16(float c[4], uint32_t a0, uint32_t a1, u
       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
+// ldmatrix: four (two) 8x8 b16 matrices from shared memory; lane i gives
+// the address of row i % 8 of matrix i / 8 (16 contiguous bytes, 16-byte
+// aligned), and receives the elements (row i / 4, columns 2 (i % 4) and
+// 2 (i % 4) + 1) of each matrix in order: the mma.sync fragment layout.
+__device__ __forceinline__ void ldsm_x4(uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3,
+                                        const void* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(a)
+               : "memory");
+}
+
+__device__ __forceinline__ void ldsm_x2(uint32_t& r0, uint32_t& r1, const void* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n"
+               : "=r"(r0), "=r"(r1)
+               : "r"(a)
+               : "memory");
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
   return *reinterpret_cast<uint32_t*>(&h);
@@ -306,6 +327,15 @@ ws_infer_kernel(const float* __restrict__ params, const float* __restrict__ vg,
     s.b2[tid] = bf16_round(params[kOffB2 + tid]);
   }
   if (tid == 0) s.b3 = bf16_round(params[kOffB3]);
+  __syncthreads();  // weights staged
+  // Layer 3's B fragments for its 18 k-steps (only output column 0 is used).
+  uint32_t b3[36];
+  {
+    const int bn = lane & 7, bkoff = ((lane >> 3) & 1) << 3;
+#pragma unroll
+    for (int ks = 0; ks < 18; ks++)
+      ldsm_x2(b3[2 * ks], b3[2 * ks + 1], &s.w3[bn * kW2S + ks * 16 + bkoff]);
+  }
   const int tiles_x = (W + kTX - 1) / kTX, tiles_y = (H + kTY - 1) / kTY;
   for (int tile = blockIdx.x; tile < tiles_x * tiles_y; tile += gridDim.x) {
     const int x0 = (tile % tiles_x) * kTX, y0 = (tile / tiles_x) * kTY;
@@ -370,56 +400,75 @@ ws_infer_kernel(const float* __restrict__ params, const float* __restrict__ vg,
     }
     __syncthreads();
     // Layer 2: M = 34x18 cells (39 m-tiles, the last one partly padding),
-    // K = 9 taps x 32 channels (18 k-steps), N = 32.
-    constexpr int kM2 = kA2X * kA2Y;
-    for (int mt = warp; mt < (kM2 + 15) / 16; mt += kInferWarps) {
-      float acc[4][4] = {};
-      const int r0 = mt * 16 + g, r1 = r0 + 8;
-      const int q0 = min(r0, kM2 - 1), q1 = min(r1, kM2 - 1);
-      const int p0 = (q0 / kA2X) * kA1X + q0 % kA2X, p1 = (q1 / kA2X) * kA1X + q1 % kA2X;
+    // K = 9 taps x 32 channels (18 k-steps), N = 32.  A and B fragments come
+    // from ldmatrix: the A rows are cells (the 16 channels of a k-step are
+    // 32 contiguous bytes of a cell), the B rows output channels.  A warp
+    // takes two m-tiles at a time so each k-step's B fragments serve both.
+    constexpr int kM2 = kA2X * kA2Y, kMT2 = (kM2 + 15) / 16;
+    {
+      const int arow = lane & 15, akoff = (lane >> 4) << 3;
+      const int bn = (lane & 7) + ((lane >> 4) << 3), bkoff = ((lane >> 3) & 1) << 3;
+      for (int mt = warp; mt < kMT2; mt += 2 * kInferWarps) {
+        const int mtb = mt + kInferWarps;
+        const bool two = mtb < kMT2;
+        const int ra = min(mt * 16 + arow, kM2 - 1), rb = min(mtb * 16 + arow, kM2 - 1);
+        const int pa = (ra / kA2X) * kA1X + ra % kA2X, pb = (rb / kA2X) * kA1X + rb % kA2X;
+        float acc[2][4][4] = {};
 #pragma unroll 2
-      for (int ks = 0; ks < 18; ks++) {
-        const int tap = ks >> 1, ci = (ks & 1) * 16 + 2 * tq;
-        const int off = (tap / 3) * kA1X + tap % 3;
-        const uint32_t a0 = ld32(&s.a1[(p0 + off) * kAS + ci]);
-        const uint32_t a1 = ld32(&s.a1[(p1 + off) * kAS + ci]);
-        const uint32_t a2 = ld32(&s.a1[(p0 + off) * kAS + ci + 8]);
-        const uint32_t a3 = ld32(&s.a1[(p1 + off) * kAS + ci + 8]);
+        for (int ks = 0; ks < 18; ks++) {
+          const int tap = ks >> 1, cb = (ks & 1) * 16;
+          const int off = (tap / 3) * kA1X + tap % 3;
+          uint32_t b[8];
+          ldsm_x4(b[0], b[1], b[2], b[3], &s.w2[bn * kW2S + ks * 16 + bkoff]);
+          ldsm_x4(b[4], b[5], b[6], b[7], &s.w2[(bn + 16) * kW2S + ks * 16 + bkoff]);
+          uint32_t a[4];
+          ldsm_x4(a[0], a[1], a[2], a[3], &s.a1[(pa + off) * kAS + cb + akoff]);
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-          const __nv_bfloat16* wb = &s.w2[(j * 8 + g) * kW2S + ks * 16 + 2 * tq];
-          mma_bf16(acc[j], a0, a1, a2, a3, ld32(wb), ld32(wb + 8));
+          for (int j = 0; j < 4; j++) mma_bf16(acc[0][j], a[0], a[1], a[2], a[3], b[2 * j], b[2 * j + 1]);
+          if (two) {
+            ldsm_x4(a[0], a[1], a[2], a[3], &s.a1[(pb + off) * kAS + cb + akoff]);
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+              mma_bf16(acc[1][j], a[0], a[1], a[2], a[3], b[2 * j], b[2 * j + 1]);
+          }
         }
-      }
 #pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int r = h ? r1 : r0;
-        if (r >= kM2) continue;
-        const int gy = y0 - 1 + r / kA2X, gx = x0 - 1 + r % kA2X;
-        const bool in = gx >= 0 && gy >= 0 && gx < W && gy < H;
+        for (int m = 0; m < 2; m++) {
+          if (m == 1 && !two) break;
+          const int r0 = (m ? mtb : mt) * 16 + g, r1 = r0 + 8;
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-          const int n = j * 8 + 2 * tq;
-          const float lo = in ? fmaxf(acc[j][2 * h] + s.b2[n], 0.0f) : 0.0f;
-          const float hi = in ? fmaxf(acc[j][2 * h + 1] + s.b2[n + 1], 0.0f) : 0.0f;
-          *reinterpret_cast<uint32_t*>(&s.a2[r * kAS + n]) = pack_bf16(lo, hi);
+          for (int h = 0; h < 2; h++) {
+            const int r = h ? r1 : r0;
+            if (r >= kM2) continue;
+            const int gy = y0 - 1 + r / kA2X, gx = x0 - 1 + r % kA2X;
+            const bool in = gx >= 0 && gy >= 0 && gx < W && gy < H;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+              const int n = j * 8 + 2 * tq;
+              const float lo = in ? fmaxf(acc[m][j][2 * h] + s.b2[n], 0.0f) : 0.0f;
+              const float hi = in ? fmaxf(acc[m][j][2 * h + 1] + s.b2[n + 1], 0.0f) : 0.0f;
+              *reinterpret_cast<uint32_t*>(&s.a2[r * kAS + n]) = pack_bf16(lo, hi);
+            }
+          }
         }
       }
     }
     __syncthreads();
-    // Layer 3: M = 32x16 outputs (32 m-tiles), K = 288, N = 8 (only column 0 used).
+    // Layer 3: M = 32x16 outputs (32 m-tiles), K = 288, N = 8 (only column 0
+    // used).  The B fragments of all 18 k-steps are the same for every
+    // m-tile and stay in registers (b3, loaded once per block).
     for (int mt = warp; mt < kTX * kTY / 16; mt += kInferWarps) {
       float acc[4] = {};
       const int r0 = mt * 16 + g, r1 = r0 + 8;
-      const int p0 = (r0 / kTX) * kA2X + r0 % kTX, p1 = (r1 / kTX) * kA2X + r1 % kTX;
-#pragma unroll 2
+      const int ar = mt * 16 + (lane & 15), akoff = (lane >> 4) << 3;
+      const int pa = (ar / kTX) * kA2X + ar % kTX;
+#pragma unroll
       for (int ks = 0; ks < 18; ks++) {
-        const int tap = ks >> 1, ci = (ks & 1) * 16 + 2 * tq;
+        const int tap = ks >> 1, cb = (ks & 1) * 16;
         const int off = (tap / 3) * kA2X + tap % 3;
-        const __nv_bfloat16* wb = &s.w3[g * kW2S + ks * 16 + 2 * tq];
-        mma_bf16(acc, ld32(&s.a2[(p0 + off) * kAS + ci]), ld32(&s.a2[(p1 + off) * kAS + ci]),
-                 ld32(&s.a2[(p0 + off) * kAS + ci + 8]), ld32(&s.a2[(p1 + off) * kAS + ci + 8]),
-                 ld32(wb), ld32(wb + 8));
+        uint32_t a[4];
+        ldsm_x4(a[0], a[1], a[2], a[3], &s.a2[(pa + off) * kAS + cb + akoff]);
+        mma_bf16(acc, a[0], a[1], a[2], a[3], b3[2 * ks], b3[2 * ks + 1]);
       }
       if (tq == 0) {
 #pragma unroll
