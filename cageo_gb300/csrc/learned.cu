@@ -345,18 +345,65 @@ ws_infer_kernel(const float* __restrict__ params, const float* __restrict__ vg,
       s.v[k] = (gx < 0 || gy < 0 || gx >= W || gy >= H) ? NAN : vg[(int64_t)gy * W + gx];
     }
     __syncthreads();
-    for (int k = tid; k < kFY * kFX; k += blockDim.x) {
-      const int fy = k / kFX, fx = k % kFX;
-      const float* c = &s.v[(fy + 3) * kVX + fx + 3];
-      float f[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-      if (*c == *c) {  // inside the grid
-        auto at = [&](int dy, int dx) { return c[dy * kVX + dx]; };
-        ws_features(*c, nodata, at, f);
+    // Features (ws_features), separably: first per elevation row and
+    // feature column the 7-wide minimum, maximum, sum and count of the
+    // valid cells and the 3-wide minimum, then the 7-high (3-high) column
+    // of those.  Minima and maxima equal ws_features' exactly; the mean's
+    // sum runs in another order (last bits).  The row results use the
+    // layer-1 buffer, which is free until layer 1 runs.
+    {
+      float* rmn7 = reinterpret_cast<float*>(s.a1);
+      float* rmx7 = rmn7 + kVY * kFX;
+      float* rsum = rmx7 + kVY * kFX;
+      float* rcnt = rsum + kVY * kFX;
+      float* rmn3 = rcnt + kVY * kFX;
+      for (int k = tid; k < kVY * kFX; k += blockDim.x) {
+        const int vy = k / kFX, fx = k - vy * kFX;
+        const float* r = &s.v[vy * kVX + fx];  // columns fx .. fx + 6 (centre fx + 3)
+        float mn = kInf, mx = -kInf, sm = 0.0f, m3 = kInf;
+        int cnt = 0;
+#pragma unroll
+        for (int dx = 0; dx < 7; dx++) {
+          const float e = r[dx];
+          if (e != e || e == nodata) continue;  // outside the grid or NODATA
+          mn = fminf(mn, e);
+          mx = fmaxf(mx, e);
+          sm = __fadd_rn(sm, e);
+          cnt++;
+          if (dx >= 2 && dx <= 4) m3 = fminf(m3, e);
+        }
+        rmn7[k] = mn;
+        rmx7[k] = mx;
+        rsum[k] = sm;
+        rcnt[k] = (float)cnt;
+        rmn3[k] = m3;
       }
-      uint2 pk;
-      pk.x = pack_bf16(f[0], f[1]);
-      pk.y = pack_bf16(f[2], f[3]);
-      *reinterpret_cast<uint2*>(&s.f[k * 4]) = pk;
+      __syncthreads();
+      for (int k = tid; k < kFY * kFX; k += blockDim.x) {
+        const int fy = k / kFX, fx = k - fy * kFX;
+        const float c = s.v[(fy + 3) * kVX + fx + 3];
+        float f[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (c == c && c != nodata) {  // inside the grid and not NODATA
+          float mn = kInf, mx = -kInf, sm = 0.0f, cn = 0.0f, m3 = kInf;
+#pragma unroll
+          for (int dy = 0; dy < 7; dy++) {
+            const int b = (fy + dy) * kFX + fx;
+            mn = fminf(mn, rmn7[b]);
+            mx = fmaxf(mx, rmx7[b]);
+            sm = __fadd_rn(sm, rsum[b]);
+            cn += rcnt[b];
+            if (dy >= 2 && dy <= 4) m3 = fminf(m3, rmn3[b]);
+          }
+          f[0] = __fsub_rn(c, m3);
+          f[1] = __fsub_rn(c, mn);
+          f[2] = __fsub_rn(mx, c);
+          f[3] = __fsub_rn(c, __fdiv_rn(sm, cn));
+        }
+        uint2 pk;
+        pk.x = pack_bf16(f[0], f[1]);
+        pk.y = pack_bf16(f[2], f[3]);
+        *reinterpret_cast<uint2*>(&s.f[k * 4]) = pk;
+      }
     }
     __syncthreads();
     // Layer 1: M = 36x20 cells (45 m-tiles), K = 9 taps x 4 features (3 k-steps), N = 32.
