@@ -243,7 +243,7 @@ constexpr int kA1X = kTX + 4, kA1Y = kTY + 4;    // layer-1 outputs
 constexpr int kA2X = kTX + 2, kA2Y = kTY + 2;    // layer-2 outputs
 constexpr int kAS = 40;                          // activation row stride (bf16), 80 B
 constexpr int kW1S = 56, kW2S = 296;             // weight row strides (bf16)
-constexpr int kInferWarps = 8;
+constexpr int kInferWarps = 16;
 
 struct InferSmem {
   float v[kVY * kVX];
