@@ -342,8 +342,10 @@ ws_infer_kernel(const float* __restrict__ params, const float* __restrict__ vg,
     __syncthreads();  // weights staged / previous tile done
     for (int k = tid; k < kVY * kVX; k += blockDim.x) {
       const int gy = y0 - 6 + k / kVX, gx = x0 - 6 + k % kVX;
-      s.v[k] = (gx < 0 || gy < 0 || gx >= W || gy >= H) ? NAN : vg[(int64_t)gy * W + gx];
+      if (gx < 0 || gy < 0 || gx >= W || gy >= H) s.v[k] = NAN;
+      else cp_async4(&s.v[k], vg + (int64_t)gy * W + gx);  // all in flight at once
     }
+    cp_async_wait();
     __syncthreads();
     // Features (ws_features), separably: first per elevation row and
     // feature column the 7-wide minimum, maximum, sum and count of the
@@ -505,7 +507,8 @@ ws_infer_kernel(const float* __restrict__ params, const float* __restrict__ vg,
     // used).  The B fragments of all 18 k-steps are the same for every
     // m-tile and stay in registers (b3, loaded once per block).
     for (int mt = warp; mt < kTX * kTY / 16; mt += kInferWarps) {
-      float acc[4] = {};
+      // Two accumulators (even and odd k-steps) halve the dependent chain.
+      float acc[4] = {}, acc2[4] = {};
       const int r0 = mt * 16 + g, r1 = r0 + 8;
       const int ar = mt * 16 + (lane & 15), akoff = (lane >> 4) << 3;
       const int pa = (ar / kTX) * kA2X + ar % kTX;
@@ -515,8 +518,10 @@ ws_infer_kernel(const float* __restrict__ params, const float* __restrict__ vg,
         const int off = (tap / 3) * kA2X + tap % 3;
         uint32_t a[4];
         ldsm_x4(a[0], a[1], a[2], a[3], &s.a2[(pa + off) * kAS + cb + akoff]);
-        mma_bf16(acc, a[0], a[1], a[2], a[3], b3[2 * ks], b3[2 * ks + 1]);
+        mma_bf16((ks & 1) ? acc2 : acc, a[0], a[1], a[2], a[3], b3[2 * ks], b3[2 * ks + 1]);
       }
+#pragma unroll
+      for (int q = 0; q < 4; q++) acc[q] += acc2[q];
       if (tq == 0) {
 #pragma unroll
         for (int h = 0; h < 2; h++) {
