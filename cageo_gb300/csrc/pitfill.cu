@@ -708,6 +708,23 @@ fill_flood_kernel(FloodArgs a) {
   }
 }
 
+// fill_passable() of a quantized value q = RN(k / 1000) (k an integer, as
+// fill_quantize makes every value the fill sees).  With minE = 0 and
+// 0 <= q < 4096, p = RN(1000 q) lies within 0.25 of k: |q - k/1000| is at
+// most half an ulp of q (<= 2^-13), so |1000 q - k| <= 0.123, and rounding
+// 1000 q (< 2^22) moves it by at most 0.125.  Then toIndex(q) = trunc(p)
+// equals k exactly when p >= k = rint(p), and toElev(k) = RN(k / 1000) = q,
+// while toElev of any other index differs from q (values 0.001 apart are
+// distinct floats below 8192): passable <=> p >= rint(p), no division.
+// Other values take the general test.
+__device__ __forceinline__ bool passable_quantized(float q, float minE) {
+  if (minE == 0.0f && q >= 0.0f && q < 4096.0f) {
+    const float p = __fmul_rn(1000.0f, q);
+    return p >= rintf(p);
+  }
+  return fill_passable(q, minE);
+}
+
 // Cells per thread of the elementwise fill kernels (fewer, longer blocks).
 constexpr int kCellsPerThread = 4;
 
@@ -729,7 +746,7 @@ __global__ void fill_init_kernel(const float* __restrict__ q, float* __restrict_
     if (qv == nodata) {
       f = FNODATA;
     } else {
-      if (!fill_passable(qv, minE)) f |= FNONPASS;
+      if (!passable_quantized(qv, minE)) f |= FNONPASS;
       if (x == 0 || y == 0 || x == W - 1 || y == H - 1 || qv == 0.0f) f |= FOUTLET;
     }
     F[i] = f;
