@@ -13,6 +13,7 @@ pair per step, each (tile, realization) used once.
 Usage (on a GPU):
     python -m cageo_gb300.learned train --steps 2000 --out params.npy
     python -m cageo_gb300.learned evaluate --params params.npy
+    python -m cageo_gb300.learned infer --size 2048 --repeat 3   # time the inference
 """
 import argparse
 import json
@@ -161,9 +162,30 @@ def evaluate(params, source=None, pairs=8, first_realization=1000,
     return dict(cells=cells, pairs=pairs, thresholds=rows, sweeps=sweep)
 
 
+def time_inference(params=None, size=2048, repeat=3, threshold=0.005, seed=3):
+    """Runs the fused inference `repeat` times on a seeded size x size fBm
+    grid (after one untimed call); returns (ms per call, share of cells
+    started at +inf)."""
+    import torch
+    dem = synth.fbm_dem(size, size, 0.8, seed, 0.0, 300.0 * (size / 8192.0) ** 0.8)
+    v = torch.from_numpy(dem).cuda()
+    p = torch.from_numpy(np.asarray(params if params is not None else load_params(),
+                                    np.float32)).cuda()
+    warm, _ = api.ws_infer(p, v, threshold)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(repeat):
+        warm, _ = api.ws_infer(p, v, threshold)
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / repeat, float(warm.isinf().float().mean())
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("cmd", choices=["train", "evaluate"])
+    ap.add_argument("cmd", choices=["train", "evaluate", "infer"])
+    ap.add_argument("--size", type=int, default=2048)
+    ap.add_argument("--repeat", type=int, default=3)
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--tiles", type=int, default=40)
     ap.add_argument("--cap", type=float, default=2.0)
@@ -171,6 +193,10 @@ def main():
     ap.add_argument("--params", default=DEFAULT_PARAMS)
     ap.add_argument("--pairs", type=int, default=8)
     a = ap.parse_args()
+    if a.cmd == "infer":
+        ms, wet = time_inference(load_params(a.params), a.size, a.repeat)
+        print(json.dumps({"size": a.size, "ms_per_inference": ms, "wet_start_share": wet}))
+        return
     src = PairSource(tiles=a.tiles, cap=a.cap)
     if a.cmd == "train":
         params, hist = train(a.steps, source=src)
