@@ -43,10 +43,12 @@ __global__ void noise_kernel(float* __restrict__ out, int64_t n, uint32_t k0,
   float v[4];
 #pragma unroll
   for (int j = 0; j < 4; j++) v[j] = __fadd_rn(mean, __fmul_rn(z[j], sd));
-  if (base + 4 <= n) {
+  // One float4 store when the field is 16-byte aligned (a caller's buffer
+  // may start at any 4-byte boundary: then four scalar stores).
+  if (base + 4 <= n && (((uintptr_t)out) & 15u) == 0) {
     *reinterpret_cast<float4*>(out + base) = make_float4(v[0], v[1], v[2], v[3]);
   } else {
-    for (int j = 0; base + j < n; j++) out[base + j] = v[j];
+    for (int j = 0; j < 4 && base + j < n; j++) out[base + j] = v[j];
   }
 }
 

@@ -590,34 +590,44 @@ fill_flood_kernel(FloodArgs a) {
       if (!cand_built) {
         t_conv = global_ns();
         if (blockIdx.x == 0 && threadIdx.x == 0) vs[S_PASSES_B] = (unsigned int)(p - p0 + 1);
-        // Four cells per thread and iteration (independent loads); the
-        // arrays are 256-byte aligned so the vector loads are aligned.
-        for (int64_t b4 = tid0 * 4; b4 < ncell; b4 += tstride * 4) {
-          uint8_t fv[4];
-          float wav[4], wbv[4];
-          if (b4 + 4 <= ncell) {
-            const uchar4 f4 = *reinterpret_cast<const uchar4*>(w.flags + b4);
-            const uint4 a4 = *reinterpret_cast<const uint4*>(w.aux + b4);
-            const float4 w4 = *reinterpret_cast<const float4*>(a.Wg + b4);
-            fv[0] = f4.x; fv[1] = f4.y; fv[2] = f4.z; fv[3] = f4.w;
-            wav[0] = __uint_as_float(a4.x); wav[1] = __uint_as_float(a4.y);
-            wav[2] = __uint_as_float(a4.z); wav[3] = __uint_as_float(a4.w);
-            wbv[0] = w4.x; wbv[1] = w4.y; wbv[2] = w4.z; wbv[3] = w4.w;
-          } else {
-            for (int k = 0; k < 4; k++) {
-              const bool in = b4 + k < ncell;
-              fv[k] = in ? w.flags[b4 + k] : FNODATA;
-              wav[k] = in ? __uint_as_float(w.aux[b4 + k]) : 0.0f;
-              wbv[k] = in ? a.Wg[b4 + k] : 0.0f;
+        // Undecided cells, 16 per thread and iteration: four groups of 4
+        // cells a grid-stride apart (each group one coalesced vector load per
+        // array), all loaded before any is classified so that four loads per
+        // array are in flight.  The flags and flood-A values live in the
+        // 256-byte aligned workspace; the filled grid is the caller's and is
+        // read as float4 only when it is 16-byte aligned.
+        const bool wvec = (((uintptr_t)a.Wg) & 15u) == 0;
+        for (int64_t b = tid0; b * 4 < ncell; b += 4 * tstride) {
+          uint8_t fv[16];
+          float wav[16], wbv[16];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const int64_t b4 = (b + u * tstride) * 4;
+            if (b4 + 4 <= ncell && wvec) {
+              const uchar4 f4 = *reinterpret_cast<const uchar4*>(w.flags + b4);
+              const uint4 a4 = *reinterpret_cast<const uint4*>(w.aux + b4);
+              const float4 w4 = *reinterpret_cast<const float4*>(a.Wg + b4);
+              fv[4 * u] = f4.x; fv[4 * u + 1] = f4.y; fv[4 * u + 2] = f4.z; fv[4 * u + 3] = f4.w;
+              wav[4 * u] = __uint_as_float(a4.x); wav[4 * u + 1] = __uint_as_float(a4.y);
+              wav[4 * u + 2] = __uint_as_float(a4.z); wav[4 * u + 3] = __uint_as_float(a4.w);
+              wbv[4 * u] = w4.x; wbv[4 * u + 1] = w4.y; wbv[4 * u + 2] = w4.z; wbv[4 * u + 3] = w4.w;
+            } else {
+#pragma unroll
+              for (int k = 0; k < 4; k++) {
+                const bool in = b4 + k < ncell;
+                fv[4 * u + k] = in ? w.flags[b4 + k] : FNODATA;
+                wav[4 * u + k] = in ? __uint_as_float(w.aux[b4 + k]) : 0.0f;
+                wbv[4 * u + k] = in ? a.Wg[b4 + k] : 0.0f;
+              }
             }
           }
 #pragma unroll
-          for (int k = 0; k < 4; k++) {
+          for (int k = 0; k < 16; k++) {
             const uint8_t f = fv[k];
             const bool unsure = !(f & (FNODATA | FOUTLET)) &&
                                 (wav[k] != wbv[k] ||
                                  ((f & FNONPASS) && (((f & FBELOWA) != 0) != ((f & FBELOW) != 0))));
-            const int64_t i = b4 + k;
+            const int64_t i = (b + (k >> 2) * tstride) * 4 + (k & 3);
             if (unsure) {
               w.flags[i] = f | FUNSURE;
               w.aux[i] = (uint32_t)i;

@@ -80,6 +80,30 @@ def test_pitfill_unaligned_grids(cuda, oracle):
     with pytest.raises(api.CageoError) as e:
         api.pitfill(_t(rdem, cuda), workspace=ws)
     assert e.value.status == 1 and "256-byte" in str(e.value)  # CAGEO_ERR_ARGUMENT
+    # The filled grid off a 16-byte boundary too, through the C ABI.
+    d2 = _t(rdem, cuda)
+    fbuf = torch.empty(W * H + 1, dtype=torch.float32, device=cuda)
+    f2 = fbuf[1:].view(H, W)
+    assert f2.data_ptr() % 16 == 4
+    st = api.lib().cageo_pitfill(api._ptr(d2), api._ptr(f2), W, H, -9999.0, api.FILL_CPU_COMPAT,
+                                 None, 0, api._stream())
+    assert st == 0, api.lib().cageo_last_error_string()
+    assert np.array_equal(bits(f2.cpu().numpy()), bits(f_ref)), "filled DEM (unaligned output)"
+
+
+def test_noise_into_unaligned_field(cuda):
+    """Noise written to a field that starts 4 bytes past a 16-byte boundary
+    equals the noise written to an aligned one."""
+    import torch
+    from cageo_gb300 import api
+    W, H = 301, 77
+    a = torch.empty((H, W), dtype=torch.float32, device=cuda)
+    api.noise_philox(a, 91, 4, 0.5, 1.5)
+    buf = torch.empty(W * H + 1, dtype=torch.float32, device=cuda)
+    b = buf[1:].view(H, W)
+    assert b.data_ptr() % 16 == 4
+    api.noise_philox(b, 91, 4, 0.5, 1.5)
+    assert torch.equal(a, b)
 
 
 @pytest.mark.parametrize("realization", range(4))
