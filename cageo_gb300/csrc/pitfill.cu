@@ -86,9 +86,8 @@ constexpr int kRS = 35;           // relay row stride (34 used)
 constexpr int kWS = 33;           // W/q row stride
 constexpr int kFS = 36;           // flag row stride (bytes)
 
-// Per-warp staged tile: relay values with halo, W and flags of the tile's
-// own cells.  q is static during a flood and is read through the read-only
-// cache instead of being staged.
+// Per-warp staged tile: relay values of the tile and its one-cell halo,
+// and (W, q) pairs and flags of the tile's own cells.
 struct WarpSmem {
   float R[34 * kRS];
   float2 WQ[kTile * kWS];  // (W, q) of the tile's own cells
