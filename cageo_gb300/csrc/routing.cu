@@ -233,10 +233,10 @@ __device__ void flat_tile(FlatSmem& s, const float* __restrict__ dem, int* fd, c
   // its distance; old values inside the tile came from halo values that can
   // only have dropped since, so they are never below the new ones.
   //
-  // Only cells on the tile's rim or next to a non-flat cell of the tile can
-  // be seeds.  Inside the rim a seed's non-flat neighbours are all inside
-  // the tile, where the least relay is 0 (an exit), so inner seeds are all
-  // at level 1.  Rim seeds are held one per lane: the top and bottom rows by
+  // Only cells on the tile's rim or next to an exit of the tile (a non-flat
+  // cell with relay 0) can be seeds.  Inside the rim a seed's non-flat
+  // neighbours are all inside the tile, where the least relay is 0 (an exit)
+  // or none, so inner seeds are all at level 1.  Rim seeds are held one per lane: the top and bottom rows by
   // column (lane = x), the left and right columns by row (lane = y, rows
   // 1..30); each level's seed masks then come from two ballots.
   unsigned int fup = __shfl_up_sync(0xffffffffu, flat, 1);
