@@ -49,11 +49,12 @@ PIPE_BYTES = 75
 # ncu capture of the 4096^2 workload (1681 MB for 16.8 M cells), applied
 # per cell to the benchmark grid.
 FILL_TRAFFIC_PER_CELL = 1680.6e6 / (4096 * 4096)
-# Kernels per realization on the graph path: fill 6 (scalars, init, two
-# floods, classify, final), noise 1, front 1, routing 4 (scalars, d8, flat
-# relaxation, flat directions), tracing 3 (scalars, init, jump), border
-# (which also writes the labels) 1, realization end 1.
-KERNELS_PER_REALIZATION = 17
+# Kernels per realization on the graph path: fill 10 (scalars, init, flood
+# A, classify, flood B's main drain, undecided cells, union, flatten, flood
+# B's confirmation phases, final), noise 1, front 1, routing 4 (scalars,
+# d8, flat relaxation, flat directions), tracing 3 (scalars, init, jump),
+# border (which also writes the labels) 1, realization end 1.
+KERNELS_PER_REALIZATION = 21
 
 
 def peak_hbm():

@@ -143,6 +143,10 @@ struct FloodArgs {
   const float* q;
   float* Wg;
   FillWork w;
+  // Flood B runs as two launches: 1 = seeding and the main drain, 2 = the
+  // confirmation phases (the undecided cells found and labelled by plain
+  // kernels in between).  Flood A ignores it.
+  int stage = 0;
 };
 
 // ---- asynchronous tile work queue ---------------------------------------
@@ -543,15 +547,13 @@ fill_flood_kernel(FloodArgs a) {
   const unsigned int nblocks = gridDim.x;
   const int gwarp = blockIdx.x * kWarps + warp, nwarps = gridDim.x * kWarps;
   const int ntiles = w.tiles_x * w.tiles_y;
-  const int64_t ncell = (int64_t)w.W * w.H;
   GridSync gs{w.scal + S_BAR_COUNT, w.scal + S_BAR_GEN, (int*)(w.scal + S_ERR)};
   volatile unsigned int* vs = w.scal;
   const int p0 = (int)vs[S_PASS] + 2;
   int p = p0;
-  bool cand_built = false;
   int ph = 0;
+  const bool phases = MODE == 1 && a.stage == 2;
   const unsigned long long t_start = global_ns();
-  unsigned long long t_conv = 0;
   // Seed the queue with the tiles that hold a relaying outlet (a tile
   // without one cannot change before a neighbour does, which queues it),
   // one 2x2 parity class of tiles after another with a grid barrier in
@@ -561,7 +563,7 @@ fill_flood_kernel(FloodArgs a) {
   // queue (2048^2 realization, 1/29 of the tiles in flight) this took the
   // visits per tile from 3.19 in plain tile order to 2.68.
   bool go = true;
-  for (int c = 0; c < 4 && go; c++) {
+  for (int c = 0; c < 4 && go && !phases; c++) {
     for (int i = gwarp; i < ntiles; i += nwarps) {
       const int tx = i % w.tiles_x, ty = i / w.tiles_x;
       if (lane == 0 && ((tx & 1) | ((ty & 1) << 1)) == c && w.tseed[i]) enqueue(w, i);
@@ -572,91 +574,22 @@ fill_flood_kernel(FloodArgs a) {
     const bool drained = drain<MODE>(s, a, lane, ntiles);
     if (!grid_barrier(gs, nblocks) || !drained) break;
     {
-      if (MODE == 0) break;
+      if (!phases) break;  // flood A, or flood B's main drain
       // The queue is empty (abandoned tickets aside): restart its positions.
       // No push comes before the next grid barrier.
       if (blockIdx.x == 0 && threadIdx.x == 0) {
         vs[S_HEAD] = 0u;
         vs[S_TAIL] = 0u;
       }
-      // ---- confirmation phases ----
+      // ---- confirmation phase ----
       // Flood A gave a lower bound (W_A in aux, FBELOWA), flood B an upper
       // bound (Wg, FBELOW).  Where they agree the cell is final; the
-      // undecided cells form 8-connected components that no later change
-      // can leave, so each component takes its own phase minimum.
+      // undecided cells (listed in cand, labelled by component in aux by
+      // the kernels between the two flood B launches) form 8-connected
+      // components that no later change can leave, so each component takes
+      // its own phase minimum.
       const int64_t tid0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
       const int64_t tstride = (int64_t)gridDim.x * blockDim.x;
-      if (!cand_built) {
-        t_conv = global_ns();
-        if (blockIdx.x == 0 && threadIdx.x == 0) vs[S_PASSES_B] = (unsigned int)(p - p0 + 1);
-        // Undecided cells, 16 per thread and iteration: four groups of 4
-        // cells a grid-stride apart (each group one coalesced vector load per
-        // array), all loaded before any is classified so that four loads per
-        // array are in flight.  The flags and flood-A values live in the
-        // 256-byte aligned workspace; the filled grid is the caller's and is
-        // read as float4 only when it is 16-byte aligned.
-        const bool wvec = (((uintptr_t)a.Wg) & 15u) == 0;
-        for (int64_t b = tid0; b * 4 < ncell; b += 4 * tstride) {
-          uint8_t fv[16];
-          float wav[16], wbv[16];
-#pragma unroll
-          for (int u = 0; u < 4; u++) {
-            const int64_t b4 = (b + u * tstride) * 4;
-            if (b4 + 4 <= ncell && wvec) {
-              const uchar4 f4 = *reinterpret_cast<const uchar4*>(w.flags + b4);
-              const uint4 a4 = *reinterpret_cast<const uint4*>(w.aux + b4);
-              const float4 w4 = *reinterpret_cast<const float4*>(a.Wg + b4);
-              fv[4 * u] = f4.x; fv[4 * u + 1] = f4.y; fv[4 * u + 2] = f4.z; fv[4 * u + 3] = f4.w;
-              wav[4 * u] = __uint_as_float(a4.x); wav[4 * u + 1] = __uint_as_float(a4.y);
-              wav[4 * u + 2] = __uint_as_float(a4.z); wav[4 * u + 3] = __uint_as_float(a4.w);
-              wbv[4 * u] = w4.x; wbv[4 * u + 1] = w4.y; wbv[4 * u + 2] = w4.z; wbv[4 * u + 3] = w4.w;
-            } else {
-#pragma unroll
-              for (int k = 0; k < 4; k++) {
-                const bool in = b4 + k < ncell;
-                fv[4 * u + k] = in ? w.flags[b4 + k] : FNODATA;
-                wav[4 * u + k] = in ? __uint_as_float(w.aux[b4 + k]) : 0.0f;
-                wbv[4 * u + k] = in ? a.Wg[b4 + k] : 0.0f;
-              }
-            }
-          }
-#pragma unroll
-          for (int k = 0; k < 16; k++) {
-            const uint8_t f = fv[k];
-            const bool unsure = !(f & (FNODATA | FOUTLET)) &&
-                                (wav[k] != wbv[k] ||
-                                 ((f & FNONPASS) && (((f & FBELOWA) != 0) != ((f & FBELOW) != 0))));
-            const int64_t i = (b + (k >> 2) * tstride) * 4 + (k & 3);
-            if (unsure) {
-              w.flags[i] = f | FUNSURE;
-              w.aux[i] = (uint32_t)i;
-            }
-            const unsigned int pos = warp_append(&w.scal[S_CAND], unsure);
-            if (unsure) w.cand[pos] = (uint32_t)i;
-          }
-        }
-        if (!grid_barrier(gs, nblocks)) break;
-        const unsigned int nu = vs[S_CAND];
-        bool ok = true;
-        for (int64_t j = tid0; j < nu; j += tstride) {
-          uint32_t c = w.cand[j];
-          int cx = (int)(c % (uint32_t)w.W), cy = (int)(c / (uint32_t)w.W);
-          for (int k = 0; k < 4; k++) {  // W, NW, N, NE: each pair once
-            int nx = cx + (k == 0 ? -1 : k - 2), ny = cy + (k == 0 ? 0 : -1);
-            if (nx < 0 || ny < 0 || nx >= w.W) continue;
-            uint32_t n = (uint32_t)ny * (uint32_t)w.W + (uint32_t)nx;
-            if (w.flags[n] & FUNSURE) ok &= uf_unite(w.aux, c, n);
-          }
-        }
-        if (!ok) atomicCAS((int*)(w.scal + S_ERR), 0, 2);
-        if (!grid_barrier(gs, nblocks)) break;
-        for (int64_t j = tid0; j < nu; j += tstride) {
-          uint32_t c = w.cand[j];
-          w.aux[c] = uf_find(w.aux, c);
-        }
-        cand_built = true;
-        if (!grid_barrier(gs, nblocks)) break;
-      }
       const unsigned int nu = vs[S_CAND];
       if (blockIdx.x == 0 && threadIdx.x == 0) vs[S_PEND + (ph + 1) % 3] = 0u;
       for (int64_t j = tid0; j < nu; j += tstride) {
@@ -704,15 +637,16 @@ fill_flood_kernel(FloodArgs a) {
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     vs[S_PASS] = (unsigned int)p;
-    const unsigned long long t_end = global_ns();
+    const unsigned int us = (unsigned int)((global_ns() - t_start) / 1000);
     if (MODE == 0) {
       vs[S_PASSES_A] = (unsigned int)(p - p0 + 1);
-      vs[S_US_A] = (unsigned int)((t_end - t_start) / 1000);
+      vs[S_US_A] = us;
+    } else if (!phases) {
+      vs[S_PASSES_B] = (unsigned int)(p - p0 + 1);
+      vs[S_US_B] = us;
     } else {
       vs[S_PHASES] = (unsigned int)ph;
-      if (!t_conv) t_conv = t_end;
-      vs[S_US_B] = (unsigned int)((t_conv - t_start) / 1000);
-      vs[S_US_P] = (unsigned int)((t_end - t_conv) / 1000);
+      vs[S_US_P] = us;
     }
   }
 }
@@ -823,6 +757,83 @@ __global__ void fill_classify_kernel(float* __restrict__ Wg, uint8_t* __restrict
   }
 }
 
+// Between flood B's two launches: the undecided cells -- flood A's lower
+// bound (aux) and flood B's upper bound (Wg) differ in value, or in the
+// blocked status of a non-passable cell -- are flagged FUNSURE, labelled
+// with their own index and appended to the candidate list.  Four cells per
+// thread; the filled grid is the caller's and is read as float4 only when
+// it is 16-byte aligned.
+__global__ void fill_undecided_kernel(const float* __restrict__ Wg, uint8_t* __restrict__ F,
+                                      uint32_t* __restrict__ aux, uint32_t* __restrict__ cand,
+                                      unsigned int* scal, int64_t n) {
+  const int64_t b4 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+  if (b4 >= n) return;
+  uint8_t fv[4];
+  float wav[4], wbv[4];
+  if (b4 + 4 <= n && (((uintptr_t)Wg) & 15u) == 0) {
+    const uchar4 f4 = *reinterpret_cast<const uchar4*>(F + b4);
+    const uint4 a4 = *reinterpret_cast<const uint4*>(aux + b4);
+    const float4 w4 = *reinterpret_cast<const float4*>(Wg + b4);
+    fv[0] = f4.x; fv[1] = f4.y; fv[2] = f4.z; fv[3] = f4.w;
+    wav[0] = __uint_as_float(a4.x); wav[1] = __uint_as_float(a4.y);
+    wav[2] = __uint_as_float(a4.z); wav[3] = __uint_as_float(a4.w);
+    wbv[0] = w4.x; wbv[1] = w4.y; wbv[2] = w4.z; wbv[3] = w4.w;
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const bool in = b4 + k < n;
+      fv[k] = in ? F[b4 + k] : FNODATA;
+      wav[k] = in ? __uint_as_float(aux[b4 + k]) : 0.0f;
+      wbv[k] = in ? Wg[b4 + k] : 0.0f;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const uint8_t f = fv[k];
+    const bool unsure = !(f & (FNODATA | FOUTLET)) &&
+                        (wav[k] != wbv[k] ||
+                         ((f & FNONPASS) && (((f & FBELOWA) != 0) != ((f & FBELOW) != 0))));
+    const int64_t i = b4 + k;
+    if (unsure) {
+      F[i] = f | FUNSURE;
+      aux[i] = (uint32_t)i;
+    }
+    const unsigned int pos = warp_append(&scal[S_CAND], unsure);
+    if (unsure) cand[pos] = (uint32_t)i;
+  }
+}
+
+// Union of undecided neighbours (W, NW, N, NE: each pair once) into
+// 8-connected components; labels in aux.
+__global__ void fill_unite_kernel(const uint32_t* __restrict__ cand, unsigned int* scal,
+                                  const uint8_t* __restrict__ F, uint32_t* aux, int W) {
+  const unsigned int nu = ((volatile unsigned int*)scal)[S_CAND];
+  bool ok = true;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nu;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = cand[j];
+    const int cx = (int)(c % (uint32_t)W), cy = (int)(c / (uint32_t)W);
+    for (int k = 0; k < 4; k++) {
+      const int nx = cx + (k == 0 ? -1 : k - 2), ny = cy + (k == 0 ? 0 : -1);
+      if (nx < 0 || ny < 0 || nx >= W) continue;
+      const uint32_t nb = (uint32_t)ny * (uint32_t)W + (uint32_t)nx;
+      if (F[nb] & FUNSURE) ok &= uf_unite(aux, c, nb);
+    }
+  }
+  if (!ok) atomicCAS((int*)(scal + S_ERR), 0, 2);
+}
+
+// Every undecided cell's label becomes its component's root.
+__global__ void fill_flatten_kernel(const uint32_t* __restrict__ cand,
+                                    const unsigned int* scal, uint32_t* aux) {
+  const unsigned int nu = ((const volatile unsigned int*)scal)[S_CAND];
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nu;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = cand[j];
+    aux[c] = uf_find(aux, c);
+  }
+}
+
 __global__ void fill_final_kernel(const float* __restrict__ q, float* __restrict__ Wg,
                                   int64_t n) {
 #pragma unroll
@@ -912,6 +923,16 @@ cageo_status fill_run(const float* q, float* filled, const FillWork& w, float no
   CAGEO_CUDA(cudaGetLastError());
   CAGEO_CUDA(cudaMemsetAsync(w.queued, 0, sizeof(int) * nt, s));  // all idle
   CAGEO_CUDA(cudaMemsetAsync(w.tconv, 0, nt, s));
+  a.stage = 1;  // flood B's main drain
+  st = launch_flood<1>(a, s);
+  if (st) return st;
+  const unsigned vblocks = (unsigned)((n + 4 * 256 - 1) / (4 * 256));
+  fill_undecided_kernel<<<vblocks, 256, 0, s>>>(filled, w.flags, w.aux, w.cand, w.scal, n);
+  const unsigned ublocks = (unsigned)std::min<int64_t>((n + 255) / 256, 2048);
+  fill_unite_kernel<<<ublocks, 256, 0, s>>>(w.cand, w.scal, w.flags, w.aux, w.W);
+  fill_flatten_kernel<<<ublocks, 256, 0, s>>>(w.cand, w.scal, w.aux);
+  CAGEO_CUDA(cudaGetLastError());
+  a.stage = 2;  // the confirmation phases
   st = launch_flood<1>(a, s);
   if (st) return st;
   fill_final_kernel<<<blocks, 256, 0, s>>>(q, filled, n);
