@@ -45,10 +45,10 @@ FALLBACK_HBM = 6800.0
 # Algorithmic bytes per cell of each stage (unfused compulsory I/O).
 STAGE_BYTES = {"noise": 4, "front": 40, "fill": 8, "route": 5, "trace": 6, "border": 12}
 PIPE_BYTES = 75
-# DRAM bytes per cell moved by one pit fill (both flood launches), from an
-# ncu capture of the 4096^2 workload (1681 MB for 16.8 M cells), applied
+# DRAM bytes per cell moved by one pit fill (its three flood launches), from an
+# ncu capture of the 4096^2 workload (1552 MB for 16.8 M cells), applied
 # per cell to the benchmark grid.
-FILL_TRAFFIC_PER_CELL = 1680.6e6 / (4096 * 4096)
+FILL_TRAFFIC_PER_CELL = 1552.0e6 / (4096 * 4096)
 # Kernels per realization on the graph path: fill 10 (scalars, init, flood
 # A, classify, flood B's main drain, undecided cells, union, flatten, flood
 # B's confirmation phases, final), noise 1, front 1, routing 4 (scalars,
