@@ -35,6 +35,36 @@ def test_argument_checks_refuse_before_device_work():
     assert not p.value
 
 
+def test_mode_and_workspace_checks_refuse_before_device_work():
+    """Unknown modes, aliasing outputs, and caller workspaces that are too
+    small or off their 256-byte boundary are refused on the host."""
+    L = api.lib()
+    a, b, c = P(4096), P(8192), P(12288)  # never dereferenced
+    assert L.cageo_route_d8_mode(a, b, c, 10, 10, -9999.0, 5, None, 0, None) == 1
+    assert "routing mode" in _err()
+    assert L.cageo_trace_mode(a, b, c, 10, 10, 7, None, 0, None) == 1 and "tracing mode" in _err()
+    assert L.cageo_pitfill_exact_warm(a, b, b, 10, 10, -9999.0, None, 0, None, None) == 1
+    assert "alias" in _err()
+    need = L.cageo_pitfill_workspace_size(64, 64)
+    assert L.cageo_pitfill(a, b, 64, 64, -9999.0, 0, P(1 << 20), need - 1, None) == 1
+    assert "smaller" in _err()
+    assert L.cageo_pitfill(a, b, 64, 64, -9999.0, 0, P((1 << 20) + 4), need, None) == 1
+    assert "256-byte" in _err()
+    need_t = L.cageo_trace_workspace_size(64, 64)
+    assert L.cageo_trace_mode(a, b, c, 64, 64, 0, P((1 << 20) + 64), need_t, None) == 1
+    assert "256-byte" in _err()
+    cfg = api.PipelineConfig(64, 64, 10.0, 1, 60.0, 0.0, 1.0, 2, -9999.0, -9999.0, 1, 1, 0)
+    p = P()
+    for field, bad, word in (("bevel_radius", 6, "bevel"), ("fill_mode", 2, "fill mode"),
+                             ("width", 1, "grid size"), ("height", 70000, "65535")):
+        good = getattr(cfg, field)
+        setattr(cfg, field, bad)
+        assert L.cageo_pipeline_create(ctypes.byref(p), ctypes.byref(cfg), a, b) == 1, field
+        assert word in _err(), (field, _err())
+        setattr(cfg, field, good)
+    assert not p.value
+
+
 def test_workspace_sizes_scale_with_grid():
     L = api.lib()
     s1, s2 = L.cageo_pitfill_workspace_size(512, 512), L.cageo_pitfill_workspace_size(1024, 1024)
