@@ -33,7 +33,8 @@ def _numpy_filter(model, rng_m, cell, r):
 def test_header_symbols_exported():
     from cageo_gb300 import _build
     lib = ctypes.CDLL(_build.LIB)
-    decl = open(os.path.join(ROOT, "include", "cageo.h")).read()
+    with open(os.path.join(ROOT, "include", "cageo.h")) as f:
+        decl = f.read()
     names = set(re.findall(r"\b(cageo_[a-z0-9_]+)\s*\(", decl))
     assert len(names) > 20
     missing = [n for n in sorted(names) if not hasattr(lib, n)]
