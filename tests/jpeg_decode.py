@@ -59,7 +59,8 @@ def _extend(v, n):
 
 
 def decode(path):
-    data = open(path, "rb").read()
+    with open(path, "rb") as f:
+        data = f.read()
     assert data[:2] == b"\xff\xd8", "SOI"
     i, q, tables, W, H = 2, None, {}, None, None
     while True:

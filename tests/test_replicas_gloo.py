@@ -46,7 +46,7 @@ def _worker(rank, world, port, out):
 def test_gloo_world2_count_sum():
     import torch.multiprocessing as mp
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.start_processes(_worker, args=(2, port, out), nprocs=2, join=True, start_method="spawn")
         expect = float(sum(k + 1 for k in range(10)))
