@@ -53,6 +53,29 @@ class InjectedConvolution : public ConvolutionAlgorithm_CPU_OpenMP<float> {
   }
 };
 
+// The reference allocates its 121-entry search-offset table with new[]
+// (src/streamburning/StreamBurningAlgorithm.h:121-128,
+// src/framework/ManagedData.h:638) and its generator writes only the offsets
+// within the bevel radius (:143-166); the burn loop stops at the first (0,0)
+// entry (src/streamburning/StreamBurningAlgorithmCPUOpenMP.h:57-60).  The
+// entries after the last offset are therefore whatever the heap held, and in
+// a long-lived process the loop can run on into stale offsets.  This subclass
+// allocates the table itself, zero-filled (what fresh memory holds), and lets
+// the reference's own generator write the offsets; execute() then finds the
+// table present and uses it.
+class ZeroTailBurning : public StreamBurningAlgorithm_CPU_OpenMP<float, float> {
+ public:
+  explicit ZeroTailBurning(int bevel) {
+    this->setBevelRadius(bevel);
+    this->circularSearchArray =
+        ManagedDataFactory::create<CoordOffset>(MAX_CIRCULAR_ARRAY_SIZE, HOST);
+    this->circularSearchArray->allocateData();
+    std::memset((void*)this->circularSearchArray->getData(), 0,
+                sizeof(CoordOffset) * MAX_CIRCULAR_ARRAY_SIZE);
+    this->generateCircularSearchArray(this->circularSearchArray->getData(), bevel);
+  }
+};
+
 template <typename G>
 void load(G& g, const void* src, size_t bytes) {
   std::memcpy((void*)g.getData(), src, bytes);
@@ -92,8 +115,7 @@ void ref_stream_burn(float* dem, const float* streams, int W, int H, int bevel,
   load(d, dem, sizeof(float) * W * H);
   StreamData_t s(d, AS_TEMPLATE);
   load(s, streams, sizeof(float) * W * H);
-  StreamBurningAlgorithm_CPU_OpenMP<float, float> alg;
-  alg.setBevelRadius(bevel);
+  ZeroTailBurning alg(bevel);
   alg.setNoDataValueDEM(nodata_dem);
   alg.setNoDataValueStream(nodata_stream);
   alg.execute(&d, &s);
