@@ -16,7 +16,6 @@
 //    (src/randomfield/RandomFieldAlgorithmCPUOpenMP.h:47-76).
 #include <cstring>
 #include <cstdint>
-#include <malloc.h>
 
 #include "AbstractFactory.h"
 #include "GlobalParameters.h"
@@ -73,6 +72,26 @@ class ZeroTailBurning : public StreamBurningAlgorithm_CPU_OpenMP<float, float> {
     std::memset((void*)this->circularSearchArray->getData(), 0,
                 sizeof(CoordOffset) * MAX_CIRCULAR_ARRAY_SIZE);
     this->generateCircularSearchArray(this->circularSearchArray->getData(), bevel);
+  }
+};
+
+// The reference allocates each realization's border grid with new[] and
+// writes only its 1s (src/catchmentborder/CatchmentBorderAlgorithm.h:64-66,
+// src/catchmentborder/CatchmentBorderAlgorithmCPUOpenMP.h:30-82,
+// src/framework/ManagedData.h:638); the other cells are whatever the heap
+// held.  This subclass zeroes the grid (what fresh memory holds) before the
+// reference's own extraction runs on it.
+class ZeroedBorder
+    : public CatchmentBorderAlgorithm_CPU_OpenMP<CatchmentBorderType, FlowTraceDataType> {
+ public:
+  void performExtractDrainageBorder(CatchmentBorderClass<CatchmentBorderType>* border,
+                                    FlowTraceDataClass<FlowTraceDataType>* trace) {
+    border->toHost();
+    std::memset((void*)border->getData(), 0,
+                sizeof(CatchmentBorderType) * (size_t)border->width * border->height);
+    CatchmentBorderAlgorithm_CPU_OpenMP<CatchmentBorderType,
+                                        FlowTraceDataType>::performExtractDrainageBorder(border,
+                                                                                         trace);
   }
 };
 
@@ -156,18 +175,12 @@ void ref_flow_trace(const int8_t* dir, const float* streams, int* label, int W,
   std::memcpy(label, t.getData(), sizeof(int) * (size_t)W * H);
 }
 
-// The reference allocates the per-realization border grid with new[] and
-// writes only its 1s (src/catchmentborder/CatchmentBorderAlgorithm.h:64,
-// src/framework/ManagedData.h:638).  Routing every allocation of a page or
-// more through mmap makes that grid start at zero, as it does for the large
-// grids of a real run, so the harness output does not depend on heap reuse.
 void ref_border_accumulate(const int* label, float* mc, int W, int H) {
-  mallopt(M_MMAP_THRESHOLD, 4096);
   FlowTraceData_t t(W, H, HOST);
   load(t, label, sizeof(int) * (size_t)W * H);
   CatchmentBorder_t m(t, AS_TEMPLATE);
   load(m, mc, sizeof(float) * (size_t)W * H);
-  CatchmentBorderAlgorithm_CPU_OpenMP<CatchmentBorderType, FlowTraceDataType> alg;
+  ZeroedBorder alg;
   alg.execute(&m, &t);
   std::memcpy(mc, m.getData(), sizeof(float) * (size_t)W * H);
 }
