@@ -76,3 +76,33 @@ def test_port_matches_reference_seeded(oracle, ref, W, H, seed, model, bevel, op
         nod = dem == -9999.0
         assert np.array_equal(b["realistic"][nod], np.where(b["conv"][nod] <= 0, 1.0,
                                                             b["conv"][nod]).astype(np.float32))
+
+
+@pytest.mark.parametrize("noise_seed", [7, 8])
+def test_port_matches_reference_plain512(oracle, ref, noise_seed):
+    """The 512 x 512 workload (Hurst 0.8, 80-180 m, 200 pits, streams above
+    500 cells, Gaussian 60 m, sigma 1.5) at full size."""
+    from cageo_gb300 import api, synth
+    dem, streams, p = synth.workload("plain-512")
+    r = api.filter_radius(p["range_m"], p["cell"])
+    taps = api.filter_build(api.FILTER_GAUSSIAN, p["range_m"], p["cell"], r)
+    noise = gaussian_noise(p["width"], p["height"], noise_seed, p["sigma"])
+    a = _stages(oracle, dem, noise, streams, taps, r, 1, 2)
+    b = _stages(ref, dem, noise, streams, taps, r, 1, 2)
+    for k in a:
+        assert _same(a[k], b[k]), k
+
+
+def test_port_matches_reference_uneven_tiles(oracle, ref):
+    """The batch's uneven grids (257 x 1013, 1500 x 733, 3001 x 401) at full
+    size with the exponential filter at 30, 75 and 120 m (radius 8, 19, 30)."""
+    from cageo_gb300 import api, synth
+    for (dem, streams), rng_m in zip(synth.batched_grids()[1:], (30.0, 75.0, 120.0)):
+        H, W = dem.shape
+        r = api.filter_radius(rng_m, 10.0)
+        taps = api.filter_build(api.FILTER_EXPONENTIAL, rng_m, 10.0, r)
+        noise = gaussian_noise(W, H, 3, 2.0)
+        a = _stages(oracle, dem, noise, streams, taps, r, 0, 2)
+        b = _stages(ref, dem, noise, streams, taps, r, 0, 2)
+        for k in a:
+            assert _same(a[k], b[k]), (W, H, k)
