@@ -1,5 +1,6 @@
 // common.cuh -- shared device/host helpers for the cageo kernels.
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <cuda_runtime.h>
@@ -44,6 +45,48 @@ struct Scratch {
 };
 
 inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// ---- per-device launch set-up ----------------------------------------------
+// A kernel's launch set-up (its dynamic shared-memory limit raised, the
+// number of blocks a cooperative launch may have) is made once per device
+// and kept in a process-wide table.  Function attributes belong to the
+// device, so each device is set up on its own.  Host threads may race to
+// fill an entry: each runs the (idempotent) set-up and stores the same value.
+constexpr int kMaxDevices = 64;
+struct PerDevice {
+  std::atomic<int> value[kMaxDevices];  // 0 until set up (static storage starts zeroed)
+};
+
+// *out = the cached value for the current device; `setup(dev, &v)` makes
+// it (v >= 1) the first time.
+template <typename SetUp>
+cageo_status per_device(PerDevice& cache, int* out, SetUp&& setup) {
+  int dev = 0;
+  CAGEO_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) {
+    set_error("device %d is beyond the %d devices a process may use", dev, kMaxDevices);
+    return CAGEO_ERR_ARGUMENT;
+  }
+  int v = cache.value[dev].load(std::memory_order_acquire);
+  if (v == 0) {
+    cageo_status st = setup(dev, &v);
+    if (st) return st;
+    cache.value[dev].store(v, std::memory_order_release);
+  }
+  *out = v;
+  return CAGEO_OK;
+}
+
+// Blocks of `fn` (`threads` threads, `smem` bytes of dynamic shared memory)
+// that device `dev` holds at once: the largest grid of a cooperative launch.
+inline cageo_status resident_blocks(const void* fn, int threads, size_t smem, int dev,
+                                    int* out) {
+  int sms = 0, per = 0;
+  CAGEO_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  CAGEO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, smem));
+  *out = (per > 1 ? per : 1) * (sms > 1 ? sms : 1);
+  return CAGEO_OK;
+}
 
 // ---- device helpers --------------------------------------------------------
 constexpr float kInf = __builtin_huge_valf();

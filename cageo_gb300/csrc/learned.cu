@@ -540,16 +540,18 @@ ws_infer_kernel(const float* __restrict__ params, const float* __restrict__ vg,
 
 cageo_status ws_infer(const float* params, const float* v, float* warm, float* depth, int W,
                       int H, float nodata, float threshold, cudaStream_t s) {
-  static int blocks = 0;
+  static PerDevice sm_count;
   const size_t smem = sizeof(InferSmem);
-  if (!blocks) {
+  int blocks = 0;
+  cageo_status st = per_device(sm_count, &blocks, [&](int dev, int* v) -> cageo_status {
     CAGEO_CUDA(cudaFuncSetAttribute(ws_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem));
-    int dev = 0, sms = 0;
-    CAGEO_CUDA(cudaGetDevice(&dev));
+    int sms = 0;
     CAGEO_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    blocks = sms;
-  }
+    *v = sms > 1 ? sms : 1;
+    return CAGEO_OK;
+  });
+  if (st) return st;
   const int tiles = ((W + kTX - 1) / kTX) * ((H + kTY - 1) / kTY);
   ws_infer_kernel<<<std::min(blocks, tiles), kInferWarps * 32, smem, s>>>(params, v, warm, depth,
                                                                          W, H, nodata, threshold);

@@ -869,27 +869,23 @@ __global__ void fill_scalars_kernel(unsigned int* s) {
     s[i] = (i == S_MIN || (i >= S_M && i < S_M + 3)) ? 0xffffffffu : 0u;
 }
 
-static int coop_blocks(const void* fn, size_t smem) {
-  int dev = 0, sms = 0, per = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kWarps * 32, smem);
-  return std::max(1, per) * sms;
-}
-
 template <int MODE>
 static cageo_status launch_flood(const FloodArgs& a, cudaStream_t s) {
   const size_t smem = sizeof(WarpSmem) * kWarps;
   auto fn = fill_flood_kernel<MODE>;
   CAGEO_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  static int blocks[2] = {0, 0};
-  if (!blocks[MODE]) blocks[MODE] = coop_blocks((const void*)fn, smem);
+  static PerDevice resident;  // one table per MODE
+  int blocks = 0;
+  cageo_status st = per_device(resident, &blocks, [&](int dev, int* v) -> cageo_status {
+    return resident_blocks((const void*)fn, kWarps * 32, smem, dev, v);
+  });
+  if (st) return st;
   FloodArgs args = a;
   void* params[] = {&args};
   // No more blocks than the tiles can keep busy (small grids leave the
   // rest of the GPU idle instead of polling the work queue).
   const int ntiles = a.w.tiles_x * a.w.tiles_y;
-  const int grid = std::max(1, std::min(blocks[MODE], (ntiles + kWarps - 1) / kWarps));
+  const int grid = std::max(1, std::min(blocks, (ntiles + kWarps - 1) / kWarps));
   CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(grid),
                                          dim3(kWarps * 32), params, smem, s));
   return CAGEO_OK;

@@ -27,7 +27,6 @@ static __device__ __align__(256) unsigned char g_static_fill_scratch[kStaticFill
 
 // Host code cannot use the array's name as a device address; its address
 // on each device is looked up once, with that device current.
-constexpr int kMaxDevices = 64;
 static void* g_static_fill_addr[kMaxDevices] = {};
 static std::mutex g_static_fill_mutex;
 

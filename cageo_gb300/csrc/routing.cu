@@ -558,17 +558,15 @@ cageo_status route_run(const float* filled, int8_t* dir, int* fd, const RouteWor
   if (gpu) d8_kernel<true><<<g, b, 0, s>>>(filled, (char2*)dir, fd, w, nodata);
   else d8_kernel<false><<<g, b, 0, s>>>(filled, (char2*)dir, fd, w, nodata);
   CAGEO_CUDA(cudaGetLastError());
-  static int coop = 0;
+  static PerDevice resident;
   const size_t smem = sizeof(FlatSmem) * kFWarps;
-  if (!coop) {
+  int coop = 0;
+  cageo_status st = per_device(resident, &coop, [&](int dev, int* v) -> cageo_status {
     CAGEO_CUDA(cudaFuncSetAttribute(flat_relax_kernel,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, flat_relax_kernel, kFWarps * 32, smem);
-    coop = std::max(1, per) * sms;
-  }
+    return resident_blocks((const void*)flat_relax_kernel, kFWarps * 32, smem, dev, v);
+  });
+  if (st) return st;
   const float* f = filled;
   int* fdp = fd;
   RouteWork wc = w;

@@ -250,14 +250,12 @@ cageo_status trace_run(const int8_t* dir, const float* streams, int* label,
   trace_init_kernel<<<dim3(w.tiles_x, w.tiles_y), 256, 0, s>>>(
       (const char2*)dir, streams, w.state, w.bstate, w.W, w.H, w.scal);
   CAGEO_CUDA(cudaGetLastError());
-  static int coop = 0;
-  if (!coop) {
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, trace_jump_kernel, kJumpThreads, 0);
-    coop = std::max(1, per) * sms;
-  }
+  static PerDevice resident;
+  int coop = 0;
+  cageo_status st = per_device(resident, &coop, [&](int dev, int* v) -> cageo_status {
+    return resident_blocks((const void*)trace_jump_kernel, kJumpThreads, 0, dev, v);
+  });
+  if (st) return st;
   int* stp = w.bstate;
   TraceWork wc = w;
   void* params[] = {(void*)&stp, (void*)&wc};
