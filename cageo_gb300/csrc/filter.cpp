@@ -17,6 +17,7 @@
 #include <cmath>
 #include <vector>
 #include "cageo.h"
+#include "guard.h"
 
 namespace {
 
@@ -88,10 +89,15 @@ extern "C" int cageo_filter_radius(float practical_range, float cell_size) {
   return (int)std::ceil((float)s);
 }
 
-extern "C" cageo_status cageo_filter_build(int model, float range, float cell, int r,
-                                           float* h_filter) {
-  if (!h_filter || r < 0 || r > 512 || !(range > 0) || !(cell > 0)) return CAGEO_ERR_ARGUMENT;
-  if (model != CAGEO_FILTER_GAUSSIAN && model != CAGEO_FILTER_EXPONENTIAL) return CAGEO_ERR_ARGUMENT;
+static cageo_status filter_build(int model, float range, float cell, int r, float* h_filter) {
+  if (!h_filter || r < 0 || r > 512 || !(range > 0) || !(cell > 0)) {
+    cageo::set_error("invalid argument: filter output, radius (0..512), range or cell size");
+    return CAGEO_ERR_ARGUMENT;
+  }
+  if (model != CAGEO_FILTER_GAUSSIAN && model != CAGEO_FILTER_EXPONENTIAL) {
+    cageo::set_error("invalid argument: filter model");
+    return CAGEO_ERR_ARGUMENT;
+  }
   const int n = 2 * r + 1;
   std::vector<double> corr(n * n);
   for (int y = -r, i = 0; y <= r; y++)
@@ -160,8 +166,17 @@ extern "C" cageo_status cageo_filter_build(int model, float range, float cell, i
     unorm += s * s;
   }
   unorm = std::sqrt(unorm);
-  if (!(unorm > 0)) return CAGEO_ERR_ARGUMENT;
+  if (!(unorm > 0)) {
+    cageo::set_error("invalid argument: the filter has no leading singular vector");
+    return CAGEO_ERR_ARGUMENT;
+  }
   const double root = std::sqrt(sigma);
   for (int i = 0; i < n; i++) h_filter[i] = (float)(u[i] / unorm * root);
   return CAGEO_OK;
+}
+
+extern "C" cageo_status cageo_filter_build(int model, float range, float cell, int r,
+                                           float* h_filter) {
+  return cageo::guarded("cageo_filter_build",
+                        [&] { return filter_build(model, range, cell, r, h_filter); });
 }

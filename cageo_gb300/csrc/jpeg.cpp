@@ -13,10 +13,7 @@
 #include <cstdio>
 #include <vector>
 #include "cageo.h"
-
-namespace cageo {
-void set_error(const char* fmt, ...);
-}
+#include "guard.h"
 
 namespace {
 
@@ -102,10 +99,16 @@ void put16(std::vector<uint8_t>& o, int v) {
 
 }  // namespace
 
-extern "C" cageo_status cageo_write_jpeg(const char* path, const uint8_t* h_gray, int W, int H,
-                                         int quality) {
-  if (!path || !h_gray || W <= 0 || H <= 0 || W > 65535 || H > 65535) return CAGEO_ERR_ARGUMENT;
-  if (quality < 1 || quality > 100) return CAGEO_ERR_ARGUMENT;
+static cageo_status write_jpeg(const char* path, const uint8_t* h_gray, int W, int H,
+                               int quality) {
+  if (!path || !h_gray || W <= 0 || H <= 0 || W > 65535 || H > 65535) {
+    cageo::set_error("invalid argument: JPEG path, image or size (1..65535 per side)");
+    return CAGEO_ERR_ARGUMENT;
+  }
+  if (quality < 1 || quality > 100) {
+    cageo::set_error("invalid argument: JPEG quality must be 1..100");
+    return CAGEO_ERR_ARGUMENT;
+  }
   const int scale = quality < 50 ? 5000 / quality : 200 - 2 * quality;
   uint8_t q[64];
   for (int i = 0; i < 64; i++) {
@@ -192,10 +195,16 @@ extern "C" cageo_status cageo_write_jpeg(const char* path, const uint8_t* h_gray
     return CAGEO_ERR_IO;
   }
   const size_t put = std::fwrite(o.data(), 1, o.size(), f);
-  std::fclose(f);
-  if (put != o.size()) {
+  const bool closed = std::fclose(f) == 0;
+  if (put != o.size() || !closed) {
     cageo::set_error("short write to \"%s\"", path);
     return CAGEO_ERR_IO;
   }
   return CAGEO_OK;
+}
+
+extern "C" cageo_status cageo_write_jpeg(const char* path, const uint8_t* h_gray, int W, int H,
+                                         int quality) {
+  return cageo::guarded("cageo_write_jpeg",
+                        [&] { return write_jpeg(path, h_gray, W, H, quality); });
 }

@@ -20,8 +20,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <new>
 #include <vector>
 #include "common.cuh"
+#include "guard.h"
 #include "front.cuh"
 #include "pitfill.cuh"
 #include "routing.cuh"
@@ -291,13 +293,22 @@ cageo_status create_common(cageo_pipeline** out, const cageo_pipeline_config* cf
   const int r = cageo_filter_radius(cfg->practical_range, cfg->cell_size);
   CAGEO_CHECK_ARG(r >= 0 && r < W && r < H, "filter radius must be below the grid size");
   CAGEO_CHECK_ARG(r <= kMaxRunRadius, "filter radius above 64");
-  auto* p = new cageo_pipeline();
+  const int L = 2 * r + 1;
+  const int taps = cfg->filter_model == CAGEO_FILTER_GAUSSIAN ? L : L * L;
+  std::vector<float> hf(taps);
+  cageo_status st = cageo_filter_build(cfg->filter_model, cfg->practical_range, cfg->cell_size,
+                                       r, hf.data());
+  if (st) return st;
+  auto* p = new (std::nothrow) cageo_pipeline();
+  if (!p) {
+    set_error("out of host memory for the pipeline object");
+    return CAGEO_ERR_HOST;
+  }
   p->cfg = *cfg;
   p->W = W;
   p->H = H;
   p->N = (int64_t)W * H;
   p->radius = r;
-  cageo_status st = CAGEO_OK;
   auto fail = [&](cageo_status s) {
     free_all(p);
     delete p;
@@ -306,8 +317,6 @@ cageo_status create_common(cageo_pipeline** out, const cageo_pipeline_config* cf
   if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess)
     return fail(cuda_fail(cudaGetLastError(), "cudaStreamCreate"));
   const size_t fb = sizeof(float) * p->N;
-  const int L = 2 * r + 1;
-  const int taps = cfg->filter_model == CAGEO_FILTER_GAUSSIAN ? L : L * L;
   if ((st = dalloc(&p->dem, fb)) || (st = dalloc(&p->streams, fb)) ||
       (st = dalloc(&p->noise, fb)) || (st = dalloc(&p->q, fb)) || (st = dalloc(&p->filled, fb)) ||
       (st = dalloc(&p->tmp, fb)) ||
@@ -323,10 +332,6 @@ cageo_status create_common(cageo_pipeline** out, const cageo_pipeline_config* cf
   p->fw = fill_carve(p->fill_ws, W, H);
   p->rw = route_carve(p->route_ws, W, H);
   p->tw = trace_carve(p->trace_ws, W, H);
-  std::vector<float> hf(taps);
-  if ((st = cageo_filter_build(cfg->filter_model, cfg->practical_range, cfg->cell_size, r,
-                               hf.data())))
-    return fail(st);
   cudaStream_t s = p->stream;
 #define PCUDA(call)                                          \
   do {                                                       \
@@ -359,17 +364,21 @@ cageo_status create_common(cageo_pipeline** out, const cageo_pipeline_config* cf
 extern "C" cageo_status cageo_pipeline_create(cageo_pipeline** out,
                                               const cageo_pipeline_config* cfg,
                                               const float* h_dem, const float* h_streams) {
-  return create_common(out, cfg, h_dem, h_streams, cudaMemcpyHostToDevice);
+  return guarded("cageo_pipeline_create", [&] {
+    return create_common(out, cfg, h_dem, h_streams, cudaMemcpyHostToDevice);
+  });
 }
 
 extern "C" cageo_status cageo_pipeline_create_device(cageo_pipeline** out,
                                                      const cageo_pipeline_config* cfg,
                                                      const float* d_dem,
                                                      const float* d_streams) {
-  return create_common(out, cfg, d_dem, d_streams, cudaMemcpyDeviceToDevice);
+  return guarded("cageo_pipeline_create_device", [&] {
+    return create_common(out, cfg, d_dem, d_streams, cudaMemcpyDeviceToDevice);
+  });
 }
 
-extern "C" cageo_status cageo_pipeline_run(cageo_pipeline* p, uint32_t first, int count) {
+static cageo_status pipeline_run(cageo_pipeline* p, uint32_t first, int count) {
   CAGEO_CHECK_ARG(p && count >= 0, "pipeline and count");
   cudaStream_t s = p->stream;
   cageo_status st;
@@ -445,6 +454,10 @@ extern "C" cageo_status cageo_pipeline_run(cageo_pipeline* p, uint32_t first, in
   return CAGEO_OK;
 }
 
+extern "C" cageo_status cageo_pipeline_run(cageo_pipeline* p, uint32_t first, int count) {
+  return guarded("cageo_pipeline_run", [&] { return pipeline_run(p, first, count); });
+}
+
 // One fast-path realization with CUDA events between the stages on the
 // pipeline's stream (no graph).  It is a real realization: its border mask
 // is accumulated like any other.  h_ms receives up to 6 stage times:
@@ -506,9 +519,9 @@ extern "C" cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t reali
   return st;
 }
 
-extern "C" cageo_status cageo_pipeline_run_filter(cageo_pipeline* p, uint32_t first, int count,
-                                                  int model, float practical_range,
-                                                  float error_mean, float error_stddev) {
+static cageo_status pipeline_run_filter(cageo_pipeline* p, uint32_t first, int count, int model,
+                                        float practical_range, float error_mean,
+                                        float error_stddev) {
   CAGEO_CHECK_ARG(p && count >= 0, "pipeline and count");
   CAGEO_CHECK_ARG(model == CAGEO_FILTER_GAUSSIAN || model == CAGEO_FILTER_EXPONENTIAL,
                   "filter model");
@@ -534,13 +547,22 @@ extern "C" cageo_status cageo_pipeline_run_filter(cageo_pipeline* p, uint32_t fi
   p->graph = nullptr;
   p->graph_ok = false;
   p->cfg.use_graphs = 0;
-  return cageo_pipeline_run(p, first, count);
+  return pipeline_run(p, first, count);
+}
+
+extern "C" cageo_status cageo_pipeline_run_filter(cageo_pipeline* p, uint32_t first, int count,
+                                                  int model, float practical_range,
+                                                  float error_mean, float error_stddev) {
+  return guarded("cageo_pipeline_run_filter", [&] {
+    return pipeline_run_filter(p, first, count, model, practical_range, error_mean,
+                               error_stddev);
+  });
 }
 
 // Checkpoint file: "CAGEOCK1", int32 W, H, uint64 seed, uint32 next
 // realization, then W*H uint32 counts (native byte order).
-extern "C" cageo_status cageo_pipeline_save(cageo_pipeline* p, const char* path,
-                                            uint32_t next_realization) {
+static cageo_status pipeline_save(cageo_pipeline* p, const char* path,
+                                  uint32_t next_realization) {
   CAGEO_CHECK_ARG(p && path, "null argument");
   std::vector<uint32_t> h((size_t)p->N);
   CAGEO_CUDA(cudaStreamSynchronize(p->stream));
@@ -563,8 +585,13 @@ extern "C" cageo_status cageo_pipeline_save(cageo_pipeline* p, const char* path,
   return CAGEO_OK;
 }
 
-extern "C" cageo_status cageo_pipeline_load(cageo_pipeline* p, const char* path,
-                                            uint32_t* next_realization) {
+extern "C" cageo_status cageo_pipeline_save(cageo_pipeline* p, const char* path,
+                                            uint32_t next_realization) {
+  return guarded("cageo_pipeline_save", [&] { return pipeline_save(p, path, next_realization); });
+}
+
+static cageo_status pipeline_load(cageo_pipeline* p, const char* path,
+                                  uint32_t* next_realization) {
   CAGEO_CHECK_ARG(p && path && next_realization, "null argument");
   FILE* f = std::fopen(path, "rb");
   if (!f) {
@@ -595,6 +622,11 @@ extern "C" cageo_status cageo_pipeline_load(cageo_pipeline* p, const char* path,
   CAGEO_CUDA(cudaMemcpy(p->counts, h.data(), 4 * (size_t)p->N, cudaMemcpyHostToDevice));
   *next_realization = next;
   return CAGEO_OK;
+}
+
+extern "C" cageo_status cageo_pipeline_load(cageo_pipeline* p, const char* path,
+                                            uint32_t* next_realization) {
+  return guarded("cageo_pipeline_load", [&] { return pipeline_load(p, path, next_realization); });
 }
 
 extern "C" cageo_status cageo_pipeline_counts_device(cageo_pipeline* p, float* d_out) {

@@ -11,13 +11,13 @@
 #include <fstream>
 #include <string>
 #include "cageo.h"
+#include "guard.h"
 
-namespace cageo {
-void set_error(const char* fmt, ...);
-}
-
-extern "C" cageo_status cageo_read_header(const char* path, cageo_raster_info* info) {
-  if (!path || !info) return CAGEO_ERR_ARGUMENT;
+static cageo_status read_header(const char* path, cageo_raster_info* info) {
+  if (!path || !info) {
+    cageo::set_error("invalid argument: null header path or output");
+    return CAGEO_ERR_ARGUMENT;
+  }
   std::ifstream f(path);
   if (!f.is_open()) {
     cageo::set_error("unable to open header \"%s\"", path);
@@ -60,23 +60,37 @@ extern "C" cageo_status cageo_read_header(const char* path, cageo_raster_info* i
   return CAGEO_OK;
 }
 
+extern "C" cageo_status cageo_read_header(const char* path, cageo_raster_info* info) {
+  return cageo::guarded("cageo_read_header", [&] { return read_header(path, info); });
+}
+
 extern "C" cageo_status cageo_write_header(const char* path, const cageo_raster_info* info) {
-  if (!path || !info) return CAGEO_ERR_ARGUMENT;
+  if (!path || !info) {
+    cageo::set_error("invalid argument: null header path or input");
+    return CAGEO_ERR_ARGUMENT;
+  }
   FILE* f = std::fopen(path, "w");
   if (!f) {
     cageo::set_error("unable to open \"%s\" for writing", path);
     return CAGEO_ERR_IO;
   }
-  std::fprintf(f, "ncols         %d\nnrows         %d\nxllcorner     %.10g\nyllcorner     %.10g\n"
-                  "cellsize      %.9g\nNODATA_value  %.9g\nbyteorder     %s\n",
-               info->ncols, info->nrows, info->xllcorner, info->yllcorner, info->cellsize,
-               info->nodata_value, info->byteorder_msb ? "MSBFIRST" : "LSBFIRST");
-  std::fclose(f);
+  const int put =
+      std::fprintf(f, "ncols         %d\nnrows         %d\nxllcorner     %.10g\nyllcorner     %.10g\n"
+                      "cellsize      %.9g\nNODATA_value  %.9g\nbyteorder     %s\n",
+                   info->ncols, info->nrows, info->xllcorner, info->yllcorner, info->cellsize,
+                   info->nodata_value, info->byteorder_msb ? "MSBFIRST" : "LSBFIRST");
+  if ((std::fclose(f) != 0) || put < 0) {
+    cageo::set_error("short write to \"%s\"", path);
+    return CAGEO_ERR_IO;
+  }
   return CAGEO_OK;
 }
 
 extern "C" cageo_status cageo_read_raster(const char* path, float* h_out, size_t count) {
-  if (!path || !h_out) return CAGEO_ERR_ARGUMENT;
+  if (!path || !h_out) {
+    cageo::set_error("invalid argument: null raster path or output");
+    return CAGEO_ERR_ARGUMENT;
+  }
   FILE* f = std::fopen(path, "rb");
   if (!f) {
     cageo::set_error("unable to open file \"%s\"", path);
@@ -100,15 +114,18 @@ extern "C" cageo_status cageo_read_raster(const char* path, float* h_out, size_t
 }
 
 extern "C" cageo_status cageo_write_raster(const char* path, const float* h_data, size_t count) {
-  if (!path || !h_data) return CAGEO_ERR_ARGUMENT;
+  if (!path || !h_data) {
+    cageo::set_error("invalid argument: null raster path or input");
+    return CAGEO_ERR_ARGUMENT;
+  }
   FILE* f = std::fopen(path, "wb");
   if (!f) {
     cageo::set_error("unable to open \"%s\" for writing", path);
     return CAGEO_ERR_IO;
   }
-  size_t put = std::fwrite(h_data, sizeof(float), count, f);
-  std::fclose(f);
-  if (put != count) {
+  const size_t put = std::fwrite(h_data, sizeof(float), count, f);
+  const bool closed = std::fclose(f) == 0;
+  if (put != count || !closed) {
     cageo::set_error("short write to \"%s\"", path);
     return CAGEO_ERR_IO;
   }

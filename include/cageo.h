@@ -41,6 +41,8 @@ typedef int cageo_status;
 #define CAGEO_ERR_NO_CONVERGENCE 3 /* an iterative stage hit its iteration or wait limit */
 #define CAGEO_ERR_IO 4         /* a raster or header file could not be read or written */
 #define CAGEO_ERR_FORMAT 5     /* a header tag or value is not understood */
+#define CAGEO_ERR_HOST 6       /* host memory could not be allocated (no C++ exception
+                                  leaves the library) */
 
 /* Filter models, src/convolution/ConvolutionCommon.h:21-24. */
 #define CAGEO_FILTER_EXPONENTIAL 0

@@ -115,3 +115,51 @@ def test_synthetic_streams_follow_accumulation():
     assert np.all((s >= 0) == (acc > 40))
     assert acc.max() <= 64 * 48 and acc.min() >= 1
     assert s[s >= 0].min() >= 1  # stream ids start at 1 (0 would alias index 0 in tracing)
+
+
+def test_host_refusals_set_the_error_string(tmp_path):
+    L = api.lib()
+    out = (ctypes.c_float * 9)()
+    assert L.cageo_filter_build(7, 60.0, 10.0, 1, out) == 1 and "filter model" in _err()
+    assert L.cageo_filter_build(1, 60.0, 10.0, -1, out) == 1 and "radius" in _err()
+    img = np.zeros((8, 8), np.uint8)
+    p = str(tmp_path / "x.jpg").encode()
+    assert L.cageo_write_jpeg(p, img.ctypes.data_as(P), 8, 8, 0) == 1 and "quality" in _err()
+    assert L.cageo_write_jpeg(p, None, 8, 8, 85) == 1 and "JPEG" in _err()
+    assert L.cageo_read_header(None, None) == 1 and "header" in _err()
+    assert L.cageo_write_raster(None, None, 0) == 1 and "raster" in _err()
+
+
+_OOM_CHILD = r"""
+import ctypes, resource, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+from cageo_gb300 import api
+L = api.lib()
+W = H = 40000
+img = np.zeros(W * H, np.uint8)  # reserved, not touched
+def vm_bytes():
+    with open("/proc/self/status") as f:
+        for line in f:
+            if line.startswith("VmSize:"):
+                return int(line.split()[1]) * 1024
+lim = vm_bytes() + (64 << 20)
+resource.setrlimit(resource.RLIMIT_AS, (lim, lim))
+st = L.cageo_write_jpeg(sys.argv[2].encode(), img.ctypes.data_as(ctypes.c_void_p), W, H, 85)
+print(st, L.cageo_last_error_string().decode())
+"""
+
+
+def test_host_allocation_failure_is_a_status_not_an_abort(tmp_path):
+    """The JPEG writer's output buffer cannot be allocated under a small
+    address-space limit: the call returns CAGEO_ERR_HOST with a message
+    instead of letting std::bad_alloc terminate the process."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", _OOM_CHILD, root, str(tmp_path / "big.jpg")],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]
+    status, msg = r.stdout.strip().split(" ", 1)
+    assert int(status) == 6 and "out of host memory" in msg, r.stdout
