@@ -11,15 +11,18 @@
 // reverse pop order.  Cells whose accumulation exceeds `threshold` become
 // stream cells, numbered per 8-connected stream component (1, 2, ...) or all
 // 1.0; the rest get `nodata`.
+//
+// Returns 0, 1 for a grid below 3 x 3 or of 2^32 cells or more (cell
+// indices are uint32), 2 when host memory runs out (no C++ exception
+// leaves the library).
 #include <cstdint>
+#include <new>
 #include <queue>
 #include <vector>
 
-extern "C" int cageo_synth_streams(const float* dem, int W, int H,
-                                   int threshold, int per_component_ids,
-                                   float nodata, float* streams_out,
-                                   int* accum_out) {
-  if (W < 3 || H < 3) return 1;
+static int synth_streams(const float* dem, int W, int H, int threshold, int per_component_ids,
+                         float nodata, float* streams_out, int* accum_out) {
+  if (W < 3 || H < 3 || (int64_t)W * H >= ((int64_t)1 << 32)) return 1;
   const int64_t N = (int64_t)W * H;
   struct Item {
     float z;
@@ -96,4 +99,15 @@ extern "C" int cageo_synth_streams(const float* dem, int W, int H,
   if (accum_out)
     for (int64_t i = 0; i < N; i++) accum_out[i] = acc[i];
   return 0;
+}
+
+extern "C" int cageo_synth_streams(const float* dem, int W, int H, int threshold,
+                                   int per_component_ids, float nodata, float* streams_out,
+                                   int* accum_out) {
+  try {
+    return synth_streams(dem, W, H, threshold, per_component_ids, nodata, streams_out,
+                         accum_out);
+  } catch (const std::bad_alloc&) {
+    return 2;
+  }
 }

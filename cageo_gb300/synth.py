@@ -87,8 +87,10 @@ def make_streams(dem, threshold, nodata=-9999.0, ids="ones", return_accum=False)
         1 if ids == "components" else 0, ctypes.c_float(nodata),
         out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
         acc.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    if rc == 2:
+        raise MemoryError("stream synthesis ran out of host memory")
     if rc:
-        raise ValueError("grid too small for stream synthesis")
+        raise ValueError("grid too small (or too large) for stream synthesis")
     return (out, acc) if return_accum else out
 
 
