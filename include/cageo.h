@@ -22,6 +22,12 @@
  *    query the size with the matching *_workspace_size().  A workspace must
  *    start on a 256-byte boundary (CAGEO_ERR_ARGUMENT otherwise).  Passing
  *    NULL lets the call allocate and free it stream-ordered (cudaMallocAsync).
+ *  - Threads: stage calls keep no state between calls (launch set-up is
+ *    cached per device, safely), so host threads may call them at once on
+ *    different buffers and streams.  A pipeline object is used by one host
+ *    thread at a time; separate pipelines may run on separate threads, as
+ *    the batched workload does.  cageo_pitfill_static shares one scratch
+ *    array among all callers and must be serialized by them.
  */
 #ifndef CAGEO_H_
 #define CAGEO_H_
