@@ -161,6 +161,14 @@ int main(int argc, char** argv) {
   if (o.filter == "Gaussian") model = CAGEO_FILTER_GAUSSIAN;
   else if (o.filter == "Exponential") model = CAGEO_FILTER_EXPONENTIAL;
   else { std::printf("Unknown filter type provided: %s. Exiting...\n", o.filter.c_str()); return 1; }
+  if (o.iterations < 0) {
+    std::printf("The number of iterations (%d) must not be negative. Exiting...\n", o.iterations);
+    return 1;
+  }
+  if (!(o.range > 0.0f)) {
+    std::printf("The practical range must be a positive number. Exiting...\n");
+    return 1;
+  }
   if (o.bevel < 1 || o.bevel > 5) {
     std::printf("Bevel radius (%d) is outside 1..5 (MAX_BEVEL_RADIUS 5).\n", o.bevel);
     return 1;

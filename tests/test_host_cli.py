@@ -46,6 +46,9 @@ def test_help_lists_reference_options(tmp_path):
     (["--bevel-radius=0"], "outside 1..5"),
     (["-o", "counts.tif"], "Unknown output extension"),
     (["--output-option", "middle"], "Unknown output option"),
+    (["-i", "-3"], "must not be negative"),
+    (["--practical-range", "abc"], "practical range"),
+    (["--practical-range=0"], "practical range"),
 ])
 def test_refusals(inputs, args, text):
     r = _run(["--dem-path", str(inputs), "-i", "1", "--seed", "1", *args], inputs.parent)
