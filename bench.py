@@ -154,6 +154,16 @@ def cpu_rate(dem, streams, p, steps, first_real, window=2048, gpu_noise=True):
     return rate, o.threads(), total
 
 
+def sample_text(steps, dem, window=2048):
+    """What cpu_rate timed: `steps` realizations on its window of `dem`."""
+    H, W = dem.shape
+    wy, wx = min(window, H), min(window, W)
+    if (wy, wx) == (H, W):
+        return "%d realizations of the whole %dx%d DEM" % (steps, W, H)
+    return "%d realizations on a %dx%d window of the %dx%d DEM, rate scaled by cell count" % (
+        steps, wx, wy, W, H)
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -164,7 +174,7 @@ def run_reference(args, rank, world):
     rate, threads, sec = cpu_rate(dem, streams, p, args.steps, 0, gpu_noise=False)
     wall = time.perf_counter() - t0
     H, W = dem.shape
-    sample = "%d realizations on a 2048x2048 window of the 8192^2 DEM, rate scaled by cell count" % args.steps
+    sample = sample_text(args.steps, dem)
     line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "realizations/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 / rate, "higher_is_better": True, "scaling": "weak",
@@ -405,8 +415,7 @@ def main():
         rate, threads, sec = cpu_rate(dem, streams, p, args.cpu_steps, 50_000)
         line["cpu_baseline"] = {"value": rate, "unit": "realizations/s", "cores": threads,
                                 "kind": "port", "seconds": sec,
-                                "sample": "%d realizations on a 2048x2048 window, rate scaled by cell count"
-                                % args.cpu_steps}
+                                "sample": sample_text(args.cpu_steps, dem)}
     print(json.dumps(line), flush=True)
     pipe.close()
     if world > 1:

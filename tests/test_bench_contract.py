@@ -29,6 +29,7 @@ def test_reference_arm_line():
     assert d["higher_is_better"] is True and d["config"]["workload"] == "plain-512"
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["cores"] >= 1 and cb["kind"] in ("port", "reference")
+    assert cb["sample"] == "1 realizations of the whole 512x512 DEM"
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
 
 
