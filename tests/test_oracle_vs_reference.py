@@ -19,11 +19,12 @@ def ref():
     return Reference()
 
 
-def _stages(impl, dem, noise, streams, taps, r, model, bevel):
+def _stages(impl, dem, noise, streams, taps, r, model, bevel, nodata_dem=-9999.0,
+            nodata_stream=-9999.0):
     conv = impl.convolve(noise, taps, r, model)
-    real = impl.realistic_dem(dem, conv)
-    burned = impl.stream_burn(real, streams, bevel)
-    q, filled = impl.pitfill(burned)
+    real = impl.realistic_dem(dem, conv, nodata_dem)
+    burned = impl.stream_burn(real, streams, bevel, nodata_dem, nodata_stream)
+    q, filled = impl.pitfill(burned, nodata_dem)
     dirs = impl.flow_route(filled)
     labels = impl.flow_trace(dirs, streams)
     mc = impl.border_accumulate(labels, np.full(dem.shape, 2.0, np.float32))
@@ -106,3 +107,31 @@ def test_port_matches_reference_uneven_tiles(oracle, ref):
         b = _stages(ref, dem, noise, streams, taps, r, 0, 2)
         for k in a:
             assert _same(a[k], b[k]), (W, H, k)
+
+
+@pytest.mark.parametrize("nodata_dem, nodata_stream", [(0.0, -9999.0), (-9999.0, 0.0), (-1.0, -1.0)])
+def test_port_matches_reference_other_nodata(oracle, ref, nodata_dem, nodata_stream):
+    """NODATA values other than -9999 in the DEM and the stream raster.
+    With a DEM NODATA of 0 the burned stream cells equal NODATA, and the
+    reference's in-place OpenMP burn reads neighbours that other threads
+    may already have zeroed (src/streamburning/StreamBurningAlgorithmCPUOpenMP.h:46-71):
+    its result then depends on the thread schedule.  The port burns in
+    raster order, which is what the reference gives on one thread, so the
+    reference runs on one OpenMP thread here."""
+    import ctypes
+    from cageo_gb300 import api
+    dem, streams = make_case(120, 90, seed=3, nodata_cells=30)
+    dem[dem == -9999.0] = nodata_dem
+    streams = np.where(streams == -9999.0, np.float32(nodata_stream), streams).astype(np.float32)
+    taps = api.filter_build(api.FILTER_GAUSSIAN, 60.0, 10.0, 15)
+    noise = gaussian_noise(120, 90, 4, 1.5)
+    a = _stages(oracle, dem, noise, streams, taps, 15, 1, 2, nodata_dem, nodata_stream)
+    gomp = ctypes.CDLL("libgomp.so.1")
+    threads = gomp.omp_get_max_threads()
+    gomp.omp_set_num_threads(1)
+    try:
+        b = _stages(ref, dem, noise, streams, taps, 15, 1, 2, nodata_dem, nodata_stream)
+    finally:
+        gomp.omp_set_num_threads(threads)
+    for k in a:
+        assert _same(a[k], b[k]), k
