@@ -135,3 +135,36 @@ def test_port_matches_reference_other_nodata(oracle, ref, nodata_dem, nodata_str
         gomp.omp_set_num_threads(threads)
     for k in a:
         assert _same(a[k], b[k]), k
+
+
+def test_port_matches_reference_stream_values(oracle, ref):
+    """Stream rasters with fractional, zero and negative (non-NODATA) ids:
+    burning treats every non-NODATA value as a stream, tracing only values
+    >= 0, and labels are -(int)id (src/flowtracing/FlowTracingAlgorithmCPUOpenMP.h:58-99)."""
+    from cageo_gb300 import api
+    dem, streams = make_case(140, 100, seed=8)
+    ids = streams >= 0
+    vals = np.random.default_rng(5).choice(np.array([2.7, 0.0, -5.0, 3.0, 0.4], np.float32),
+                                           size=int(ids.sum()))
+    streams[ids] = vals
+    taps = api.filter_build(api.FILTER_GAUSSIAN, 60.0, 10.0, 15)
+    noise = gaussian_noise(140, 100, 9, 1.5)
+    a = _stages(oracle, dem, noise, streams, taps, 15, 1, 2)
+    b = _stages(ref, dem, noise, streams, taps, 15, 1, 2)
+    for k in a:
+        assert _same(a[k], b[k]), k
+
+
+def test_port_matches_reference_trace_dead_ends(oracle, ref):
+    """Directions with dead ends (no direction off the border) and label-0
+    streams: the reference's walk gives up after its step limit and the
+    connect pass copies cell 0's label (src/flowtracing/FlowTracingAlgorithmCPUOpenMP.h:66-75,115-134)."""
+    rng = np.random.default_rng(5)
+    H, W = 40, 50
+    dirs = rng.integers(-1, 2, size=(H, W, 2)).astype(np.int8)
+    dirs[..., 0] = -1
+    dirs[rng.random((H, W)) < 0.05] = 0
+    st = np.full((H, W), -9999.0, np.float32)
+    st[rng.random((H, W)) < 0.05] = 0.0
+    st[rng.random((H, W)) < 0.05] = 2.0
+    assert np.array_equal(oracle.flow_trace(dirs, st), ref.flow_trace(dirs, st))
