@@ -14,6 +14,7 @@
 //  * the noise: written straight into the RandomField buffer, as
 //    RandomFieldAlgorithm_CPU_OpenMP::generateRandomField would
 //    (src/randomfield/RandomFieldAlgorithmCPUOpenMP.h:47-76).
+#include <cstdio>
 #include <cstring>
 #include <cstdint>
 
@@ -173,6 +174,7 @@ void ref_flow_trace(const int8_t* dir, const float* streams, int* label, int W,
   FlowTracingAlgorithm_CPU_OpenMP<FlowTraceDataType, FlowDirDataType, DemData> alg;
   alg.execute(&t, &fd, &s);
   std::memcpy(label, t.getData(), sizeof(int) * (size_t)W * H);
+  std::fflush(stdout);  // the walk's "Infinite loop?" notes go out with this call's output
 }
 
 void ref_border_accumulate(const int* label, float* mc, int W, int H) {
