@@ -168,3 +168,23 @@ def test_port_matches_reference_trace_dead_ends(oracle, ref):
     st[rng.random((H, W)) < 0.05] = 0.0
     st[rng.random((H, W)) < 0.05] = 2.0
     assert np.array_equal(oracle.flow_trace(dirs, st), ref.flow_trace(dirs, st))
+
+
+@pytest.mark.parametrize("H,W", [(1, 1), (1, 7), (7, 1), (2, 2), (3, 3), (2, 9), (5, 4), (33, 1)])
+def test_port_matches_reference_tiny_grids(oracle, ref, H, W):
+    """Grids that are all or almost all border, single rows and columns:
+    fill, routing, tracing and border counts."""
+    rng = np.random.default_rng(H * 100 + W)
+    for _ in range(5):
+        dem = np.round(rng.uniform(0, 5, (H, W)), 2).astype(np.float32)
+        dem[rng.random((H, W)) < 0.1] = 0.0
+        streams = np.where(rng.random((H, W)) < 0.1, np.float32(1.0), np.float32(-9999.0))
+        qa, fa = oracle.pitfill(dem)
+        qb, fb = ref.pitfill(dem)
+        assert _same(qa, qb) and _same(fa, fb)
+        da, db = oracle.flow_route(fa), ref.flow_route(fb)
+        assert np.array_equal(da, db)
+        la, lb = oracle.flow_trace(da, streams), ref.flow_trace(db, streams)
+        assert np.array_equal(la, lb)
+        zero = np.zeros((H, W), np.float32)
+        assert _same(oracle.border_accumulate(la, zero), ref.border_accumulate(lb, zero))
