@@ -41,7 +41,9 @@ def test_header_symbols_exported():
     assert not missing, missing
 
 
-@pytest.mark.parametrize("model,rng_m", [(1, 60.0), (1, 90.0), (1, 30.0), (0, 30.0), (0, 60.0)])
+@pytest.mark.parametrize("model,rng_m", [(1, 60.0), (1, 90.0), (1, 30.0), (0, 30.0), (0, 60.0),
+                                         (0, 45.0), (0, 75.0), (0, 97.5), (0, 120.0),
+                                         (1, 120.0), (1, 42.0)])
 def test_filter_matches_numpy(model, rng_m):
     from cageo_gb300 import api
     r = api.filter_radius(rng_m, 10.0)
