@@ -56,6 +56,7 @@ _SIGS = {
     "cageo_version": ([], ctypes.c_char_p),
     "cageo_last_error_string": ([], ctypes.c_char_p),
     "cageo_noise_philox": ([_vp, _i, _i, ctypes.c_uint64, ctypes.c_uint32, _f, _f, _vp], _i),
+    "cageo_philox4x32_10": ([_vp, ctypes.c_int64, _vp, _vp, _vp], _i),
     "cageo_filter_radius": ([_f, _f], _i),
     "cageo_filter_build": ([_i, _f, _f, _i, _vp], _i),
     "cageo_convolve": ([_vp, _vp, _i, _i, _i, _vp, _i, _vp], _i),
@@ -92,6 +93,7 @@ _SIGS = {
     "cageo_pipeline_save": ([_vp, ctypes.c_char_p, ctypes.c_uint32], _i),
     "cageo_pipeline_load": ([_vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint32)], _i),
     "cageo_pipeline_stream": ([_vp], _vp),
+    "cageo_pipeline_graph_kernels": ([_vp, _vp], _i),
     "cageo_pipeline_stats": ([_vp, _vp, _i], _i),
     "cageo_pipeline_profile": ([_vp, ctypes.c_uint32, _vp, _i], _i),
     "cageo_pipeline_destroy": ([_vp], None),
@@ -155,6 +157,18 @@ def noise_philox(field, seed, realization, mean=0.0, stddev=1.0):
     H, W = field.shape
     _check(lib().cageo_noise_philox(_ptr(field), W, H, seed, realization, mean, stddev, _stream()))
     return field
+
+
+def philox4x32_10(counter, key, n=1, device=None):
+    """Raw Philox4x32-10 words: (n, 4) uint32 numpy array; block i uses the
+    counter (counter[0] + i, counter[1], counter[2], counter[3])."""
+    import torch
+    out = torch.empty(4 * n, dtype=torch.int32, device=device or "cuda")
+    c = (ctypes.c_uint32 * 4)(*[int(x) & 0xFFFFFFFF for x in counter])
+    k = (ctypes.c_uint32 * 2)(*[int(x) & 0xFFFFFFFF for x in key])
+    _check(lib().cageo_philox4x32_10(_ptr(out), n, ctypes.cast(c, _vp), ctypes.cast(k, _vp),
+                                     _stream()))
+    return out.cpu().numpy().view(np.uint32).reshape(n, 4)
 
 
 # ---- A2 ---------------------------------------------------------------------
@@ -441,6 +455,12 @@ class Pipeline:
         ms = np.zeros(6, np.float32)
         _check(lib().cageo_pipeline_profile(self._p, realization, ms.ctypes.data_as(_vp), 6))
         return dict(zip(self.STAGES, (float(v) for v in ms)))
+
+    def graph_kernels(self):
+        """Kernel launches in the captured per-realization CUDA graph."""
+        n = ctypes.c_int64()
+        _check(lib().cageo_pipeline_graph_kernels(self._p, ctypes.byref(n)))
+        return n.value
 
     @property
     def stream(self):

@@ -214,8 +214,29 @@ int main(int argc, char** argv) {
     uint32_t nxt = 0;
     if (cageo_pipeline_load(p, o.resume.c_str(), &nxt)) { cageo_pipeline_destroy(p); return fail("resume"); }
     start = (int)nxt;
+    if (nxt > (uint32_t)o.iterations) {
+      std::printf("The checkpoint %s already holds %u realizations, more than --iterations (%d). "
+                  "Exiting...\n", o.resume.c_str(), nxt, o.iterations);
+      cageo_pipeline_destroy(p);
+      return 1;
+    }
     std::printf("Resuming at realization %d\n", start);
   }
+  // The END output (or the frame of realization it - 1): false on failure.
+  auto write_output = [&](int it) {
+    char name[4096];
+    const char* suffix = jpeg ? ".jpg" : ".bin";
+    if (opt == FRAMES) std::snprintf(name, sizeof(name), "%s_%04d%s", out_name.c_str(), it - 1, suffix);
+    else std::snprintf(name, sizeof(name), "%s%s", out_name.c_str(), suffix);
+    if (jpeg) {
+      if (cageo_pipeline_counts_bytes(p, image.data())) return fail("counts") == 0;
+      if (cageo_write_jpeg(name, image.data(), W, H, 85)) return fail("output") == 0;
+    } else {
+      if (cageo_pipeline_counts(p, counts.data())) return fail("counts") == 0;
+      if (cageo_write_raster(name, counts.data(), N)) return fail("output") == 0;
+    }
+    return true;
+  };
   auto t0 = std::chrono::steady_clock::now();
   for (int it = start; it < o.iterations;) {
     // One realization per call when every realization is written or saved.
@@ -226,26 +247,22 @@ int main(int argc, char** argv) {
       cageo_pipeline_destroy(p);
       return fail("checkpoint");
     }
-    if ((opt == END && it == o.iterations) || opt == FRAMES) {
-      char name[4096];
-      const char* suffix = jpeg ? ".jpg" : ".bin";
-      if (opt == FRAMES) std::snprintf(name, sizeof(name), "%s_%04d%s", out_name.c_str(), it - 1, suffix);
-      else std::snprintf(name, sizeof(name), "%s%s", out_name.c_str(), suffix);
-      if (jpeg) {
-        if (cageo_pipeline_counts_bytes(p, image.data())) { cageo_pipeline_destroy(p); return fail("counts"); }
-        if (cageo_write_jpeg(name, image.data(), W, H, 85)) { cageo_pipeline_destroy(p); return fail("output"); }
-      } else {
-        if (cageo_pipeline_counts(p, counts.data())) { cageo_pipeline_destroy(p); return fail("counts"); }
-        if (cageo_write_raster(name, counts.data(), N)) { cageo_pipeline_destroy(p); return fail("output"); }
-      }
+    if (((opt == END && it == o.iterations) || opt == FRAMES) && !write_output(it)) {
+      cageo_pipeline_destroy(p);
+      return 1;
     }
+  }
+  // A resumed run with nothing left to do still writes the END output.
+  if (opt == END && start == o.iterations && !write_output(start)) {
+    cageo_pipeline_destroy(p);
+    return 1;
   }
   double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   int64_t st[5] = {0};
   cageo_pipeline_stats(p, st, 5);
   const int done = o.iterations - start;
   std::fprintf(stderr, "\n***********\n\n%d realizations in %.3f s: %.3f realizations/s, %.3e cells/s\n",
-               done, sec, done / sec, done * (double)N / sec);
+               done, sec, done > 0 ? done / sec : 0.0, done > 0 ? done * (double)N / sec : 0.0);
   std::fprintf(stderr, "last realization: fill passes %lld, phases %lld, flat layers %lld\n",
                (long long)st[0], (long long)st[1], (long long)st[2]);
   cageo_pipeline_destroy(p);

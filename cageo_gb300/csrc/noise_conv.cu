@@ -470,6 +470,32 @@ extern "C" cageo_status cageo_noise_philox(float* d_field, int W, int H,
                       stream);
 }
 
+// Raw Philox4x32-10 blocks: block i is philox4x32_10((c0 + i, c1, c2, c3),
+// (k0, k1)), the generator noise_kernel draws from.
+__global__ void philox_bits_kernel(uint32_t* __restrict__ out, int64_t n, U4 c, uint32_t k0,
+                                   uint32_t k1) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  U4 ci = c;
+  ci.x += (uint32_t)i;
+  const U4 r = philox4x32_10(ci, k0, k1);
+  out[4 * i] = r.x;
+  out[4 * i + 1] = r.y;
+  out[4 * i + 2] = r.z;
+  out[4 * i + 3] = r.w;
+}
+
+extern "C" cageo_status cageo_philox4x32_10(uint32_t* d_out, int64_t n, const uint32_t* h_ctr,
+                                            const uint32_t* h_key, cudaStream_t stream) {
+  CAGEO_CHECK_ARG(d_out && h_ctr && h_key && n > 0 && n < ((int64_t)1 << 31),
+                  "pointers and block count");
+  const U4 c = {h_ctr[0], h_ctr[1], h_ctr[2], h_ctr[3]};
+  philox_bits_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(d_out, n, c, h_key[0],
+                                                                      h_key[1]);
+  CAGEO_CUDA(cudaGetLastError());
+  return CAGEO_OK;
+}
+
 extern "C" cageo_status cageo_convolve(const float* d_in, float* d_out, int W,
                                        int H, int model, const float* d_filter,
                                        int radius, cudaStream_t stream) {

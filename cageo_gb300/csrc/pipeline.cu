@@ -21,7 +21,9 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <string>
 #include <vector>
+#include <unistd.h>
 #include "common.cuh"
 #include "guard.h"
 #include "front.cuh"
@@ -85,6 +87,26 @@ __global__ void realization_end_kernel(uint32_t* real, int* anomaly, uint32_t* r
   }
 }
 
+// Order-independent 64-bit digest of a float grid: the wrapping sum over
+// cells of a SplitMix64 finalizer of (cell index, value bits).  The
+// checkpoint records it so that a resume onto other input grids is refused.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__global__ void grid_digest_kernel(const float* __restrict__ g, int64_t n,
+                                   unsigned long long salt, unsigned long long* out) {
+  unsigned long long h = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    h += mix64(((unsigned long long)i * 0x9E3779B97F4A7C15ull) ^
+               ((unsigned long long)__float_as_uint(g[i]) << 32) ^ salt);
+  for (int o = 16; o; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, h);
+}
+
 __global__ void counts_to_float_kernel(const uint32_t* __restrict__ c, float* __restrict__ f,
                                        int64_t n) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -124,6 +146,8 @@ struct cageo_pipeline {
   unsigned int* ws_count = nullptr;
   float ws_threshold = 0.0f;
   int64_t ws_stats[8] = {};
+  // Digest of the DEM and stream grids (grid_digest_kernel), for checkpoints.
+  unsigned long long input_digest = 0;
 };
 
 namespace {
@@ -343,6 +367,15 @@ cageo_status create_common(cageo_pipeline** out, const cageo_pipeline_config* cf
   PCUDA(cudaMemcpyAsync(p->streams, streams, fb, kind, s));
   PCUDA(cudaMemsetAsync(p->counts, 0, 4 * (size_t)p->N, s));
   PCUDA(cudaMemsetAsync(p->dscal, 0, sizeof(uint32_t) * 3, s));
+  {
+    // dscal[4..5] holds the digest until the first realization.
+    unsigned long long* dig = (unsigned long long*)(p->dscal + 4);
+    PCUDA(cudaMemsetAsync(dig, 0, 8, s));
+    grid_digest_kernel<<<1024, 256, 0, s>>>(p->dem, p->N, 0x44454dull, dig);
+    grid_digest_kernel<<<1024, 256, 0, s>>>(p->streams, p->N, 0x535452ull << 20, dig);
+    PCUDA(cudaGetLastError());
+    PCUDA(cudaMemcpyAsync(&p->input_digest, dig, 8, cudaMemcpyDeviceToHost, s));
+  }
   if ((st = launch_burn_code(p->streams, p->code, W, H, cfg->nodata_stream, cfg->bevel_radius,
                              p->fp.factor, s)))
     return fail(st);
@@ -559,27 +592,92 @@ extern "C" cageo_status cageo_pipeline_run_filter(cageo_pipeline* p, uint32_t fi
   });
 }
 
-// Checkpoint file: "CAGEOCK1", int32 W, H, uint64 seed, uint32 next
-// realization, then W*H uint32 counts (native byte order).
+// Checkpoint file (native byte order): the 8-byte magic "CAGEOCK2", a
+// fixed header recording everything the counts depend on -- the grid size,
+// the seed, the next realization number, the pipeline's filter and error
+// model, bevel radius, fill mode, NODATA values and cell size, and a digest
+// of the DEM and stream grids -- then W*H uint32 counts.  Loading refuses a
+// checkpoint whose header differs from the pipeline in any of them, so a
+// resume can only continue the same Monte Carlo run.
+struct CheckpointHeader {
+  char magic[8];
+  int32_t width, height;
+  uint64_t seed;
+  uint32_t next_realization;
+  int32_t filter_model;
+  float practical_range, cell_size, error_mean, error_stddev;
+  int32_t bevel_radius, fill_mode;
+  float nodata_dem, nodata_stream;
+  uint64_t input_digest;
+};
+
+static CheckpointHeader checkpoint_header(const cageo_pipeline* p, uint32_t next) {
+  CheckpointHeader h;
+  std::memset(&h, 0, sizeof(h));
+  std::memcpy(h.magic, "CAGEOCK2", 8);
+  h.width = p->W;
+  h.height = p->H;
+  h.seed = p->cfg.seed;
+  h.next_realization = next;
+  h.filter_model = p->cfg.filter_model;
+  h.practical_range = p->cfg.practical_range;
+  h.cell_size = p->cfg.cell_size;
+  h.error_mean = p->cfg.error_mean;
+  h.error_stddev = p->cfg.error_stddev;
+  h.bevel_radius = p->cfg.bevel_radius;
+  h.fill_mode = p->cfg.fill_mode;
+  h.nodata_dem = p->cfg.nodata_dem;
+  h.nodata_stream = p->cfg.nodata_stream;
+  h.input_digest = p->input_digest;
+  return h;
+}
+
+// The first header field that differs, or nullptr.  Floats compare by bits.
+static const char* checkpoint_mismatch(const CheckpointHeader& a, const CheckpointHeader& b) {
+  auto same = [](const void* x, const void* y, size_t n) { return std::memcmp(x, y, n) == 0; };
+  if (a.width != b.width || a.height != b.height) return "grid size";
+  if (a.seed != b.seed) return "seed";
+  if (a.filter_model != b.filter_model) return "filter model";
+  if (!same(&a.practical_range, &b.practical_range, 4)) return "practical range";
+  if (!same(&a.cell_size, &b.cell_size, 4)) return "cell size";
+  if (!same(&a.error_mean, &b.error_mean, 4)) return "error mean";
+  if (!same(&a.error_stddev, &b.error_stddev, 4)) return "error standard deviation";
+  if (a.bevel_radius != b.bevel_radius) return "bevel radius";
+  if (a.fill_mode != b.fill_mode) return "fill mode";
+  if (!same(&a.nodata_dem, &b.nodata_dem, 4) || !same(&a.nodata_stream, &b.nodata_stream, 4))
+    return "NODATA values";
+  if (a.input_digest != b.input_digest) return "DEM or stream grid";
+  return nullptr;
+}
+
+// The file is written beside the target as "<path>.tmp", flushed to disk and
+// renamed over the target, so a crash or kill during the write leaves the
+// previous checkpoint intact.
 static cageo_status pipeline_save(cageo_pipeline* p, const char* path,
                                   uint32_t next_realization) {
   CAGEO_CHECK_ARG(p && path, "null argument");
   std::vector<uint32_t> h((size_t)p->N);
   CAGEO_CUDA(cudaStreamSynchronize(p->stream));
   CAGEO_CUDA(cudaMemcpy(h.data(), p->counts, 4 * (size_t)p->N, cudaMemcpyDeviceToHost));
-  FILE* f = std::fopen(path, "wb");
+  const std::string tmp = std::string(path) + ".tmp";
+  FILE* f = std::fopen(tmp.c_str(), "wb");
   if (!f) {
-    set_error("unable to open \"%s\" for writing", path);
+    set_error("unable to open \"%s\" for writing", tmp.c_str());
     return CAGEO_ERR_IO;
   }
-  const int32_t wh[2] = {p->W, p->H};
-  const uint64_t seed = p->cfg.seed;
-  bool ok = std::fwrite("CAGEOCK1", 1, 8, f) == 8 && std::fwrite(wh, 4, 2, f) == 2 &&
-            std::fwrite(&seed, 8, 1, f) == 1 && std::fwrite(&next_realization, 4, 1, f) == 1 &&
+  const CheckpointHeader hd = checkpoint_header(p, next_realization);
+  bool ok = std::fwrite(&hd, sizeof(hd), 1, f) == 1 &&
             std::fwrite(h.data(), 4, h.size(), f) == h.size();
+  ok = ok && std::fflush(f) == 0 && fsync(fileno(f)) == 0;
   ok = (std::fclose(f) == 0) && ok;
   if (!ok) {
-    set_error("short write to \"%s\"", path);
+    std::remove(tmp.c_str());
+    set_error("short write to \"%s\"", tmp.c_str());
+    return CAGEO_ERR_IO;
+  }
+  if (std::rename(tmp.c_str(), path) != 0) {
+    std::remove(tmp.c_str());
+    set_error("unable to replace \"%s\"", path);
     return CAGEO_ERR_IO;
   }
   return CAGEO_OK;
@@ -598,21 +696,18 @@ static cageo_status pipeline_load(cageo_pipeline* p, const char* path,
     set_error("unable to open checkpoint \"%s\"", path);
     return CAGEO_ERR_IO;
   }
-  char magic[8];
-  int32_t wh[2];
-  uint64_t seed = 0;
-  uint32_t next = 0;
+  CheckpointHeader hd;
   std::vector<uint32_t> h((size_t)p->N);
-  bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "CAGEOCK1", 8) == 0 &&
-            std::fread(wh, 4, 2, f) == 2 && std::fread(&seed, 8, 1, f) == 1 &&
-            std::fread(&next, 4, 1, f) == 1;
-  if (ok && (wh[0] != p->W || wh[1] != p->H || seed != p->cfg.seed)) {
-    std::fclose(f);
-    set_error("checkpoint \"%s\" is for a %dx%d grid with seed %llu", path, wh[0], wh[1],
-              (unsigned long long)seed);
-    return CAGEO_ERR_FORMAT;
+  bool ok = std::fread(&hd, sizeof(hd), 1, f) == 1 && std::memcmp(hd.magic, "CAGEOCK2", 8) == 0;
+  if (ok) {
+    const CheckpointHeader mine = checkpoint_header(p, hd.next_realization);
+    if (const char* what = checkpoint_mismatch(hd, mine)) {
+      std::fclose(f);
+      set_error("checkpoint \"%s\" belongs to another run (its %s differs)", path, what);
+      return CAGEO_ERR_FORMAT;
+    }
   }
-  ok = ok && std::fread(h.data(), 4, h.size(), f) == h.size();
+  ok = ok && std::fread(h.data(), 4, h.size(), f) == h.size() && std::fgetc(f) == EOF;
   std::fclose(f);
   if (!ok) {
     set_error("\"%s\" is not a complete checkpoint", path);
@@ -620,7 +715,7 @@ static cageo_status pipeline_load(cageo_pipeline* p, const char* path,
   }
   CAGEO_CUDA(cudaStreamSynchronize(p->stream));
   CAGEO_CUDA(cudaMemcpy(p->counts, h.data(), 4 * (size_t)p->N, cudaMemcpyHostToDevice));
-  *next_realization = next;
+  *next_realization = hd.next_realization;
   return CAGEO_OK;
 }
 
@@ -768,6 +863,23 @@ extern "C" cageo_status cageo_pipeline_warmstart_stats(cageo_pipeline* p, int64_
                                                        int n) {
   CAGEO_CHECK_ARG(p && h_stats, "null argument");
   for (int i = 0; i < n && i < 8; i++) h_stats[i] = p->ws_stats[i];
+  return CAGEO_OK;
+}
+
+extern "C" cageo_status cageo_pipeline_graph_kernels(cageo_pipeline* p, int64_t* h_count) {
+  CAGEO_CHECK_ARG(p && h_count, "null argument");
+  CAGEO_CHECK_ARG(p->graph_ok && p->graph, "no realization has been captured in a CUDA graph");
+  size_t n = 0;
+  CAGEO_CUDA(cudaGraphGetNodes(p->graph, nullptr, &n));
+  std::vector<cudaGraphNode_t> nodes(n);
+  CAGEO_CUDA(cudaGraphGetNodes(p->graph, nodes.data(), &n));
+  int64_t kernels = 0;
+  for (size_t i = 0; i < n; i++) {
+    cudaGraphNodeType t;
+    CAGEO_CUDA(cudaGraphNodeGetType(nodes[i], &t));
+    kernels += t == cudaGraphNodeTypeKernel;
+  }
+  *h_count = kernels;
   return CAGEO_OK;
 }
 

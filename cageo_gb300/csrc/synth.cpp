@@ -16,6 +16,7 @@
 // indices are uint32), 2 when host memory runs out (no C++ exception
 // leaves the library).
 #include <cstdint>
+#include <cstring>
 #include <new>
 #include <queue>
 #include <vector>
@@ -24,45 +25,74 @@ static int synth_streams(const float* dem, int W, int H, int threshold, int per_
                          float nodata, float* streams_out, int* accum_out) {
   if (W < 3 || H < 3 || (int64_t)W * H >= ((int64_t)1 << 32)) return 1;
   const int64_t N = (int64_t)W * H;
+  // The flood pops cells in ascending (level, push order).  A level never
+  // falls, so every cell pushed at the level being processed goes after the
+  // ones already queued at that level: those wait in a FIFO, and only cells
+  // above the level enter the heap.  The heap key packs the level's order-
+  // preserving bits above the push counter, so one 64-bit compare orders it.
   struct Item {
-    float z;
-    int64_t order;
+    uint64_t key;  // ordered float bits << 32 | push order (N < 2^32)
     uint32_t i;
   };
   struct Cmp {
-    bool operator()(const Item& a, const Item& b) const {
-      if (a.z != b.z) return a.z > b.z;
-      return a.order > b.order;  // FIFO among equal elevations
-    }
+    bool operator()(const Item& a, const Item& b) const { return a.key > b.key; }
+  };
+  auto ordered = [](float z) {
+    uint32_t u;
+    std::memcpy(&u, &z, 4);
+    if (u == 0x80000000u) u = 0;  // -0 and +0 are one level
+    return (uint64_t)((u & 0x80000000u) ? ~u : (u | 0x80000000u));
   };
   std::priority_queue<Item, std::vector<Item>, Cmp> pq;
+  std::vector<uint32_t> level_fifo;
+  size_t fifo_head = 0;
   std::vector<uint8_t> seen(N, 0);
+  std::vector<float> zc(N);  // level at which each cell was pushed
   std::vector<uint32_t> recv(N, 0xffffffffu), pop_order;
   pop_order.reserve(N);
-  int64_t order = 0;
+  uint64_t order = 0;
   for (int y = 0; y < H; y++)
     for (int x = 0; x < W; x++)
       if (x == 0 || y == 0 || x == W - 1 || y == H - 1) {
         uint32_t i = (uint32_t)((int64_t)y * W + x);
-        pq.push({dem[i], order++, i});
+        zc[i] = dem[i];
+        pq.push({ordered(dem[i]) << 32 | order++, i});
         seen[i] = 1;
       }
   static const int dx[8] = {0, 1, 1, 1, 0, -1, -1, -1};
   static const int dy[8] = {-1, -1, 0, 1, 1, 1, 0, -1};
-  while (!pq.empty()) {
-    Item c = pq.top();
-    pq.pop();
-    pop_order.push_back(c.i);
-    int cx = (int)(c.i % (uint32_t)W), cy = (int)(c.i / (uint32_t)W);
+  uint64_t level = 0;  // ordered bits of the level being processed
+  while (!pq.empty() || fifo_head < level_fifo.size()) {
+    uint32_t ci;
+    if (!pq.empty() && (fifo_head == level_fifo.size() || (pq.top().key >> 32) == level)) {
+      ci = pq.top().i;
+      level = pq.top().key >> 32;
+      pq.pop();
+    } else {
+      ci = level_fifo[fifo_head++];
+      if (fifo_head == level_fifo.size()) {
+        level_fifo.clear();
+        fifo_head = 0;
+      }
+    }
+    const float cz = zc[ci];
+    pop_order.push_back(ci);
+    int cx = (int)(ci % (uint32_t)W), cy = (int)(ci / (uint32_t)W);
     for (int n = 0; n < 8; n++) {
       int nx = cx + dx[n], ny = cy + dy[n];
       if (nx < 0 || ny < 0 || nx >= W || ny >= H) continue;
       uint32_t ni = (uint32_t)((int64_t)ny * W + nx);
       if (seen[ni]) continue;
       seen[ni] = 1;
-      recv[ni] = c.i;
-      float z = dem[ni] < c.z ? c.z : dem[ni];
-      pq.push({z, order++, ni});
+      recv[ni] = ci;
+      float z = dem[ni] < cz ? cz : dem[ni];
+      zc[ni] = z;
+      if (ordered(z) == level) {
+        level_fifo.push_back(ni);
+        order++;
+      } else {
+        pq.push({ordered(z) << 32 | order++, ni});
+      }
     }
   }
   std::vector<int> acc(N, 1);

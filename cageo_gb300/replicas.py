@@ -1,7 +1,8 @@
 """Replicas across GPUs: realizations are independent, so N processes (one
 per GPU) run disjoint realization numbers and the per-cell border counts
 are summed once at the end -- the only exchange the Monte Carlo loop has.
-Works with any torch.distributed backend (NCCL on GPUs, gloo on CPU)."""
+NCCL reduces device tensors only, so with it the counts are reduced on the
+GPU; other backends (gloo) reduce a host copy."""
 
 
 def realization_range(rank, world, total, first=0):
@@ -21,11 +22,25 @@ def sum_counts(counts, group=None):
     return counts
 
 
+def reduces_on_device(backend):
+    """Whether a backend's all-reduce takes device tensors (NCCL) rather
+    than host tensors (gloo, mpi)."""
+    return str(backend).lower() == "nccl"
+
+
 def run(pipeline, rank, world, total, first=0, group=None):
-    """Run this rank's share on `pipeline` and return the summed float counts (CPU tensor)."""
+    """Run this rank's share on `pipeline` and return the summed float counts
+    (a host tensor)."""
     import torch
+    import torch.distributed as dist
     start, count = realization_range(rank, world, total, first)
     if count:
         pipeline.run(start, count)
+    on_device = (dist.is_available() and dist.is_initialized()
+                 and reduces_on_device(dist.get_backend(group)))
+    if on_device:
+        counts = torch.empty(pipeline.shape, dtype=torch.float32, device="cuda")
+        pipeline.counts(out=counts)
+        return sum_counts(counts, group).cpu()
     counts = torch.from_numpy(pipeline.counts())
     return sum_counts(counts, group)

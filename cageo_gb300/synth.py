@@ -61,8 +61,9 @@ def add_plateaus(dem, share=0.2, seed=0, radius=(50, 400)):
     rng = np.random.default_rng(seed + 104729)
     flat = np.zeros((H, W), bool)
     target = share * H * W
+    covered = 0  # flat.sum(), kept up to date disc by disc
     guard = 0
-    while flat.sum() < target and guard < 100000:
+    while covered < target and guard < 100000:
         guard += 1
         r = int(rng.integers(radius[0], radius[1] + 1))
         y = int(rng.integers(0, H))
@@ -71,7 +72,9 @@ def add_plateaus(dem, share=0.2, seed=0, radius=(50, 400)):
         yy, xx = np.mgrid[y0:y1, x0:x1]
         disc = (yy - y) ** 2 + (xx - x) ** 2 <= r * r
         dem[y0:y1, x0:x1][disc] = dem[y, x]
-        flat[y0:y1, x0:x1] |= disc
+        window = flat[y0:y1, x0:x1]
+        covered += int(np.count_nonzero(disc & ~window))
+        window |= disc
     return dem
 
 

@@ -96,6 +96,17 @@ cageo_status cageo_noise_philox(float* d_field, int W, int H, uint64_t seed,
                                 uint32_t realization, float mean, float stddev,
                                 cudaStream_t stream);
 
+/* The generator behind cageo_noise_philox, exposed so that it can be
+ * checked against the published Philox4x32-10 known-answer vectors (Salmon
+ * et al., SC'11; the Random123 distribution).  No counterpart in the
+ * reference (whose CPU path draws from thrust's default engine and its GPU
+ * path from cuRAND, src/randomfield/RandomFieldAlgorithmCPUOpenMP.h:56-74).
+ * d_out receives n blocks of 4 words; block i is Philox4x32-10 of the
+ * counter (h_ctr[0] + i mod 2^32, h_ctr[1], h_ctr[2], h_ctr[3]) under the key
+ * (h_key[0], h_key[1]).  0 < n < 2^31. */
+cageo_status cageo_philox4x32_10(uint32_t* d_out, int64_t n, const uint32_t* h_ctr,
+                                 const uint32_t* h_key, cudaStream_t stream);
+
 /* ---- A2 filter ----------------------------------------------------------
  * Radius used by the driver: ceil(range/cell*2.5) (src/main.cpp:110). */
 int cageo_filter_radius(float practical_range, float cell_size);
@@ -321,13 +332,23 @@ cageo_status cageo_pipeline_last_stages(cageo_pipeline* p, float* h_filled,
 cageo_status cageo_pipeline_reset_counts(cageo_pipeline* p);
 /* Checkpoint / resume of a long Monte Carlo run (no counterpart in the
  * reference, whose only persistence is the per-frame output,
- * src/main.cpp:250-256): the count grid, the seed and the next realization
- * number.  Loading refuses a checkpoint of another grid size or seed. */
+ * src/main.cpp:250-256): the count grid, the next realization number and
+ * every setting the counts depend on (grid size, seed, filter model,
+ * practical range, cell size, error mean and standard deviation, bevel
+ * radius, fill mode, NODATA values) plus a digest of the DEM and stream
+ * grids.  Loading refuses (CAGEO_ERR_FORMAT) a checkpoint that differs in
+ * any of them, or that is truncated.  Saving writes "<path>.tmp" and
+ * renames it over `path`, so an interrupted save leaves the previous
+ * checkpoint intact. */
 cageo_status cageo_pipeline_save(cageo_pipeline* p, const char* path,
                                  uint32_t next_realization);
 cageo_status cageo_pipeline_load(cageo_pipeline* p, const char* path,
                                  uint32_t* next_realization);
 cudaStream_t cageo_pipeline_stream(cageo_pipeline* p);
+/* Kernel launches in the CUDA graph that one realization replays (the
+ * graph's kernel nodes; memset nodes are not counted).  CAGEO_ERR_ARGUMENT
+ * until a run has captured the graph.  No counterpart in the reference. */
+cageo_status cageo_pipeline_graph_kernels(cageo_pipeline* p, int64_t* h_count);
 /* One realization with CUDA events between stages (fused path, no graph);
  * it is accumulated like any other.  h_ms[0..5]: noise, front
  * (convolution + realistic DEM + burning + quantization), pit fill,

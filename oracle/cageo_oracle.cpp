@@ -393,6 +393,55 @@ void orc_flow_trace(const int8_t* dir, const float* streams, int* label, int W,
   }
 }
 
+// Path statistics of a direction grid, for checking the reference walk's
+// step cap (src/flowtracing/FlowTracingAlgorithmCPUOpenMP.h:66-75: a walk
+// that has not terminated after 100001 steps gives up, and its cells take
+// cell 0's label in the connect pass).  A walk from cell c ends within its
+// path's length, the number of moves from c until one leaves the grid or
+// enters a stream cell.  out[0] = the longest such length over cells whose
+// path terminates; out[1] = the cells whose path never terminates (it
+// reaches a cell without a direction or a cycle).  Stream cells count as
+// length 0.  Iterative, memoized: O(W*H).
+void orc_trace_path_stats(const int8_t* dir, const float* streams, int W, int H,
+                          int64_t* out) {
+  const int64_t N = (int64_t)W * H;
+  const int32_t kUnknown = -1, kOnStack = -2, kNever = -3;
+  std::vector<int32_t> len(N, kUnknown);
+  std::vector<int64_t> stack;
+  int64_t longest = 0, never = 0;
+  for (int64_t s = 0; s < N; s++) {
+    if (len[s] != kUnknown) continue;
+    stack.clear();
+    int64_t c = s;
+    int32_t tail;  // length at the end of the stacked chain, or kNever
+    while (true) {
+      if (streams[c] >= 0.0f) { len[c] = 0; tail = 0; break; }
+      if (len[c] >= 0 || len[c] == kNever) { tail = len[c]; break; }
+      if (len[c] == kOnStack) { tail = kNever; break; }
+      len[c] = kOnStack;
+      stack.push_back(c);
+      const int cx = (int)(c % W) + dir[2 * c], cy = (int)(c / W) + dir[2 * c + 1];
+      if (cx < 0 || cx >= W || cy < 0 || cy >= H) { tail = 0; break; }
+      c = (int64_t)cy * W + cx;
+    }
+    // A chain that ran off the grid: its last stacked cell's move left the
+    // grid (length 1); otherwise the chain's next cell has length `tail`.
+    for (size_t k = stack.size(); k-- > 0;) {
+      const int64_t v = stack[k];
+      if (tail == kNever) {
+        len[v] = kNever;
+        never++;
+      } else {
+        len[v] = tail + 1;
+        tail = len[v];
+        if (tail > longest) longest = tail;
+      }
+    }
+  }
+  out[0] = longest;
+  out[1] = never;
+}
+
 // Catchment border: border = 1 where the label is not LAKE and some N8
 // neighbour has a larger, non-LAKE label; the Monte Carlo grid adds it
 // (float).  The reference's border grid comes from an uninitialised

@@ -25,11 +25,26 @@ def _p(a, t):
     return a.ctypes.data_as(t)
 
 
+REFERENCE_ENV = "CAGEO_REFERENCE"
+
+
+def reference_checkout():
+    """The reference checkout named by $CAGEO_REFERENCE (a directory holding
+    src/), or None when it is unset or does not hold the sources."""
+    ref = os.environ.get(REFERENCE_ENV, "")
+    return ref if ref and os.path.isdir(os.path.join(ref, "src")) else None
+
+
 def build(ref=False):
-    """Compile the restatement (and, with ref=True, the reference harness)."""
+    """Compile the restatement (and, with ref=True, the reference harness
+    from the checkout named by $CAGEO_REFERENCE)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        src = reference_checkout()
+        if src is None:
+            raise RuntimeError("set %s to a reference checkout (a directory holding src/)"
+                               % REFERENCE_ENV)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + src], check=True)
 
 
 class _Base:
@@ -132,6 +147,16 @@ class Oracle(_Base):
         if rc:
             raise ValueError("realization rejected its arguments")
         return m, filled, dirs, lab
+
+    def trace_path_stats(self, dirs, streams):
+        """(longest terminating path in moves, cells whose path never terminates)."""
+        dd = np.ascontiguousarray(dirs, np.int8)
+        s = np.ascontiguousarray(streams, np.float32)
+        H, W = s.shape
+        out = np.zeros(2, np.int64)
+        self.lib.orc_trace_path_stats(_p(dd, _i8p), _p(s, _f32p), W, H,
+                                      out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+        return int(out[0]), int(out[1])
 
     def threads(self):
         return self.lib.orc_num_threads()

@@ -26,3 +26,19 @@ def gaussian_noise(W, H, seed, sigma=1.5):
 def bits(a):
     a = np.ascontiguousarray(a)
     return a.view(np.int32) if a.dtype == np.float32 else a
+
+
+def philox_np(ctr, key):
+    """Philox4x32-10 (Salmon et al. 2011) restated with numpy uint64 arithmetic."""
+    c = [x.astype(np.uint64) for x in ctr]
+    k0, k1 = np.uint64(key[0]), np.uint64(key[1])
+    M0, M1 = np.uint64(0xD2511F53), np.uint64(0xCD9E8D57)
+    mask = np.uint64(0xFFFFFFFF)
+    for _ in range(10):
+        p0, p1 = M0 * c[0], M1 * c[2]
+        hi0, lo0 = p0 >> np.uint64(32), p0 & mask
+        hi1, lo1 = p1 >> np.uint64(32), p1 & mask
+        c = [hi1 ^ c[1] ^ k0, lo1, hi0 ^ c[3] ^ k1, lo0]
+        k0 = (k0 + np.uint64(0x9E3779B9)) & mask
+        k1 = (k1 + np.uint64(0xBB67AE85)) & mask
+    return c

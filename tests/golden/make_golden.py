@@ -6,9 +6,10 @@ Each case stores seeded inputs (DEM, stream raster, noise, filter) and the
 reference's output of every stage, run in the reference's order.  Filter
 taps are built by the library's FP64 builder and noise is seeded numpy
 noise; both are injected (the reference builds them with FFTW/Eigen and
-thrust RNG, which are not available).  Run from the repository root:
+thrust RNG, which are not available).  Run from the repository root, with
+CAGEO_REFERENCE naming the reference checkout (a directory holding src/):
 
-    python tests/golden/make_golden.py
+    CAGEO_REFERENCE=<checkout> python tests/golden/make_golden.py
 """
 import os
 import sys

@@ -6,7 +6,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from cases import make_case
+from cases import make_case, philox_np
 
 pytestmark = pytest.mark.gpu
 
@@ -65,22 +65,6 @@ def test_drainage_cli_frames_and_refusals(cuda, tmp_path):
     assert r.returncode != 0 and "don't match" in r.stdout
 
 
-def _philox_np(ctr, key):
-    """Philox4x32-10 (Salmon et al. 2011) restated with numpy uint64 arithmetic."""
-    c = [x.astype(np.uint64) for x in ctr]
-    k0, k1 = np.uint64(key[0]), np.uint64(key[1])
-    M0, M1 = np.uint64(0xD2511F53), np.uint64(0xCD9E8D57)
-    mask = np.uint64(0xFFFFFFFF)
-    for _ in range(10):
-        p0, p1 = M0 * c[0], M1 * c[2]
-        hi0, lo0 = p0 >> np.uint64(32), p0 & mask
-        hi1, lo1 = p1 >> np.uint64(32), p1 & mask
-        c = [hi1 ^ c[1] ^ k0, lo1, hi0 ^ c[3] ^ k1, lo0]
-        k0 = (k0 + np.uint64(0x9E3779B9)) & mask
-        k1 = (k1 + np.uint64(0xBB67AE85)) & mask
-    return c
-
-
 def test_noise_matches_philox_restatement(cuda):
     import torch
     from cageo_gb300 import api
@@ -89,7 +73,7 @@ def test_noise_matches_philox_restatement(cuda):
     api.noise_philox(t, seed, real, 2.0, 0.5)
     got = t.cpu().numpy().reshape(-1)
     g = np.arange(H * W // 4, dtype=np.uint64)
-    c = _philox_np([g, np.full_like(g, real), np.full_like(g, 0x63616765), np.zeros_like(g)],
+    c = philox_np([g, np.full_like(g, real), np.full_like(g, 0x63616765), np.zeros_like(g)],
                    (seed & 0xFFFFFFFF, seed >> 32))
     u = [((x >> np.uint64(8)).astype(np.float64) + 0.5) / 16777216.0 for x in c]
     z = np.empty(H * W)
@@ -165,3 +149,18 @@ def test_drainage_cli_checkpoint_resume(cuda, tmp_path):
     a = api.read_raster(str(tmp_path / "full.bin"), dem.shape)
     b = api.read_raster(str(tmp_path / "resumed.bin"), dem.shape)
     assert np.array_equal(a, b)
+    # A checkpoint holding more realizations than --iterations is refused; one
+    # holding exactly that many still writes the END output.
+    over = subprocess.run(base + ["-i", "1", "--resume", "ck.bin", "-o", "over.bin"],
+                          cwd=tmp_path, capture_output=True, text=True)
+    assert over.returncode != 0 and "more than --iterations" in over.stdout
+    assert not (tmp_path / "over.bin").exists()
+    same = subprocess.run(base + ["-i", "2", "--resume", "ck.bin", "-o", "same.bin"],
+                          cwd=tmp_path, capture_output=True, text=True)
+    assert same.returncode == 0
+    c = api.read_raster(str(tmp_path / "same.bin"), dem.shape)
+    assert c.max() <= 2 and c.sum() > 0
+    # Another practical range: the checkpoint belongs to another run.
+    other = subprocess.run(base + ["-i", "4", "--practical-range", "80", "--resume", "ck.bin"],
+                           cwd=tmp_path, capture_output=True, text=True)
+    assert other.returncode != 0 and "practical range" in other.stderr

@@ -96,6 +96,23 @@ def test_pipeline_graph_equals_direct(cuda):
     assert a.counts().max() <= 6
 
 
+def test_graph_kernel_count(cuda):
+    """The captured realization's kernel launches are counted from the graph
+    itself; a pipeline that has not captured one refuses."""
+    from cageo_gb300 import api
+    dem, streams = make_case(160, 128, seed=14)
+    p = api.Pipeline(dem, streams, seed=2, use_graphs=True)
+    with pytest.raises(api.CageoError):
+        p.graph_kernels()
+    p.run(0, 3)
+    n = p.graph_kernels()
+    assert 10 <= n <= 64
+    q = api.Pipeline(dem, streams, seed=2, use_graphs=False)
+    q.run(0, 1)
+    with pytest.raises(api.CageoError):
+        q.graph_kernels()
+
+
 def test_checkpoint_resume(cuda, tmp_path):
     from cageo_gb300 import api
     dem, streams = make_case(120, 90, seed=31)
@@ -109,8 +126,68 @@ def test_checkpoint_resume(cuda, tmp_path):
     c.run(3, 2)
     assert np.array_equal(a.counts(), c.counts())
     other = api.Pipeline(dem, streams, seed=5)
-    with pytest.raises(api.CageoError):
+    with pytest.raises(api.CageoError, match="seed"):
         other.load(str(tmp_path / "ck.bin"))
+
+
+@pytest.mark.parametrize("change,field", [
+    (dict(practical_range=80.0), "practical range"),
+    (dict(error_stddev=2.0), "error standard deviation"),
+    (dict(filter_model=0, practical_range=30.0), "filter model"),
+    (dict(bevel_radius=3), "bevel radius"),
+    (dict(fill_mode=1), "fill mode"),
+    (dict(nodata_stream=-1.0), "NODATA"),
+    ("dem", "DEM or stream grid"),
+    ("streams", "DEM or stream grid"),
+])
+def test_checkpoint_refuses_another_run(cuda, tmp_path, change, field):
+    """A checkpoint records every setting the counts depend on and a digest
+    of the input grids; loading it into a pipeline that differs in any of
+    them is refused (its counts would mix two distributions)."""
+    from cageo_gb300 import api
+    dem, streams = make_case(96, 72, seed=33)
+    a = api.Pipeline(dem, streams, seed=4)
+    a.run(0, 1)
+    a.save(str(tmp_path / "ck.bin"), 1)
+    kw, d2, s2 = dict(seed=4), dem, streams
+    if change == "dem":
+        d2 = dem.copy()
+        d2[10, 10] += 0.5
+    elif change == "streams":
+        s2 = streams.copy()
+        s2[5, 7] = 1.0 if s2[5, 7] < 0 else -9999.0
+    else:
+        kw.update(change)
+    b = api.Pipeline(d2, s2, **kw)
+    with pytest.raises(api.CageoError, match=field):
+        b.load(str(tmp_path / "ck.bin"))
+    same = api.Pipeline(dem, streams, seed=4)
+    assert same.load(str(tmp_path / "ck.bin")) == 1
+
+
+def test_checkpoint_survives_an_interrupted_save(cuda, tmp_path):
+    """A save writes "<path>.tmp" and renames it over the checkpoint: a save
+    killed part-way (a truncated .tmp left behind) leaves the previous
+    checkpoint whole, and the next save replaces both."""
+    from cageo_gb300 import api
+    dem, streams = make_case(96, 72, seed=35)
+    a = api.Pipeline(dem, streams, seed=6)
+    a.run(0, 2)
+    ck = tmp_path / "ck.bin"
+    a.save(str(ck), 2)
+    size = ck.stat().st_size
+    (tmp_path / "ck.bin.tmp").write_bytes(ck.read_bytes()[: size // 3])
+    b = api.Pipeline(dem, streams, seed=6)
+    assert b.load(str(ck)) == 2
+    assert np.array_equal(a.counts(), b.counts())
+    a.run(2, 1)
+    a.save(str(ck), 3)
+    assert not (tmp_path / "ck.bin.tmp").exists()
+    assert b.load(str(ck)) == 3
+    # a truncated checkpoint itself is refused, not half-loaded
+    (tmp_path / "cut.bin").write_bytes(ck.read_bytes()[: size - 4])
+    with pytest.raises(api.CageoError, match="not a complete checkpoint"):
+        b.load(str(tmp_path / "cut.bin"))
 
 
 def test_autotune_keeps_counts(cuda):

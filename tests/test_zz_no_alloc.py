@@ -26,24 +26,58 @@ def _burned_dem(api, cuda, W, H, seed):
     return field
 
 
-def test_static_fill_matches_allocating_fill(cuda):
+def _fill_both(lib, api, cuda, src, mode, stream):
+    """(static result, allocating result), each as (dem after the call, filled)."""
+    import torch
+    H, W = src.shape
+    a, b = src.clone(), src.clone()
+    fa, fb = torch.empty_like(src), torch.empty_like(src)
+    st = lib.cageo_pitfill_static(ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(fa.data_ptr()),
+                                  W, H, -9999.0, mode, stream)
+    assert st == 0, lib.cageo_last_error_string().decode()
+    st = lib.cageo_pitfill(ctypes.c_void_p(b.data_ptr()), ctypes.c_void_p(fb.data_ptr()), W, H,
+                           -9999.0, mode, None, 0, stream)
+    assert st == 0, lib.cageo_last_error_string().decode()
+    torch.cuda.synchronize()
+    return (a.cpu().numpy(), fa.cpu().numpy()), (b.cpu().numpy(), fb.cpu().numpy())
+
+
+@pytest.mark.parametrize("modes", [("compat", "compat"), ("compat", "exact"), ("exact", "compat")])
+def test_static_fill_matches_allocating_fill(cuda, modes):
+    """Two calls in a row on different grids, in either fill mode: the
+    second runs on the scratch the first left behind."""
     import torch
     from cageo_gb300 import api
     lib = api.lib()
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    for W, H, seed in [(512, 512, 31), (257, 131, 32)]:
+    code = {"compat": api.FILL_CPU_COMPAT, "exact": api.FILL_EXACT}
+    for (W, H, seed), mode in zip([(512, 512, 31), (257, 131, 32)], modes):
         src = _burned_dem(api, cuda, W, H, seed)
-        a, b = src.clone(), src.clone()
-        fa, fb = torch.empty_like(src), torch.empty_like(src)
-        st = lib.cageo_pitfill_static(ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(fa.data_ptr()),
-                                      W, H, -9999.0, api.FILL_CPU_COMPAT, stream)
-        assert st == 0, lib.cageo_last_error_string().decode()
-        st = lib.cageo_pitfill(ctypes.c_void_p(b.data_ptr()), ctypes.c_void_p(fb.data_ptr()), W, H,
-                               -9999.0, api.FILL_CPU_COMPAT, None, 0, stream)
-        assert st == 0, lib.cageo_last_error_string().decode()
+        (qa, fa), (qb, fb) = _fill_both(lib, api, cuda, src, code[mode], stream)
+        assert np.array_equal(bits(qa), bits(qb)), "DEM after the fill (%s)" % mode
+        assert np.array_equal(bits(fa), bits(fb)), "filled DEM (%s)" % mode
+
+
+def test_static_fill_allocates_no_device_memory(cuda):
+    """After its first call on a device (which looks up the scratch
+    array's address), a call changes the device's free memory by nothing."""
+    import torch
+    from cageo_gb300 import api
+    lib = api.lib()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    src = _burned_dem(api, cuda, 384, 320, 41)
+    dem, filled = src.clone(), torch.empty_like(src)
+    args = (ctypes.c_void_p(dem.data_ptr()), ctypes.c_void_p(filled.data_ptr()), 384, 320,
+            -9999.0, api.FILL_CPU_COMPAT, stream)
+    assert lib.cageo_pitfill_static(*args) == 0
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for mode in (api.FILL_CPU_COMPAT, api.FILL_EXACT):
+        dem.copy_(src)
+        assert lib.cageo_pitfill_static(*args[:5], mode, stream) == 0, \
+            lib.cageo_last_error_string().decode()
         torch.cuda.synchronize()
-        assert np.array_equal(bits(a.cpu().numpy()), bits(b.cpu().numpy())), "quantized DEM"
-        assert np.array_equal(bits(fa.cpu().numpy()), bits(fb.cpu().numpy())), "filled DEM"
+        assert torch.cuda.mem_get_info()[0] == free0
 
 
 def test_static_fill_refuses_grids_beyond_its_scratch(cuda):
