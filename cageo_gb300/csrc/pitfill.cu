@@ -38,9 +38,11 @@
 
 namespace cageo {
 
-// Per-cell flag bits.
+// Per-cell flag bits.  FCLEAN (flood A with clean marks): the cell's level
+// is reached by a path of passable relays from an outlet, so flood B, whose
+// walls are non-passable cells only, gives it the same value.
 constexpr uint8_t FNODATA = 0x01, FOUTLET = 0x02, FNONPASS = 0x04, FCONF = 0x08,
-                  FBELOW = 0x10, FBELOWA = 0x20, FUNSURE = 0x80;
+                  FBELOW = 0x10, FBELOWA = 0x20, FCLEAN = 0x40, FUNSURE = 0x80;
 
 // Scalar block layout (unsigned ints).
 enum : int {
@@ -92,6 +94,10 @@ struct WarpSmem {
   float R[34 * kRS];
   float2 WQ[kTile * kWS];  // (W, q) of the tile's own cells
   uint8_t F[kTile * kFS];
+  // Clean relays of the halo (flood A with clean marks): [0] the row above
+  // and [1] the row below the tile (halo x 0..33), [2] the column left and
+  // [3] the column right of it (halo y 0..33); 1 = clean and passable.
+  uint8_t HC[4][34];
 };
 
 size_t fill_workspace_bytes(int W, int H) {
@@ -131,11 +137,14 @@ FillWork fill_carve(void* base, int W, int H) {
 
 unsigned int* fill_min_slot(const FillWork& w) { return w.scal + S_MIN; }
 
+// Flood modes: 0 = flood A (every reached cell relays), 2 = flood A that
+// also keeps the clean marks (FCLEAN), 1 = flood B (non-passable cells that
+// are not confirmed are walls).
 template <int MODE>
 __device__ __forceinline__ float relay(float w, uint8_t f, float q) {
   if (f & FNODATA) return kInf;
   if (f & FOUTLET) return (f & FNONPASS) ? kInf : q;
-  if (MODE == 0 || !(f & FNONPASS)) return w;
+  if (MODE != 1 || !(f & FNONPASS)) return w;
   return ((f & FCONF) && !(f & FBELOW)) ? w : kInf;
 }
 
@@ -255,7 +264,10 @@ __device__ __forceinline__ bool cell_store(WarpSmem& s, int x, int y, const Cell
   const bool below = e.m < e.q;  // sets FBELOW, which the cell does not have yet
   if (nw == e.w && !below) return false;
   s.WQ[y * kWS + x].x = nw;
-  if (below) s.F[y * kFS + x] = e.f | FBELOW;
+  // A fall of W withdraws the cell's clean mark (its clean path may not
+  // reach the new level); the clean pass after the sweeps derives it again.
+  if (MODE == 2 && nw != e.w) s.F[y * kFS + x] = (e.f | (below ? FBELOW : 0)) & (uint8_t)~FCLEAN;
+  else if (below) s.F[y * kFS + x] = e.f | FBELOW;
   // relay<MODE>() of a cell that is neither NODATA nor an outlet
   const bool wall = MODE == 1 && (e.f & FNONPASS) && (below || !(e.f & FCONF));
   s.R[(y + 1) * kRS + (x + 1)] = wall ? kInf : nw;
@@ -287,15 +299,89 @@ struct VisitStats {
 template <int MODE>
 __device__ __forceinline__ void flush_stats(const FillWork& w, VisitStats& st) {
   if (!st.tiles) return;
-  atomicAdd(&w.scal[MODE == 0 ? S_TILES_A : S_TILES_B], st.tiles);
-  atomicAdd(&w.scal[MODE == 0 ? S_ROUNDS_A : S_ROUNDS_B], st.rounds);
+  atomicAdd(&w.scal[MODE != 1 ? S_TILES_A : S_TILES_B], st.tiles);
+  atomicAdd(&w.scal[MODE != 1 ? S_ROUNDS_A : S_ROUNDS_B], st.rounds);
   atomicAdd(&w.scal[S_KCYC_LOAD], st.kload);
   atomicAdd(&w.scal[S_KCYC_SWEEP], st.ksweep);
   atomicAdd(&w.scal[S_KCYC_STORE], st.kstore);
   st = VisitStats{};
 }
 
-// Returns whether every cell of the tile is final (NODATA, outlet or FBELOW).
+// Clean marks of a tile whose W has converged for its halo (flood A with
+// clean marks).  A cell turns clean when a neighbour that is clean and
+// passable (a relay flood B keeps) offers a level <= its W: that
+// neighbour's clean path, extended by the cell, reaches the cell at no more
+// than W, and flood B, which never undershoots flood A, then gives it W
+// too.  The rule is sound whatever W is, so a cell keeps its mark until its
+// W falls (cell_store withdraws it).  Lane = tile column x; per-lane masks
+// hold bit y for tile row y.  The eight "offers <= W" tests are made once
+// per cell; the marks then spread by bit operations on the column masks
+// (neighbour columns by shuffles) until no lane changes, at most
+// `max_iter` times.  Returns this lane's column of newly clean cells.
+__device__ __forceinline__ unsigned int clean_pass(WarpSmem& s, int lane, int max_iter) {
+  unsigned int qN = 0, qS = 0, qW = 0, qE = 0, qNW = 0, qNE = 0, qSW = 0, qSE = 0;
+  unsigned int cl = 0, pas = 0;
+  // Relay rows y, y+1, y+2 (tile rows y-1, y, y+1) at columns lane..lane+2.
+  float a0 = s.R[lane], a1 = s.R[lane + 1], a2 = s.R[lane + 2];
+  float b0 = s.R[kRS + lane], b1 = s.R[kRS + lane + 1], b2 = s.R[kRS + lane + 2];
+#pragma unroll 4
+  for (int y = 0; y < kTile; y++) {
+    const float* rc = &s.R[(y + 2) * kRS + lane];
+    const float c0 = rc[0], c1 = rc[1], c2 = rc[2];
+    const uint8_t f = s.F[y * kFS + lane];
+    const unsigned int bit = 1u << y;
+    // b1 is the cell's own relay: its W (every non-outlet cell relays in flood A).
+    const float wv = b1;
+    if (f & FCLEAN) cl |= bit;
+    if (!(f & (FNONPASS | FNODATA))) pas |= bit;
+    if (!(f & (FCLEAN | FNODATA)) && wv < kInf) {
+      if (a0 <= wv) qNW |= bit;
+      if (a1 <= wv) qN |= bit;
+      if (a2 <= wv) qNE |= bit;
+      if (b0 <= wv) qW |= bit;
+      if (b2 <= wv) qE |= bit;
+      if (c0 <= wv) qSW |= bit;
+      if (c1 <= wv) qS |= bit;
+      if (c2 <= wv) qSE |= bit;
+    }
+    a0 = b0; a1 = b1; a2 = b2;
+    b0 = c0; b1 = c1; b2 = c2;
+  }
+  const unsigned int cl0 = cl;
+  if (!__any_sync(0xffffffffu, (qN | qS | qW | qE | qNW | qNE | qSW | qSE) != 0)) return 0u;
+  // Clean relays of the halo: this lane's cells of the rows above and below
+  // the tile, and the halo columns as 34-bit masks (bit = halo row 0..33).
+  const unsigned long long top = s.HC[0][lane + 1], bot = s.HC[1][lane + 1];
+  unsigned long long lcol = __ballot_sync(0xffffffffu, s.HC[2][lane] != 0);
+  unsigned long long rcol = __ballot_sync(0xffffffffu, s.HC[3][lane] != 0);
+  lcol |= ((unsigned long long)s.HC[2][32] << 32) | ((unsigned long long)s.HC[2][33] << 33);
+  rcol |= ((unsigned long long)s.HC[3][32] << 32) | ((unsigned long long)s.HC[3][33] << 33);
+  for (int it = 0; it < max_iter; it++) {
+    // Column mask of clean relays, bit = halo row (tile row + 1).
+    const unsigned long long own = ((unsigned long long)(cl & pas) << 1) | top | (bot << 33);
+    unsigned long long L = __shfl_up_sync(0xffffffffu, own, 1);
+    unsigned long long R = __shfl_down_sync(0xffffffffu, own, 1);
+    if (lane == 0) L = lcol;
+    if (lane == 31) R = rcol;
+    const unsigned int nc =
+        cl | (qN & (unsigned int)own) | (qS & (unsigned int)(own >> 2)) |
+        (qW & (unsigned int)(L >> 1)) | (qE & (unsigned int)(R >> 1)) | (qNW & (unsigned int)L) |
+        (qNE & (unsigned int)R) | (qSW & (unsigned int)(L >> 2)) | (qSE & (unsigned int)(R >> 2));
+    const bool changed = nc != cl;
+    cl = nc;
+    if (!__any_sync(0xffffffffu, changed)) break;
+  }
+  const unsigned int turned = cl & ~cl0;
+  for (unsigned int m = turned; m; m &= m - 1) {
+    const int y = __ffs(m) - 1;
+    s.F[y * kFS + lane] |= FCLEAN;
+  }
+  __syncwarp();
+  return turned;
+}
+
+// Returns whether every cell of the tile is final (NODATA, outlet or FBELOW;
+// with clean marks also clean).
 template <int MODE>
 __device__ bool process_tile(WarpSmem& s, const FloodArgs& a, int t, int lane, VisitStats& st) {
   const FillWork& w = a.w;
@@ -319,6 +405,20 @@ __device__ bool process_tile(WarpSmem& s, const FloodArgs& a, int t, int lane, V
     if (hx >= 1 && hx <= kTile && hy >= 1 && hy <= kTile) {
       s.WQ[(hy - 1) * kWS + hx - 1] = make_float2(wv, qv);
       s.F[(hy - 1) * kFS + hx - 1] = fv;
+    }
+  }
+  if (MODE == 2) {
+    // Clean relays of the halo: strips of 34 cells (row above, row below,
+    // column left, column right), flags read again from L2.  A loop of its
+    // own keeps the staging loop above as it is in the other modes.
+    for (int k = lane; k < 4 * 34; k += 32) {
+      const int strip = k / 34, j = k - strip * 34;
+      const int hx = strip < 2 ? j : (strip == 2 ? 0 : 33);
+      const int hy = strip < 2 ? (strip == 0 ? 0 : 33) : j;
+      const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
+      uint8_t fv = FNODATA;
+      if (gx >= 0 && gx < W && gy >= 0 && gy < H) fv = __ldcg(w.flags + (int64_t)gy * W + gx);
+      s.HC[strip][j] = (fv & (FCLEAN | FNONPASS | FNODATA)) == FCLEAN;
     }
   }
   __syncwarp();
@@ -401,6 +501,9 @@ __device__ bool process_tile(WarpSmem& s, const FloodArgs& a, int t, int lane, V
     }
   }
   const bool capped = (pd | pu | pr | pl) != 0;
+  // Each round of the clean pass marks at least one more cell, so 1024
+  // rounds always reach its fixpoint.
+  if (MODE == 2) dc |= clean_pass(s, lane, kTile * kTile);
   const long long c2 = clock64();
   if (lane == 0) {
     w.tconv[t] = capped ? 0 : 1;
@@ -433,8 +536,12 @@ __device__ bool process_tile(WarpSmem& s, const FloodArgs& a, int t, int lane, V
   bool done = false;
   if (rows_changed || !revisit) {
     bool fin = true;
-    for (int idx = lane; idx < kTile * kTile; idx += 32)
-      fin &= (s.F[(idx >> 5) * kFS + (idx & 31)] & (FNODATA | FOUTLET | FBELOW)) != 0;
+    for (int idx = lane; idx < kTile * kTile; idx += 32) {
+      const uint8_t f = s.F[(idx >> 5) * kFS + (idx & 31)];
+      fin &= (f & (FNODATA | FOUTLET | FBELOW)) != 0;
+      // With clean marks, a cell that may still turn clean is not final.
+      if (MODE == 2) fin &= (f & (FNODATA | FCLEAN)) != 0;
+    }
     done = __all_sync(0xffffffffu, fin);
   }
   // Lanes 0..8 queue self (if capped) and the 8 neighbours whose halo changed.
@@ -524,7 +631,7 @@ __device__ bool drain(WarpSmem& s, const FloodArgs& a, int lane, int ntiles) {
       break;
     }
     if (vs[S_PENDING] == 0u) break;
-    if (++idle > (1LL << 24) || vs[MODE == 0 ? S_TILES_A : S_TILES_B] > visit_cap) {
+    if (++idle > (1LL << 24) || vs[MODE != 1 ? S_TILES_A : S_TILES_B] > visit_cap) {
       if (lane == 0) atomicCAS((int*)(w.scal + S_ERR), 0, 2);
       ok = false;
       break;
@@ -638,7 +745,7 @@ fill_flood_kernel(FloodArgs a) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     vs[S_PASS] = (unsigned int)p;
     const unsigned int us = (unsigned int)((global_ns() - t_start) / 1000);
-    if (MODE == 0) {
+    if (MODE != 1) {
       vs[S_PASSES_A] = (unsigned int)(p - p0 + 1);
       vs[S_US_A] = us;
     } else if (!phases) {
@@ -690,7 +797,8 @@ __global__ void fill_init_kernel(const float* __restrict__ q, float* __restrict_
       f = FNODATA;
     } else {
       if (!passable_quantized(qv, minE)) f |= FNONPASS;
-      if (x == 0 || y == 0 || x == W - 1 || y == H - 1 || qv == 0.0f) f |= FOUTLET;
+      // Outlets keep q in both floods: clean from the start.
+      if (x == 0 || y == 0 || x == W - 1 || y == H - 1 || qv == 0.0f) f |= FOUTLET | FCLEAN;
     }
     F[i] = f;
     Wg[i] = (f & (FNODATA | FOUTLET)) ? qv : kInf;
@@ -732,45 +840,73 @@ __global__ void fill_final_exact_kernel(float* __restrict__ Wg, int64_t n) {
 }
 
 // Between the floods: keep flood A's result (lower bound) in aux and
-// FBELOWA, confirm non-passable cells reached at a level >= q, reset W.
-// Also clears the worklist counts: flood A's last count slot is the one
-// flood B's first pass appends to.
+// FBELOWA, confirm non-passable cells reached at a level >= q, and start
+// flood B.  A clean cell keeps flood A's value and below-q flag, which flood
+// B would give it too (every value flood B relays is a passable level, so a
+// non-passable cell's incoming level never equals its q, and a clean cell's
+// level is reached by a path flood B keeps); every other cell restarts from
+// +inf and marks its tile for flood B (tseed).  Also resets the work queue.
 __global__ void fill_classify_kernel(float* __restrict__ Wg, uint8_t* __restrict__ F,
-                                     uint32_t* __restrict__ aux, unsigned int* scal, int64_t n) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+                                     uint32_t* __restrict__ aux, unsigned int* scal,
+                                     uint8_t* __restrict__ tseed, int tiles_x, int W) {
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
     scal[S_HEAD] = 0u;
     scal[S_TAIL] = 0u;
     scal[S_PENDING] = 0u;
   }
+  const int y = blockIdx.y;
 #pragma unroll
   for (int k = 0; k < kCellsPerThread; k++) {
-    const int64_t i = ((int64_t)blockIdx.x * kCellsPerThread + k) * blockDim.x + threadIdx.x;
-    if (i >= n) break;
+    const int x = (blockIdx.x * kCellsPerThread + k) * blockDim.x + threadIdx.x;
+    if (x >= W) break;
+    const int64_t i = (int64_t)y * W + x;
     uint8_t f = F[i];
     const float wa = Wg[i];
     aux[i] = __float_as_uint(wa);
     if (f & (FNODATA | FOUTLET)) continue;
     if ((f & FNONPASS) && !(f & FBELOW) && wa < kInf) f |= FCONF;
     if (f & FBELOW) f |= FBELOWA;
-    F[i] = f & (uint8_t)~FBELOW;
-    Wg[i] = kInf;
+    if (f & FCLEAN) {
+      F[i] = f;
+    } else {
+      F[i] = f & (uint8_t)~FBELOW;
+      Wg[i] = kInf;
+      tseed[(y / kTile) * tiles_x + x / kTile] = 1;
+    }
   }
+}
+
+// Flood B's tile states: a tile without a cell to recompute is done from
+// the start (its cells hold flood B's values already); the others are idle.
+__global__ void fill_tile_states_kernel(int* __restrict__ queued, const uint8_t* __restrict__ tseed,
+                                        int ntiles) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < ntiles) queued[t] = tseed[t] ? kIdle : kDone;
 }
 
 // Between flood B's two launches: the undecided cells -- flood A's lower
 // bound (aux) and flood B's upper bound (Wg) differ in value, or in the
 // blocked status of a non-passable cell -- are flagged FUNSURE, labelled
-// with their own index and appended to the candidate list.  Four cells per
+// with their own index and appended to the candidate list.  Only tiles that
+// held a cell to recompute (tseed) are read: a clean cell kept flood A's
+// value and flag.  One block per tile, one row segment of 4 cells per
 // thread; the filled grid is the caller's and is read as float4 only when
-// it is 16-byte aligned.
+// the row segment is 16-byte aligned.
 __global__ void fill_undecided_kernel(const float* __restrict__ Wg, uint8_t* __restrict__ F,
                                       uint32_t* __restrict__ aux, uint32_t* __restrict__ cand,
-                                      unsigned int* scal, int64_t n) {
-  const int64_t b4 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
-  if (b4 >= n) return;
+                                      unsigned int* scal, const uint8_t* __restrict__ tseed,
+                                      int tiles_x, int W, int H) {
+  const int t = blockIdx.x;
+  if (!tseed[t]) return;
+  const int y = (t / tiles_x) * kTile + (int)(threadIdx.x >> 3);
+  const int x = (t % tiles_x) * kTile + (int)(threadIdx.x & 7) * 4;
+  if (y >= H || x >= W) return;
+  const int64_t b4 = (int64_t)y * W + x;
   uint8_t fv[4];
   float wav[4], wbv[4];
-  if (b4 + 4 <= n && (((uintptr_t)Wg) & 15u) == 0) {
+  // b4 % 4 == 0 aligns the workspace arrays (256-byte aligned bases);
+  // the caller's grid is checked on its own.
+  if (x + 4 <= W && (b4 & 3) == 0 && ((uintptr_t)(Wg + b4) & 15u) == 0) {
     const uchar4 f4 = *reinterpret_cast<const uchar4*>(F + b4);
     const uint4 a4 = *reinterpret_cast<const uint4*>(aux + b4);
     const float4 w4 = *reinterpret_cast<const float4*>(Wg + b4);
@@ -781,7 +917,7 @@ __global__ void fill_undecided_kernel(const float* __restrict__ Wg, uint8_t* __r
   } else {
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      const bool in = b4 + k < n;
+      const bool in = x + k < W;
       fv[k] = in ? F[b4 + k] : FNODATA;
       wav[k] = in ? __uint_as_float(aux[b4 + k]) : 0.0f;
       wbv[k] = in ? Wg[b4 + k] : 0.0f;
@@ -913,17 +1049,20 @@ cageo_status fill_run(const float* q, float* filled, const FillWork& w, float no
   CAGEO_CUDA(cudaMemsetAsync(w.queued, 0, sizeof(int) * nt, s));  // all idle
   CAGEO_CUDA(cudaMemsetAsync(w.tconv, 0, nt, s));
   CAGEO_CUDA(cudaMemsetAsync(w.lists, 0xff, (2 * nt + kRingSlack) * sizeof(int), s));  // empty ring
-  cageo_status st = launch_flood<0>(a, s);
+  cageo_status st = launch_flood<2>(a, s);  // flood A with clean marks
   if (st) return st;
-  fill_classify_kernel<<<blocks, 256, 0, s>>>(filled, w.flags, w.aux, w.scal, n);
+  CAGEO_CUDA(cudaMemsetAsync(w.tseed, 0, nt, s));
+  fill_classify_kernel<<<rows, 256, 0, s>>>(filled, w.flags, w.aux, w.scal, w.tseed, w.tiles_x,
+                                            w.W);
+  fill_tile_states_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(w.queued, w.tseed,
+                                                                       (int)nt);
   CAGEO_CUDA(cudaGetLastError());
-  CAGEO_CUDA(cudaMemsetAsync(w.queued, 0, sizeof(int) * nt, s));  // all idle
   CAGEO_CUDA(cudaMemsetAsync(w.tconv, 0, nt, s));
-  a.stage = 1;  // flood B's main drain
+  a.stage = 1;  // flood B's main drain, from the tiles holding a cell to recompute
   st = launch_flood<1>(a, s);
   if (st) return st;
-  const unsigned vblocks = (unsigned)((n + 4 * 256 - 1) / (4 * 256));
-  fill_undecided_kernel<<<vblocks, 256, 0, s>>>(filled, w.flags, w.aux, w.cand, w.scal, n);
+  fill_undecided_kernel<<<(unsigned)nt, 256, 0, s>>>(filled, w.flags, w.aux, w.cand, w.scal,
+                                                     w.tseed, w.tiles_x, w.W, w.H);
   const unsigned ublocks = (unsigned)std::min<int64_t>((n + 255) / 256, 2048);
   fill_unite_kernel<<<ublocks, 256, 0, s>>>(w.cand, w.scal, w.flags, w.aux, w.W);
   fill_flatten_kernel<<<ublocks, 256, 0, s>>>(w.cand, w.scal, w.aux);
