@@ -44,6 +44,20 @@ class PipelineConfig(ctypes.Structure):
                 ("fill_mode", ctypes.c_int)]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("fill_rounds", ctypes.c_int), ("fill_warps", ctypes.c_int)]
+
+    def as_dict(self):
+        return {"fill_rounds": self.fill_rounds, "fill_warps": self.fill_warps}
+
+
+def autotune_candidates():
+    n = lib().cageo_autotune_candidates(None, 0)
+    arr = (Tuning * n)()
+    lib().cageo_autotune_candidates(ctypes.cast(arr, _vp), n)
+    return [t.as_dict() for t in arr]
+
+
 class RasterInfo(ctypes.Structure):
     _fields_ = [("ncols", ctypes.c_int), ("nrows", ctypes.c_int),
                 ("xllcorner", ctypes.c_double), ("yllcorner", ctypes.c_double),
@@ -98,7 +112,10 @@ _SIGS = {
     "cageo_pipeline_profile": ([_vp, ctypes.c_uint32, _vp, _i], _i),
     "cageo_pipeline_destroy": ([_vp], None),
     "cageo_pipeline_set_warmstart": ([_vp, _vp, _i, _f], _i),
-    "cageo_pipeline_autotune": ([_vp, ctypes.c_uint32, _i, _vp, _vp], _i),
+    "cageo_pipeline_autotune": ([_vp, ctypes.c_uint32, _i, _vp, _vp, _i], _i),
+    "cageo_autotune_candidates": ([_vp, _i], _i),
+    "cageo_pipeline_set_tuning": ([_vp, _vp], _i),
+    "cageo_pipeline_get_tuning": ([_vp, _vp], _i),
     "cageo_pipeline_warmstart_stats": ([_vp, _vp, _i], _i),
     "cageo_to_bytes": ([_vp, _vp, _i, _i, _vp], _i),
     "cageo_write_jpeg": ([ctypes.c_char_p, _vp, _i, _i, _i], _i),
@@ -426,13 +443,24 @@ class Pipeline:
     STAGES = ("noise", "front", "fill", "route", "trace", "border")
 
     def autotune(self, first, trials=3):
-        """Pick the fill's sweep rounds per tile visit by timing; resets the
-        counts.  Returns (chosen rounds, {rounds: ms per realization})."""
-        best = ctypes.c_int()
-        ms = np.zeros(5, np.float32)
+        """Pick the fill's tuning (sweep rounds per tile visit, warps per SM
+        of the lower-bound flood) by timing every candidate; resets the
+        counts.  Returns (chosen tuning, [(candidate, ms per realization)])."""
+        cands = autotune_candidates()
+        best = Tuning()
+        ms = np.zeros(len(cands), np.float32)
         _check(lib().cageo_pipeline_autotune(self._p, first, trials, ctypes.byref(best),
-                                             ms.ctypes.data_as(_vp)))
-        return best.value, dict(zip((4, 8, 16, 32, 64), (float(v) for v in ms)))
+                                             ms.ctypes.data_as(_vp), len(cands)))
+        return best.as_dict(), [(c, float(v)) for c, v in zip(cands, ms)]
+
+    def set_tuning(self, fill_rounds, fill_warps):
+        _check(lib().cageo_pipeline_set_tuning(self._p, ctypes.byref(Tuning(fill_rounds,
+                                                                            fill_warps))))
+
+    def tuning(self):
+        t = Tuning()
+        _check(lib().cageo_pipeline_get_tuning(self._p, ctypes.byref(t)))
+        return t.as_dict()
 
     def set_warmstart(self, params, threshold):
         """Learned warm start (exact mode); params None switches it off."""

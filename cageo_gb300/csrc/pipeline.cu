@@ -779,26 +779,67 @@ extern "C" cageo_status cageo_pipeline_reset_counts(cageo_pipeline* p) {
   return CAGEO_OK;
 }
 
-// Autotuning of the fill's sweep rounds per tile visit (the halo-sweep
-// count): each candidate runs `trials` realizations on the fast path
-// (direct launches, timed with events on the pipeline's stream); the
-// fastest is kept and the CUDA graph is captured again on the next run.
-// The counts are reset to zero afterwards.
+// Candidate settings of the autotuner: sweep rounds per fill tile visit x
+// warps per SM of the fill's lower-bound flood.
+static const int kTuneRounds[3] = {16, 32, 64};
+static const int kTuneWarps[3] = {16, 20, 22};
+constexpr int kTuneCandidates = 9;
+
+extern "C" int cageo_autotune_candidates(cageo_tuning* h_out, int n) {
+  for (int k = 0; h_out && k < n && k < kTuneCandidates; k++) {
+    h_out[k].fill_rounds = kTuneRounds[k % 3];
+    h_out[k].fill_warps = kTuneWarps[k / 3];
+  }
+  return kTuneCandidates;
+}
+
+static void drop_graph(cageo_pipeline* p) {
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  p->exec = nullptr;
+  p->graph = nullptr;
+  p->graph_ok = false;
+}
+
+extern "C" cageo_status cageo_pipeline_set_tuning(cageo_pipeline* p, const cageo_tuning* t) {
+  CAGEO_CHECK_ARG(p && t, "null argument");
+  CAGEO_CHECK_ARG(t->fill_rounds >= 1 && t->fill_rounds <= 1024, "fill rounds must be 1..1024");
+  CAGEO_CHECK_ARG(fill_flood_warps_valid(t->fill_warps), "fill warps must be 16, 20 or 22");
+  CAGEO_CUDA(cudaStreamSynchronize(p->stream));
+  p->fw.max_rounds = t->fill_rounds;
+  p->fw.flood_warps = t->fill_warps;
+  drop_graph(p);  // captured with the old launch shapes
+  return CAGEO_OK;
+}
+
+extern "C" cageo_status cageo_pipeline_get_tuning(cageo_pipeline* p, cageo_tuning* t) {
+  CAGEO_CHECK_ARG(p && t, "null argument");
+  t->fill_rounds = p->fw.max_rounds;
+  t->fill_warps = p->fw.flood_warps;
+  return CAGEO_OK;
+}
+
+// Autotuning: each candidate runs one warm-up and `trials` realizations on
+// the fast path (direct launches, timed with events on the pipeline's
+// stream); the fastest is kept and the CUDA graph is captured again on the
+// next run.  The counts are reset to zero afterwards.
 extern "C" cageo_status cageo_pipeline_autotune(cageo_pipeline* p, uint32_t first, int trials,
-                                                int* h_best_rounds, float* h_ms) {
+                                                cageo_tuning* h_best, float* h_ms, int n_ms) {
   CAGEO_CHECK_ARG(p && trials >= 1, "pipeline and trials");
   CAGEO_CHECK_ARG(p->cfg.nodata_dem != 0.0f && !p->ws_params,
                   "autotuning times the fused path (NODATA != 0, no warm start)");
-  static const int kCand[5] = {4, 8, 16, 32, 64};
   cudaStream_t s = p->stream;
   cudaEvent_t e0, e1;
   CAGEO_CUDA(cudaEventCreate(&e0));
   CAGEO_CUDA(cudaEventCreate(&e1));
   cageo_status st = CAGEO_OK;
   float best_ms = 0.0f;
-  int best = p->fw.max_rounds;
-  for (int c = 0; c < 5 && st == CAGEO_OK; c++) {
-    p->fw.max_rounds = kCand[c];
+  cageo_tuning best{p->fw.max_rounds, p->fw.flood_warps};
+  cageo_tuning cand[kTuneCandidates];
+  cageo_autotune_candidates(cand, kTuneCandidates);
+  for (int c = 0; c < kTuneCandidates && st == CAGEO_OK; c++) {
+    p->fw.max_rounds = cand[c].fill_rounds;
+    p->fw.flood_warps = cand[c].fill_warps;
     uint32_t r0 = first + (uint32_t)(c * (trials + 1));
     if (cudaMemcpyAsync(p->dscal, &r0, sizeof(r0), cudaMemcpyHostToDevice, s) != cudaSuccess) {
       st = cuda_fail(cudaGetLastError(), "cudaMemcpyAsync");
@@ -816,22 +857,19 @@ extern "C" cageo_status cageo_pipeline_autotune(cageo_pipeline* p, uint32_t firs
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, e0, e1);
     ms /= (float)trials;
-    if (h_ms) h_ms[c] = ms;
+    if (h_ms && c < n_ms) h_ms[c] = ms;
     if (c == 0 || ms < best_ms) {
       best_ms = ms;
-      best = kCand[c];
+      best = cand[c];
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (st) return st;
-  p->fw.max_rounds = best;
-  if (p->exec) cudaGraphExecDestroy(p->exec);
-  if (p->graph) cudaGraphDestroy(p->graph);
-  p->exec = nullptr;
-  p->graph = nullptr;
-  p->graph_ok = false;
-  if (h_best_rounds) *h_best_rounds = best;
+  p->fw.max_rounds = best.fill_rounds;
+  p->fw.flood_warps = best.fill_warps;
+  drop_graph(p);
+  if (h_best) *h_best = best;
   CAGEO_CUDA(cudaMemsetAsync(p->counts, 0, 4 * (size_t)p->N, s));
   CAGEO_CUDA(cudaMemsetAsync(p->dscal + 1, 0, 2 * sizeof(uint32_t), s));
   CAGEO_CUDA(cudaStreamSynchronize(s));

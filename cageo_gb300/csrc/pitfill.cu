@@ -32,6 +32,7 @@
 // Every wait and every loop is bounded; exceeding a bound sets an error
 // flag that the host turns into CAGEO_ERR_NO_CONVERGENCE.
 #include <algorithm>
+#include <type_traits>
 #include "common.cuh"
 #include "pitfill.cuh"
 #include "stage_math.cuh"
@@ -83,22 +84,49 @@ __device__ __forceinline__ unsigned long long global_ns() {
 
 constexpr int kTile = 32;
 constexpr int kRingSlack = 8192;  // work-ring room for tickets taken ahead of the pushes (> warps)
-constexpr int kWarps = 16;  // one 512-thread block per SM (16 x 14.0 KB smem, 128 registers)
 constexpr int kRS = 35;           // relay row stride (34 used)
 constexpr int kWS = 33;           // W/q row stride
 constexpr int kFS = 36;           // flag row stride (bytes)
 
-// Per-warp staged tile: relay values of the tile and its one-cell halo,
-// and (W, q) pairs and flags of the tile's own cells.
-struct WarpSmem {
+// Per-warp staged tile.  R: relay values of the tile and its one-cell halo.
+// In flood A (modes 0 and 2) every cell that can change relays its own W,
+// so W lives in R and only q is kept beside it (Q); flood B keeps (W, q)
+// pairs (WQ), since its walls relay +inf whatever their W.  F: flags of the
+// tile's own cells.  HC: clean relays of the halo (mode 2): [0] the row
+// above and [1] the row below the tile (halo x 0..33), [2] the column left
+// and [3] the column right of it (halo y 0..33); 1 = clean and passable.
+struct SmemA {
   float R[34 * kRS];
-  float2 WQ[kTile * kWS];  // (W, q) of the tile's own cells
+  float Q[kTile * kWS];
   uint8_t F[kTile * kFS];
-  // Clean relays of the halo (flood A with clean marks): [0] the row above
-  // and [1] the row below the tile (halo x 0..33), [2] the column left and
-  // [3] the column right of it (halo y 0..33); 1 = clean and passable.
   uint8_t HC[4][34];
 };
+struct SmemB {
+  float R[34 * kRS];
+  float2 WQ[kTile * kWS];
+  uint8_t F[kTile * kFS];
+};
+template <int MODE>
+using WarpSmem = typename std::conditional<MODE == 1, SmemB, SmemA>::type;
+
+// Warps per block (one block per SM) of the flood launches.  Flood B runs
+// 16 (14.0 KB of shared memory each); flood A runs 16, 20 or 22 (10.0 KB
+// each), chosen by FillWork::flood_warps (the autotuner picks it), with the
+// register budget the launch bounds give each.
+constexpr int kWarpsB = 16;
+
+__device__ __forceinline__ float staged_w(const SmemA& s, int x, int y) {
+  return s.R[(y + 1) * kRS + x + 1];
+}
+__device__ __forceinline__ float staged_w(const SmemB& s, int x, int y) {
+  return s.WQ[y * kWS + x].x;
+}
+__device__ __forceinline__ float staged_q(const SmemA& s, int x, int y) {
+  return s.Q[y * kWS + x];
+}
+__device__ __forceinline__ float staged_q(const SmemB& s, int x, int y) {
+  return s.WQ[y * kWS + x].y;
+}
 
 size_t fill_workspace_bytes(int W, int H) {
   size_t n = (size_t)W * H;
@@ -252,18 +280,18 @@ struct CellEval {
   uint8_t f;
 };
 
-__device__ __forceinline__ CellEval cell_load(const WarpSmem& s, int x, int y, float m) {
-  const float2 wq = s.WQ[y * kWS + x];
-  return CellEval{wq.x, wq.y, m, s.F[y * kFS + x]};
+template <class S>
+__device__ __forceinline__ CellEval cell_load(const S& s, int x, int y, float m) {
+  return CellEval{staged_w(s, x, y), staged_q(s, x, y), m, s.F[y * kFS + x]};
 }
 
 template <int MODE>
-__device__ __forceinline__ bool cell_store(WarpSmem& s, int x, int y, const CellEval& e) {
+__device__ __forceinline__ bool cell_store(WarpSmem<MODE>& s, int x, int y, const CellEval& e) {
   if (e.f & (FNODATA | FOUTLET | FBELOW)) return false;
   const float nw = fminf(e.w, fmaxf(e.q, e.m));
   const bool below = e.m < e.q;  // sets FBELOW, which the cell does not have yet
   if (nw == e.w && !below) return false;
-  s.WQ[y * kWS + x].x = nw;
+  if constexpr (MODE == 1) s.WQ[y * kWS + x].x = nw;  // in flood A, R below holds W
   // A fall of W withdraws the cell's clean mark (its clean path may not
   // reach the new level); the clean pass after the sweeps derives it again.
   if (MODE == 2 && nw != e.w) s.F[y * kFS + x] = (e.f | (below ? FBELOW : 0)) & (uint8_t)~FCLEAN;
@@ -277,14 +305,16 @@ __device__ __forceinline__ bool cell_store(WarpSmem& s, int x, int y, const Cell
 // Least relay of the three staged cells in relay row ry (tile row ry - 1),
 // tile columns x-1..x+1: the neighbours of (x, ry - 2) below it or of
 // (x, ry) above it.
-__device__ __forceinline__ float row3_min(const WarpSmem& s, int x, int ry) {
+template <class S>
+__device__ __forceinline__ float row3_min(const S& s, int x, int ry) {
   const float* r = &s.R[ry * kRS + x];
   return fminf(fminf(r[0], r[1]), r[2]);
 }
 
 // Least relay of the three staged cells in relay column rx (tile column
 // rx - 1), tile rows y-1..y+1.
-__device__ __forceinline__ float col3_min(const WarpSmem& s, int rx, int y) {
+template <class S>
+__device__ __forceinline__ float col3_min(const S& s, int rx, int y) {
   const float* r = &s.R[y * kRS + rx];
   return fminf(fminf(r[0], r[kRS]), r[2 * kRS]);
 }
@@ -318,7 +348,7 @@ __device__ __forceinline__ void flush_stats(const FillWork& w, VisitStats& st) {
 // per cell; the marks then spread by bit operations on the column masks
 // (neighbour columns by shuffles) until no lane changes, at most
 // `max_iter` times.  Returns this lane's column of newly clean cells.
-__device__ __forceinline__ unsigned int clean_pass(WarpSmem& s, int lane, int max_iter) {
+__device__ __forceinline__ unsigned int clean_pass(SmemA& s, int lane, int max_iter) {
   unsigned int qN = 0, qS = 0, qW = 0, qE = 0, qNW = 0, qNE = 0, qSW = 0, qSE = 0;
   unsigned int cl = 0, pas = 0;
   // Relay rows y, y+1, y+2 (tile rows y-1, y, y+1) at columns lane..lane+2.
@@ -383,7 +413,7 @@ __device__ __forceinline__ unsigned int clean_pass(WarpSmem& s, int lane, int ma
 // Returns whether every cell of the tile is final (NODATA, outlet or FBELOW;
 // with clean marks also clean).
 template <int MODE>
-__device__ bool process_tile(WarpSmem& s, const FloodArgs& a, int t, int lane, VisitStats& st) {
+__device__ bool process_tile(WarpSmem<MODE>& s, const FloodArgs& a, int t, int lane, VisitStats& st) {
   const FillWork& w = a.w;
   const int W = w.W, H = w.H;
   const int tx = t % w.tiles_x, ty = t / w.tiles_x;
@@ -403,11 +433,12 @@ __device__ bool process_tile(WarpSmem& s, const FloodArgs& a, int t, int lane, V
     }
     s.R[hy * kRS + hx] = relay<MODE>(wv, fv, qv);
     if (hx >= 1 && hx <= kTile && hy >= 1 && hy <= kTile) {
-      s.WQ[(hy - 1) * kWS + hx - 1] = make_float2(wv, qv);
+      if constexpr (MODE == 1) s.WQ[(hy - 1) * kWS + hx - 1] = make_float2(wv, qv);
+      else s.Q[(hy - 1) * kWS + hx - 1] = qv;
       s.F[(hy - 1) * kFS + hx - 1] = fv;
     }
   }
-  if (MODE == 2) {
+  if constexpr (MODE == 2) {
     // Clean relays of the halo: strips of 34 cells (row above, row below,
     // column left, column right), flags read again from L2.  A loop of its
     // own keeps the staging loop above as it is in the other modes.
@@ -503,7 +534,7 @@ __device__ bool process_tile(WarpSmem& s, const FloodArgs& a, int t, int lane, V
   const bool capped = (pd | pu | pr | pl) != 0;
   // Each round of the clean pass marks at least one more cell, so 1024
   // rounds always reach its fixpoint.
-  if (MODE == 2) dc |= clean_pass(s, lane, kTile * kTile);
+  if constexpr (MODE == 2) dc |= clean_pass(s, lane, kTile * kTile);
   const long long c2 = clock64();
   if (lane == 0) {
     w.tconv[t] = capped ? 0 : 1;
@@ -517,7 +548,7 @@ __device__ bool process_tile(WarpSmem& s, const FloodArgs& a, int t, int lane, V
     const int y = __ffs(rows) - 1;
     if ((dc >> y) & 1u) {
       const int64_t i = (int64_t)(y0 + y) * W + (x0 + lane);
-      a.Wg[i] = s.WQ[y * kWS + lane].x;
+      a.Wg[i] = staged_w(s, lane, y);
       w.flags[i] = s.F[y * kFS + lane];
     }
   }
@@ -603,7 +634,7 @@ __device__ __forceinline__ bool uf_unite(uint32_t* lab, uint32_t a, uint32_t b) 
 // come: a ticket still waiting then is abandoned (head and tail are reset
 // after the drain).  False on an error or a wait limit.
 template <int MODE>
-__device__ bool drain(WarpSmem& s, const FloodArgs& a, int lane, int ntiles) {
+__device__ bool drain(WarpSmem<MODE>& s, const FloodArgs& a, int lane, int ntiles) {
   const FillWork& w = a.w;
   volatile unsigned int* vs = w.scal;
   const unsigned int visit_cap = 1000u * (unsigned int)min(ntiles, 4000000);
@@ -644,15 +675,15 @@ __device__ bool drain(WarpSmem& s, const FloodArgs& a, int lane, int ntiles) {
   return ok;
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(kWarps * 32, 1)
+template <int MODE, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, 1)
 fill_flood_kernel(FloodArgs a) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  WarpSmem& s = reinterpret_cast<WarpSmem*>(smraw)[warp];
+  WarpSmem<MODE>& s = reinterpret_cast<WarpSmem<MODE>*>(smraw)[warp];
   const FillWork& w = a.w;
   const unsigned int nblocks = gridDim.x;
-  const int gwarp = blockIdx.x * kWarps + warp, nwarps = gridDim.x * kWarps;
+  const int gwarp = blockIdx.x * WARPS + warp, nwarps = gridDim.x * WARPS;
   const int ntiles = w.tiles_x * w.tiles_y;
   GridSync gs{w.scal + S_BAR_COUNT, w.scal + S_BAR_GEN, (int*)(w.scal + S_ERR)};
   volatile unsigned int* vs = w.scal;
@@ -1005,15 +1036,15 @@ __global__ void fill_scalars_kernel(unsigned int* s) {
     s[i] = (i == S_MIN || (i >= S_M && i < S_M + 3)) ? 0xffffffffu : 0u;
 }
 
-template <int MODE>
-static cageo_status launch_flood(const FloodArgs& a, cudaStream_t s) {
-  const size_t smem = sizeof(WarpSmem) * kWarps;
-  auto fn = fill_flood_kernel<MODE>;
+template <int MODE, int WARPS>
+static cageo_status launch_flood_warps(const FloodArgs& a, cudaStream_t s) {
+  const size_t smem = sizeof(WarpSmem<MODE>) * WARPS;
+  auto fn = fill_flood_kernel<MODE, WARPS>;
   CAGEO_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  static PerDevice resident;  // one table per MODE
+  static PerDevice resident;  // one table per instantiation
   int blocks = 0;
   cageo_status st = per_device(resident, &blocks, [&](int dev, int* v) -> cageo_status {
-    return resident_blocks((const void*)fn, kWarps * 32, smem, dev, v);
+    return resident_blocks((const void*)fn, WARPS * 32, smem, dev, v);
   });
   if (st) return st;
   FloodArgs args = a;
@@ -1021,10 +1052,24 @@ static cageo_status launch_flood(const FloodArgs& a, cudaStream_t s) {
   // No more blocks than the tiles can keep busy (small grids leave the
   // rest of the GPU idle instead of polling the work queue).
   const int ntiles = a.w.tiles_x * a.w.tiles_y;
-  const int grid = std::max(1, std::min(blocks, (ntiles + kWarps - 1) / kWarps));
-  CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(grid),
-                                         dim3(kWarps * 32), params, smem, s));
+  const int grid = std::max(1, std::min(blocks, (ntiles + WARPS - 1) / WARPS));
+  CAGEO_CUDA(cudaLaunchCooperativeKernel((const void*)fn, dim3(grid), dim3(WARPS * 32), params,
+                                         smem, s));
   return CAGEO_OK;
+}
+
+bool fill_flood_warps_valid(int warps) { return warps == 16 || warps == 20 || warps == 22; }
+
+template <int MODE>
+static cageo_status launch_flood(const FloodArgs& a, cudaStream_t s) {
+  if (MODE == 1) return launch_flood_warps<1, kWarpsB>(a, s);
+  switch (a.w.flood_warps) {
+    case 16: return launch_flood_warps<MODE == 1 ? 0 : MODE, 16>(a, s);
+    case 20: return launch_flood_warps<MODE == 1 ? 0 : MODE, 20>(a, s);
+    case 22: return launch_flood_warps<MODE == 1 ? 0 : MODE, 22>(a, s);
+  }
+  set_error("pit filling: %d warps per block is not one of 16, 20, 22", a.w.flood_warps);
+  return CAGEO_ERR_ARGUMENT;
 }
 
 cageo_status fill_reset_scalars(const FillWork& w, cudaStream_t s) {

@@ -22,7 +22,11 @@ struct FillWork {
   uint32_t* cmin = nullptr;      // W*H: per-component phase minima (at roots)
   unsigned int* scal = nullptr;  // scalar block (see pitfill.cu)
   int max_rounds = 64;           // sweep rounds per tile visit before the tile re-queues itself
+  int flood_warps = 20;          // warps per block (per SM) of flood A: 16, 20 or 22
 };
+
+// Whether `warps` is a block size flood A is built for.
+bool fill_flood_warps_valid(int warps);
 
 size_t fill_workspace_bytes(int W, int H);
 FillWork fill_carve(void* base, int W, int H);

@@ -366,15 +366,31 @@ cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t realization,
  * kilo-cycles summed over them spent staging, searching and storing
  * (last realization). */
 cageo_status cageo_pipeline_stats(cageo_pipeline* p, int64_t* h_stats, int n);
-/* Autotuner (no counterpart in the reference): times the fill with 4, 8,
- * 16, 32 and 64 sweep rounds per tile visit (a tile that has not converged
- * after that many rounds queues itself again), `trials`
- * realizations each from `first_realization` on, and keeps the fastest.
- * The results do not depend on the choice.  h_best_rounds (may be NULL)
- * receives the choice, h_ms (may be NULL) 5 milliseconds per realization.
- * Resets the counts to zero. */
+/* Tuning of the persistent fill kernels (no counterpart in the reference).
+ * The results never depend on it.  fill_rounds: sweep rounds a fill tile
+ * visit may run before the tile queues itself again (1..1024; default 64).
+ * fill_warps: warps per SM of the fill's lower-bound flood (16, 20 or 22;
+ * more warps hide more latency, fewer leave more registers to each; default
+ * 20).  The tile shape is fixed at 32 x 32 cells, the warp width: a warp
+ * owns a tile and holds its rows as 32-bit lane masks. */
+typedef struct {
+  int fill_rounds;
+  int fill_warps;
+} cageo_tuning;
+/* The autotuner's candidates: writes up to n of them to h_out (may be NULL)
+ * and returns how many there are. */
+int cageo_autotune_candidates(cageo_tuning* h_out, int n);
+cageo_status cageo_pipeline_set_tuning(cageo_pipeline* p, const cageo_tuning* t);
+cageo_status cageo_pipeline_get_tuning(cageo_pipeline* p, cageo_tuning* t);
+/* Autotuner: runs each candidate setting for one warm-up and `trials`
+ * realizations from `first_realization` on, timed with CUDA events on the
+ * pipeline's stream, and keeps the fastest.  h_best (may be NULL) receives
+ * the choice, h_ms (may be NULL) up to n_ms milliseconds per realization,
+ * one per candidate in cageo_autotune_candidates() order.  Resets the
+ * counts to zero. */
 cageo_status cageo_pipeline_autotune(cageo_pipeline* p, uint32_t first_realization,
-                                     int trials, int* h_best_rounds, float* h_ms);
+                                     int trials, cageo_tuning* h_best, float* h_ms,
+                                     int n_ms);
 /* Learned warm start for an exact-mode pipeline (no counterpart in the
  * reference): realizations then start the fill from the network's warm
  * surface (cells predicted shallower than `threshold` metres at their

@@ -191,14 +191,28 @@ def test_checkpoint_survives_an_interrupted_save(cuda, tmp_path):
 
 
 def test_autotune_keeps_counts(cuda):
-    """The autotuner only changes how many sweep rounds a tile visit may run
-    before re-queueing itself: counts equal an untuned pipeline's."""
+    """The autotuner only changes launch settings of the fill (sweep rounds
+    per tile visit, warps per SM of the lower-bound flood): counts, filled
+    surface and labels equal an untuned pipeline's under every setting."""
     from cageo_gb300 import api
     dem, streams = make_case(300, 200, seed=44)
     a = api.Pipeline(dem, streams, error_stddev=1.5, seed=9)
     best, ms = a.autotune(1000, trials=2)
-    assert best in (4, 8, 16, 32, 64) and all(v > 0 for v in ms.values())
+    cands = api.autotune_candidates()
+    assert best in cands and len(ms) == len(cands) and all(v > 0 for _, v in ms)
+    assert {c["fill_warps"] for c in cands} == {16, 20, 22}
+    assert a.tuning() == best
     a.run(0, 3)
     b = api.Pipeline(dem, streams, error_stddev=1.5, seed=9)
     b.run(0, 3)
     assert np.array_equal(a.counts(), b.counts())
+    fb = b.last_stages()
+    for rounds, warps in [(1, 16), (4, 22), (1024, 20)]:
+        c = api.Pipeline(dem, streams, error_stddev=1.5, seed=9)
+        c.set_tuning(rounds, warps)
+        c.run(0, 3)
+        assert np.array_equal(c.counts(), b.counts())
+        fc = c.last_stages()
+        assert np.array_equal(bits(fc[0]), bits(fb[0])) and np.array_equal(fc[2], fb[2])
+    with pytest.raises(api.CageoError):
+        c.set_tuning(32, 18)
