@@ -173,7 +173,9 @@ __device__ __forceinline__ float relay(float w, uint8_t f, float q) {
   if (f & FNODATA) return kInf;
   if (f & FOUTLET) return (f & FNONPASS) ? kInf : q;
   if (MODE != 1 || !(f & FNONPASS)) return w;
-  return ((f & FCONF) && !(f & FBELOW)) ? w : kInf;
+  // A clean cell kept flood A's level, which is finite; it is confirmed
+  // exactly when it is not below its q (what FCONF records for the others).
+  return ((f & (FCONF | FCLEAN)) && !(f & FBELOW)) ? w : kInf;
 }
 
 struct FloodArgs {
@@ -297,7 +299,7 @@ __device__ __forceinline__ bool cell_store(WarpSmem<MODE>& s, int x, int y, cons
   if (MODE == 2 && nw != e.w) s.F[y * kFS + x] = (e.f | (below ? FBELOW : 0)) & (uint8_t)~FCLEAN;
   else if (below) s.F[y * kFS + x] = e.f | FBELOW;
   // relay<MODE>() of a cell that is neither NODATA nor an outlet
-  const bool wall = MODE == 1 && (e.f & FNONPASS) && (below || !(e.f & FCONF));
+  const bool wall = MODE == 1 && (e.f & FNONPASS) && (below || !(e.f & (FCONF | FCLEAN)));
   s.R[(y + 1) * kRS + (x + 1)] = wall ? kInf : nw;
   return true;
 }
@@ -870,40 +872,46 @@ __global__ void fill_final_exact_kernel(float* __restrict__ Wg, int64_t n) {
   }
 }
 
-// Between the floods: keep flood A's result (lower bound) in aux and
-// FBELOWA, confirm non-passable cells reached at a level >= q, and start
-// flood B.  A clean cell keeps flood A's value and below-q flag, which flood
-// B would give it too (every value flood B relays is a passable level, so a
-// non-passable cell's incoming level never equals its q, and a clean cell's
-// level is reached by a path flood B keeps); every other cell restarts from
-// +inf and marks its tile for flood B (tseed).  Also resets the work queue.
+// Between the floods.  A clean cell keeps flood A's value and below-q flag,
+// which flood B would give it too (every value flood B relays is a passable
+// level, so a non-passable cell's incoming level never equals its q, and a
+// clean cell's level is reached by a path flood B keeps); nothing of it is
+// written.  Every other cell keeps flood A's result (a lower bound) in aux
+// and FBELOWA, is confirmed when non-passable and reached at a level >= q,
+// restarts from +inf and marks its tile for flood B (tseed).  Four
+// consecutive cells per thread; only the flags of clean cells are read.
+// Also resets the work queue.
 __global__ void fill_classify_kernel(float* __restrict__ Wg, uint8_t* __restrict__ F,
                                      uint32_t* __restrict__ aux, unsigned int* scal,
-                                     uint8_t* __restrict__ tseed, int tiles_x, int W) {
-  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+                                     uint8_t* __restrict__ tseed, int tiles_x, int W, int64_t n) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
     scal[S_HEAD] = 0u;
     scal[S_TAIL] = 0u;
     scal[S_PENDING] = 0u;
   }
-  const int y = blockIdx.y;
+  const int64_t b4 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+  if (b4 >= n) return;
+  uint8_t fv[4];
+  if (b4 + 4 <= n) {  // the flags are workspace: 256-byte aligned, b4 % 4 == 0
+    const uchar4 f4 = *reinterpret_cast<const uchar4*>(F + b4);
+    fv[0] = f4.x; fv[1] = f4.y; fv[2] = f4.z; fv[3] = f4.w;
+  } else {
 #pragma unroll
-  for (int k = 0; k < kCellsPerThread; k++) {
-    const int x = (blockIdx.x * kCellsPerThread + k) * blockDim.x + threadIdx.x;
-    if (x >= W) break;
-    const int64_t i = (int64_t)y * W + x;
-    uint8_t f = F[i];
+    for (int k = 0; k < 4; k++) fv[k] = b4 + k < n ? F[b4 + k] : FNODATA;
+  }
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    uint8_t f = fv[k];
+    if (f & (FNODATA | FOUTLET | FCLEAN)) continue;
+    const int64_t i = b4 + k;
     const float wa = Wg[i];
     aux[i] = __float_as_uint(wa);
-    if (f & (FNODATA | FOUTLET)) continue;
     if ((f & FNONPASS) && !(f & FBELOW) && wa < kInf) f |= FCONF;
     if (f & FBELOW) f |= FBELOWA;
-    if (f & FCLEAN) {
-      F[i] = f;
-    } else {
-      F[i] = f & (uint8_t)~FBELOW;
-      Wg[i] = kInf;
-      tseed[(y / kTile) * tiles_x + x / kTile] = 1;
-    }
+    F[i] = f & (uint8_t)~FBELOW;
+    Wg[i] = kInf;
+    const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
+    tseed[(y / kTile) * tiles_x + x / kTile] = 1;
   }
 }
 
@@ -957,7 +965,8 @@ __global__ void fill_undecided_kernel(const float* __restrict__ Wg, uint8_t* __r
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const uint8_t f = fv[k];
-    const bool unsure = !(f & (FNODATA | FOUTLET)) &&
+    // Clean cells agree by construction (their aux and FBELOWA are not kept).
+    const bool unsure = !(f & (FNODATA | FOUTLET | FCLEAN)) &&
                         (wav[k] != wbv[k] ||
                          ((f & FNONPASS) && (((f & FBELOWA) != 0) != ((f & FBELOW) != 0))));
     const int64_t i = b4 + k;
@@ -1001,12 +1010,22 @@ __global__ void fill_flatten_kernel(const uint32_t* __restrict__ cand,
   }
 }
 
+// Cells no outlet reached keep q.  Such a cell was never clean (a clean
+// cell's level is finite and flood B keeps it), so only the tiles flood B
+// worked on (tseed) are read: one block per tile, a row segment of 4 cells
+// per thread.
 __global__ void fill_final_kernel(const float* __restrict__ q, float* __restrict__ Wg,
-                                  int64_t n) {
+                                  const uint8_t* __restrict__ tseed, int tiles_x, int W, int H) {
+  const int t = blockIdx.x;
+  if (!tseed[t]) return;
+  const int y = (t / tiles_x) * kTile + (int)(threadIdx.x >> 3);
+  const int x0 = (t % tiles_x) * kTile + (int)(threadIdx.x & 7) * 4;
+  if (y >= H) return;
 #pragma unroll
-  for (int k = 0; k < kCellsPerThread; k++) {
-    const int64_t i = ((int64_t)blockIdx.x * kCellsPerThread + k) * blockDim.x + threadIdx.x;
-    if (i >= n) break;
+  for (int k = 0; k < 4; k++) {
+    const int x = x0 + k;
+    if (x >= W) break;
+    const int64_t i = (int64_t)y * W + x;
     if (Wg[i] == kInf) Wg[i] = q[i];
   }
 }
@@ -1097,8 +1116,9 @@ cageo_status fill_run(const float* q, float* filled, const FillWork& w, float no
   cageo_status st = launch_flood<2>(a, s);  // flood A with clean marks
   if (st) return st;
   CAGEO_CUDA(cudaMemsetAsync(w.tseed, 0, nt, s));
-  fill_classify_kernel<<<rows, 256, 0, s>>>(filled, w.flags, w.aux, w.scal, w.tseed, w.tiles_x,
-                                            w.W);
+  const unsigned cblocks = (unsigned)((n + 4 * 256 - 1) / (4 * 256));
+  fill_classify_kernel<<<cblocks, 256, 0, s>>>(filled, w.flags, w.aux, w.scal, w.tseed,
+                                               w.tiles_x, w.W, n);
   fill_tile_states_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(w.queued, w.tseed,
                                                                        (int)nt);
   CAGEO_CUDA(cudaGetLastError());
@@ -1115,7 +1135,7 @@ cageo_status fill_run(const float* q, float* filled, const FillWork& w, float no
   a.stage = 2;  // the confirmation phases
   st = launch_flood<1>(a, s);
   if (st) return st;
-  fill_final_kernel<<<blocks, 256, 0, s>>>(q, filled, n);
+  fill_final_kernel<<<(unsigned)nt, 256, 0, s>>>(q, filled, w.tseed, w.tiles_x, w.W, w.H);
   CAGEO_CUDA(cudaGetLastError());
   return CAGEO_OK;
 }
