@@ -36,6 +36,7 @@
 #include "common.cuh"
 #include "pitfill.cuh"
 #include "stage_math.cuh"
+#include "tilequeue.cuh"
 
 namespace cageo {
 
@@ -83,7 +84,6 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 constexpr int kTile = 32;
-constexpr int kRingSlack = 8192;  // work-ring room for tickets taken ahead of the pushes (> warps)
 constexpr int kRS = 35;           // relay row stride (34 used)
 constexpr int kWS = 33;           // W/q row stride
 constexpr int kFS = 36;           // flag row stride (bytes)
@@ -188,88 +188,20 @@ struct FloodArgs {
   int stage = 0;
 };
 
-// ---- asynchronous tile work queue ---------------------------------------
-// Tiles are processed as soon as they are queued, by whichever warp is free:
-// no grid-wide pass barriers.  The floods are monotone relaxations from
-// above, so the order of the updates does not change their limit; what
-// must not happen is two warps processing one tile at once (a slower
-// warp's write-back could undo a faster one's lower values).  Each tile
-// therefore has a state: idle, queued, processing, processing and queued
-// again meanwhile (re-queued when its processing ends), or done (every
-// cell final: never queued again in this flood).  `pending` counts tiles
-// that are queued or processing; the queue is drained when it reaches 0.
-// The ring (w.lists, 2 * ntiles slots, -1 = empty) holds each queued tile
-// once.
-enum : int { kIdle = 0, kQueued = 1, kBusy = 2, kBusyQueued = 3, kDone = 4 };
-constexpr int kEmptySlot = -1;
-
-__device__ __forceinline__ unsigned int ring_cap(const FillWork& w) {
-  return 2u * (unsigned int)(w.tiles_x * w.tiles_y) + kRingSlack;
+// ---- asynchronous tile work queue (tilequeue.cuh) --------------------------
+// The fill's queue: tile states in w.queued, the ring in w.lists
+// (2 * ntiles + kRingSlack slots), counters in the scalar block.
+__device__ __forceinline__ TileQueue fill_queue(const FillWork& w) {
+  return TileQueue{w.queued,
+                   w.lists,
+                   2u * (unsigned int)(w.tiles_x * w.tiles_y) + kRingSlack,
+                   w.scal + S_HEAD,
+                   w.scal + S_TAIL,
+                   w.scal + S_PENDING,
+                   (int*)(w.scal + S_ERR)};
 }
 
-__device__ __forceinline__ void ring_push(const FillWork& w, int t) {
-  const unsigned int cap = ring_cap(w);
-  const unsigned int pos = atomicAdd(&w.scal[S_TAIL], 1u);
-  // A plain store: the taker swaps the slot for "empty" and retries while
-  // it reads empty.
-  ((volatile int*)w.lists)[pos % cap] = t;
-}
-
-// Queue tile t unless it is queued already or done: idle -> queued,
-// processing -> processing and queued again.  A single compare-and-swap
-// when the state is the one expected.
-__device__ __forceinline__ void enqueue(const FillWork& w, int t) {
-  int expect = kIdle;
-  for (int it = 0; it < 256; it++) {
-    const int old = atomicCAS(&w.queued[t], expect, expect == kIdle ? kQueued : kBusyQueued);
-    if (old == expect) {
-      if (expect == kIdle) {
-        atomicAdd(&w.scal[S_PENDING], 1u);
-        ring_push(w, t);
-      }
-      return;
-    }
-    if (old != kIdle && old != kBusy) return;  // queued already, or done
-    expect = old;
-  }
-  atomicCAS((int*)(w.scal + S_ERR), 0, 3);
-}
-
-// Lane 0: take the next queued tile.  A warp takes a ticket (the next ring
-// position) when the ring looks non-empty and keeps it until the slot is
-// filled -- possibly by a later push -- so no claim ever fails.  Returns
-// the tile, or -1 while waiting; *ticket carries the ticket between calls
-// (-1: none).
-__device__ __forceinline__ int try_dequeue(const FillWork& w, long long* ticket) {
-  volatile unsigned int* vs = w.scal;
-  if (*ticket < 0) {
-    if (vs[S_HEAD] >= vs[S_TAIL]) return -1;
-    *ticket = atomicAdd(&w.scal[S_HEAD], 1u);
-  }
-  const int t = atomicExch(&w.lists[(unsigned int)*ticket % ring_cap(w)], kEmptySlot);
-  if (t == kEmptySlot) return -1;
-  *ticket = -1;
-  // Queued -> processing: only the taker changes a queued tile's state.
-  // The fence puts the change before the staging loads, so a neighbour
-  // that writes the halo later sees "processing" and queues the tile again.
-  ((volatile int*)w.queued)[t] = kBusy;
-  __threadfence();
-  return t;
-}
-
-// Lane 0, after the tile's write-back: idle again (done if every cell is
-// final), or queued again if a neighbour queued it while it was processed.
-__device__ __forceinline__ void finish_tile(const FillWork& w, int t, bool done) {
-  if (atomicCAS(&w.queued[t], kBusy, done ? kDone : kIdle) == kBusy) {
-    atomicSub(&w.scal[S_PENDING], 1u);
-  } else if (done) {  // processing and queued again: only the owner changes that state
-    ((volatile int*)w.queued)[t] = kDone;
-    atomicSub(&w.scal[S_PENDING], 1u);
-  } else {
-    ((volatile int*)w.queued)[t] = kQueued;
-    ring_push(w, t);
-  }
-}
+__device__ __forceinline__ void enqueue(const FillWork& w, int t) { tq_enqueue(fill_queue(w), t); }
 
 // Relaxation of staged cell (x, y) given m, the least relay among the
 // neighbours it reads, split into its loads (cell_load) and its update
@@ -646,12 +578,12 @@ __device__ bool drain(WarpSmem<MODE>& s, const FloodArgs& a, int lane, int ntile
   bool ok = true;
   for (long long idle = 0;;) {
     int t = -1;
-    if (lane == 0) t = try_dequeue(w, &ticket);
+    if (lane == 0) t = tq_try_dequeue(fill_queue(w), &ticket);
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= 0) {
       const bool done = process_tile<MODE>(s, a, t, lane, st);
       if (lane == 0) {
-        finish_tile(w, t, done);
+        tq_finish(fill_queue(w), t, done);
         if (st.tiles >= 64) flush_stats<MODE>(w, st);
       }
       __syncwarp();
