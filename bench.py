@@ -8,9 +8,11 @@ Workload ("eval-8192"): 8192^2 float32 DEM from seeded spectral fBm (Hurst
 cells, -9999 elsewhere; Gaussian filter, 60 m practical range, error sd
 1.5 m.  Synthetic data stands in for the reference's missing sample DEM.
 
-A step is one realization (noise -> convolution -> realistic DEM ->
-burning -> pit fill -> routing -> tracing -> border count) over the whole
-DEM.  Every grid is 256 MiB, larger than the 129 MB L2, so no flush is
+A step is one batched step: `batch` realizations (noise -> convolution ->
+realistic DEM -> burning -> pit fill -> routing -> tracing -> border count)
+over the whole DEM, their pit fills sharing one stacked grid; `batch` is
+chosen by timing among --batch-candidates, and the same realizations run
+one at a time are reported beside it (batch_steps.plain_value).  Every grid is 256 MiB, larger than the 129 MB L2, so no flush is
 needed between steps.  `value` times K steps with the grids resident on
 the device (CUDA events on the pipeline's stream); `e2e` times the same K
 steps through the C ABI from pinned host buffers: upload of DEM and
@@ -45,10 +47,14 @@ FALLBACK_HBM = 6800.0
 # Algorithmic bytes per cell of each stage (unfused compulsory I/O).
 STAGE_BYTES = {"noise": 4, "front": 40, "fill": 8, "route": 5, "trace": 6, "border": 12}
 PIPE_BYTES = 75
-# DRAM bytes per cell moved by one pit fill (its three flood launches), from an
-# ncu capture of the 4096^2 workload (1552 MB for 16.8 M cells), applied
-# per cell to the benchmark grid.
-FILL_TRAFFIC_PER_CELL = 1552.0e6 / (4096 * 4096)
+# The dominant kernel is the pit fill's lower-bound flood (fill_flood_kernel
+# with clean marks, 34% of a realization).  Its algorithmic bytes are those
+# of one fill pass: read q (4 B) and write the filled value (4 B) per cell.
+# Its DRAM bytes per launch come from an ncu capture of the 4096^2 workload
+# (dram__bytes_read.sum + dram__bytes_write.sum of that launch divided by
+# its 16.8 M cells), applied per cell to the benchmark grid.
+FLOOD_A_BYTES_PER_CELL = 8
+FLOOD_A_TRAFFIC_PER_CELL = 776.6e6 / (4096 * 4096)
 
 
 def peak_hbm():
@@ -288,9 +294,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-exact", action="store_true", help="skip the exact-mode measurement")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched measurement")
+    ap.add_argument("--batch-candidates", default="1,4,8",
+                    help="realizations per batched step to choose from (by timing)")
     ap.add_argument("--workload", default="eval-8192",
                     help="eval-8192 (the benchmark) or a smaller case for profiling (plain-4096)")
     args = ap.parse_args()
+    args.batch_candidates = [int(b) for b in args.batch_candidates.split(",") if b]
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local = int(os.environ.get("LOCAL_RANK", 0))
@@ -316,25 +325,47 @@ def main():
     from cageo_gb300.replicas import realization_range
     # disjoint realization numbers per rank (replicas; weak scaling)
     base, _ = realization_range(rank, world, world * 1_000_000)
-    # Autotuning (sweep rounds per fill tile visit), then warm-up: graph
-    # capture + stage profile.  Neither is timed.
-    tuned, tune_ms = pipe.autotune(base + 900_000, trials=3)
-    pipe.run(base, args.warmup)
-    stage_ms = pipe.profile(base + args.warmup)
-    stats = pipe.stats()
-    pipe.reset_counts()
     ext = torch.cuda.ExternalStream(pipe.stream)
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(first, count):
+        """Device milliseconds of `count` realizations on the pipeline's stream."""
+        torch.cuda.synchronize()
+        start.record(ext)
+        pipe.run(first, count)
+        stop.record(ext)
+        torch.cuda.synchronize()
+        return start.elapsed_time(stop)
+
+    # Autotuning of the fill's launch settings, then of the realizations per
+    # batched step (each candidate: one step to capture its graph, then 3
+    # timed steps), then warm-up (graph capture) and the stage profile.
+    # None of it is timed.
+    tuned, tune_ms = pipe.autotune(base + 900_000, trials=3)
+    batch_ms = {}
+    for b in args.batch_candidates:
+        pipe.set_batch(b)
+        pipe.run(base + 800_000, b)
+        batch_ms[b] = timed(base + 800_000 + 100 * b, 3 * b) / (3 * b)
+    batch = min(batch_ms, key=batch_ms.get)
+    pipe.set_batch(batch)
+    pipe.run(base, args.warmup * batch)
+    prof = pipe.profile(base + args.warmup * batch, fill_parts=True)
+    stage_ms = {k: prof[k] for k in pipe.STAGES}
+    fill_parts_ms = {k: prof[k] for k in pipe.FILL_PARTS}
+    stats = pipe.stats()
+    pipe.reset_counts()
 
     def barrier():
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
 
+    # A step is one batched step: `batch` realizations.
     barrier()
     with ClockSampler(local) as clocks:
         start.record(ext)
-        pipe.run(base + 10_000, args.steps)
+        pipe.run(base + 10_000, args.steps * batch)
         stop.record(ext)
         barrier()
     ms = start.elapsed_time(stop)
@@ -342,7 +373,14 @@ def main():
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    value = world * args.steps / (ms / 1000.0)
+    value = world * args.steps * batch / (ms / 1000.0)
+    gpu_launches = args.steps * pipe.graph_kernels()
+    # The same realizations one at a time (the plain pipeline), for the
+    # batching gain; not part of the headline.
+    pipe.set_batch(1)
+    pipe.run(base + 40_000, args.warmup)
+    plain_ms = timed(base + 50_000, args.steps * batch)
+    plain_value = world * args.steps * batch / (plain_ms / 1000.0)
 
     # End to end through the C ABI from pinned host memory.
     dem_h = torch.from_numpy(dem).pin_memory()
@@ -351,7 +389,9 @@ def main():
     barrier()
     t0 = time.perf_counter()
     pe = api.Pipeline(dem_h.numpy(), st_h.numpy(), **cfg)
-    pe.run(base + 20_000, args.steps)
+    pe.set_tuning(tuned["fill_rounds"], tuned["fill_warps"])
+    pe.set_batch(batch)
+    pe.run(base + 20_000, args.steps * batch)
     pe.counts(out=counts_h)
     if world > 1:
         c = counts_h.cuda()
@@ -364,7 +404,7 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     pe.close()
-    e2e_value = world * args.steps / e2e_s
+    e2e_value = world * args.steps * batch / e2e_s
 
     if rank != 0:
         pipe.close()
@@ -373,8 +413,9 @@ def main():
         return
 
     hbm, peak_kind = peak_hbm()
-    dom = max(stage_ms, key=stage_ms.get)
-    achieved = STAGE_BYTES[dom] * N / (stage_ms[dom] / 1000.0) / 1e9
+    flood_ms = fill_parts_ms["flood_a"]
+    achieved = FLOOD_A_BYTES_PER_CELL * N / (flood_ms / 1000.0) / 1e9
+    fill_achieved = STAGE_BYTES["fill"] * N / (stage_ms["fill"] / 1000.0) / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": "realizations/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -383,7 +424,7 @@ def main():
         "config": {"workload": args.workload, "width": W, "height": H, "filter": "Gaussian %g m" % p["range_m"],
                    "error_sd": p["sigma"], "pits": p["pits"], "stream_threshold": p["threshold"],
                    "hurst": p["hurst"], "relief_m": [p["lo"], p["hi"]],
-                   "realizations_per_step": 1, "l2": "inputs larger than L2 (256 MiB grids)",
+                   "realizations_per_step": batch, "l2": "inputs larger than L2 (256 MiB grids)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "cuda_graph": True,
                    "autotune": {"chosen": tuned,
@@ -397,19 +438,30 @@ def main():
         "gpu_launches": None,
         "stage_ms": stage_ms,
         "fill_stats": stats,
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
-                     "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": FILL_TRAFFIC_PER_CELL * N if dom == "fill" else None,
-                     "traffic_note": "DRAM bytes of one fill, ncu at 4096^2 scaled by cells"
-                     if dom == "fill" else None,
-                     "algorithmic_bytes_per_cell": STAGE_BYTES[dom], "peak_kind": peak_kind},
+        "fill_parts_ms": fill_parts_ms,
+        "roofline": {"bound": "hbm",
+                     "kernel": "fill_flood_kernel (pit fill, lower-bound flood with clean marks)",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": FLOOD_A_TRAFFIC_PER_CELL * N,
+                     "traffic_note": "DRAM bytes of one launch: ncu at 4096^2, scaled by cells",
+                     "launch_ms": flood_ms,
+                     "algorithmic_bytes_per_cell": FLOOD_A_BYTES_PER_CELL,
+                     "peak_kind": peak_kind},
+        "fill_stage_roofline": {"achieved": fill_achieved, "peak": hbm,
+                                "frac": fill_achieved / hbm, "ms": stage_ms["fill"],
+                                "algorithmic_bytes_per_cell": STAGE_BYTES["fill"]},
         "pipeline_roofline": {"achieved": value / world * N * PIPE_BYTES / 1e9, "peak": hbm,
                               "frac": value / world * N * PIPE_BYTES / 1e9 / hbm,
                               "bytes_per_cell": PIPE_BYTES},
         "clocks": clocks.summary(),
     }
-    # Kernel nodes of the captured realization graph, replayed once per step.
-    line["gpu_launches"] = args.steps * pipe.graph_kernels()
+    # Kernel nodes of the captured batched-step graph, replayed once per step.
+    line["gpu_launches"] = gpu_launches
+    line["batch_steps"] = {
+        "realizations_per_step": batch,
+        "ms_per_realization": {str(b): round(v, 4) for b, v in batch_ms.items()},
+        "value": value, "plain_value": plain_value, "batched_over_plain": value / plain_value,
+        "note": "plain: the same number of realizations one at a time (batch 1), same pipeline"}
     if not args.no_exact:
         line["exact_mode"] = exact_mode(dem, streams, cfg, args.steps, args.warmup, base)
     if not args.no_batched:

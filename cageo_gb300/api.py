@@ -100,6 +100,7 @@ _SIGS = {
                                       _vp], _i),
     "cageo_pipeline_run": ([_vp, ctypes.c_uint32, _i], _i),
     "cageo_pipeline_run_filter": ([_vp, ctypes.c_uint32, _i, _i, _f, _f, _f], _i),
+    "cageo_pipeline_set_batch": ([_vp, _i], _i),
     "cageo_pipeline_counts": ([_vp, _vp], _i),
     "cageo_pipeline_counts_device": ([_vp, _vp], _i),
     "cageo_pipeline_last_stages": ([_vp, _vp, _vp, _vp], _i),
@@ -247,7 +248,8 @@ def pitfill(dem, nodata_dem=-9999.0, workspace=None, mode=FILL_CPU_COMPAT):
 
 
 FILL_STATS = ("last_pass", "phases", "passes", "passes_b", "us", "us_b", "us_phases", "tiles",
-              "rounds", "tiles_b", "rounds_b", "kcyc_load", "kcyc_sweep", "kcyc_store")
+              "rounds", "tiles_b", "rounds_b", "kcyc_load", "kcyc_sweep", "kcyc_store",
+              "kcyc_idle", "kcyc_idle_b")
 
 
 def pitfill_exact_warm(dem, warm=None, nodata_dem=-9999.0, workspace=None):
@@ -260,7 +262,7 @@ def pitfill_exact_warm(dem, warm=None, nodata_dem=-9999.0, workspace=None):
     H, W = dem.shape
     filled = torch.empty_like(dem)
     ws, wsb = (None, 0) if workspace is None else (_ptr(workspace), workspace.numel())
-    st = (ctypes.c_int64 * 14)()
+    st = (ctypes.c_int64 * len(FILL_STATS))()
     _check(lib().cageo_pitfill_exact_warm(_ptr(dem), _ptr(warm) if warm is not None else None,
                                           _ptr(filled), W, H, nodata_dem, ws, wsb,
                                           ctypes.cast(st, _vp), _stream()))
@@ -390,6 +392,11 @@ class Pipeline:
     def run(self, first, count):
         _check(lib().cageo_pipeline_run(self._p, first, count))
 
+    def set_batch(self, batch):
+        """Realizations per batched step (1: one at a time); see
+        cageo_pipeline_set_batch."""
+        _check(lib().cageo_pipeline_set_batch(self._p, int(batch)))
+
     def run_filter(self, first, count, filter_model, practical_range, error_mean, error_stddev):
         """Run with this filter and error model (kept for later runs)."""
         _check(lib().cageo_pipeline_run_filter(self._p, first, count, filter_model,
@@ -430,14 +437,14 @@ class Pipeline:
         _check(lib().cageo_pipeline_reset_counts(self._p))
 
     def stats(self):
-        s = np.zeros(23, np.int64)
-        _check(lib().cageo_pipeline_stats(self._p, s.ctypes.data_as(_vp), 23))
+        s = np.zeros(25, np.int64)
+        _check(lib().cageo_pipeline_stats(self._p, s.ctypes.data_as(_vp), 25))
         keys = ("fill_passes", "fill_phases", "flat_layers", "trace_jumps", "burn_reruns",
                 "flood_a_passes", "flood_b_passes", "flood_a_us", "flood_b_us", "phases_us",
                 "flood_a_tiles", "flood_a_rounds", "flood_b_tiles", "flood_b_rounds",
                 "flat_cells", "flat_bfs_us", "tile_kcycles_load", "tile_kcycles_sweep",
                 "tile_kcycles_store", "flat_tiles", "flat_kcycles_load", "flat_kcycles_bfs",
-                "flat_kcycles_store")
+                "flat_kcycles_store", "flood_a_kcycles_idle", "flood_b_kcycles_idle")
         return {k: int(v) for k, v in zip(keys, s)}
 
     STAGES = ("noise", "front", "fill", "route", "trace", "border")
@@ -478,11 +485,17 @@ class Pipeline:
                 "repair_rounds", "warm_fill_us", "repair_fill_us")
         return {k: int(v) for k, v in zip(keys, s)}
 
-    def profile(self, realization):
-        """Run one realization with per-stage CUDA event timing; returns {stage: ms}."""
-        ms = np.zeros(6, np.float32)
-        _check(lib().cageo_pipeline_profile(self._p, realization, ms.ctypes.data_as(_vp), 6))
-        return dict(zip(self.STAGES, (float(v) for v in ms)))
+    FILL_PARTS = ("fill_setup", "flood_a", "flood_b", "phases", "fill_final")
+
+    def profile(self, realization, fill_parts=False):
+        """Run one realization with per-stage CUDA event timing; returns
+        {stage: ms} (with fill_parts, also the pit fill's parts)."""
+        ms = np.zeros(11, np.float32)
+        _check(lib().cageo_pipeline_profile(self._p, realization, ms.ctypes.data_as(_vp), 11))
+        out = dict(zip(self.STAGES, (float(v) for v in ms[:6])))
+        if fill_parts:
+            out.update(zip(self.FILL_PARTS, (float(v) for v in ms[6:])))
+        return out
 
     def graph_kernels(self):
         """Kernel launches in the captured per-realization CUDA graph."""

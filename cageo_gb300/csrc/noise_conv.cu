@@ -22,7 +22,7 @@ __global__ void noise_kernel(float* __restrict__ out, int64_t n, uint32_t k0,
   int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t base = g * 4;
   if (base >= n) return;
-  if (dreal) realization = *dreal;
+  if (dreal) realization += *dreal;  // an offset from the device counter
   U4 ctr = {(uint32_t)g, realization, kNoiseTag, (uint32_t)(g >> 32)};
   U4 r = philox4x32_10(ctr, k0, k1);
   float z[4];

@@ -73,17 +73,18 @@ __global__ void repair_start_kernel(const int* __restrict__ label,
   if (i < n) warm[i] = label[i] == kError ? kInf : filled[i];
 }
 
-// End of a realization: record a flagged realization, clear the flag and
-// advance the device realization counter.
+// End of a step of `count` realizations: record the realizations of a
+// flagged step (none of them was counted), clear the flag and advance the
+// device realization counter.
 __global__ void realization_end_kernel(uint32_t* real, int* anomaly, uint32_t* redo,
-                                       unsigned int* nredo) {
+                                       unsigned int* nredo, unsigned int count) {
   if (threadIdx.x == 0) {
     if (*anomaly) {
-      unsigned int k = atomicAdd(nredo, 1u);
-      if (k < 4096) redo[k] = *real;
+      const unsigned int k = atomicAdd(nredo, count);
+      for (unsigned int j = 0; j < count && k + j < 4096; j++) redo[k + j] = *real + j;
       *anomaly = 0;
     }
-    *real += 1u;
+    *real += count;
   }
 }
 
@@ -139,7 +140,7 @@ struct cageo_pipeline {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool graph_ok = false;
-  int64_t stats[23] = {};
+  int64_t stats[25] = {};
   // Learned warm start (exact mode only): parameters, warm surface, counter.
   float* ws_params = nullptr;
   float* warm = nullptr;
@@ -148,11 +149,37 @@ struct cageo_pipeline {
   int64_t ws_stats[8] = {};
   // Digest of the DEM and stream grids (grid_digest_kernel), for checkpoints.
   unsigned long long input_digest = 0;
+  // Batched steps (cageo_pipeline_set_batch): `batch` realizations share one
+  // fill over a stack of their q grids (qb, filledb: batch * N floats, fill
+  // workspace fwb for W x batch*H), each slab's minimum of q in slab_min.
+  int batch = 1;
+  float *qb = nullptr, *filledb = nullptr;
+  void* fill_ws_b = nullptr;
+  unsigned int* slab_min = nullptr;
+  FillWork fwb;
+  cudaGraph_t graph_b = nullptr;
+  cudaGraphExec_t exec_b = nullptr;
+  bool last_batched = false;  // the last realization ran in a batched step
 };
 
 namespace {
 
+void free_batch(cageo_pipeline* p) {
+  if (p->exec_b) cudaGraphExecDestroy(p->exec_b);
+  if (p->graph_b) cudaGraphDestroy(p->graph_b);
+  p->exec_b = nullptr;
+  p->graph_b = nullptr;
+  void* bufs[] = {p->qb, p->filledb, p->fill_ws_b, p->slab_min};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  p->qb = p->filledb = nullptr;
+  p->fill_ws_b = nullptr;
+  p->slab_min = nullptr;
+  p->batch = 1;
+}
+
 void free_all(cageo_pipeline* p) {
+  free_batch(p);
   if (p->exec) cudaGraphExecDestroy(p->exec);
   if (p->graph) cudaGraphDestroy(p->graph);
   void* bufs[] = {p->dem, p->streams, p->noise, p->q, p->filled, p->filter, p->tmp, p->code,
@@ -213,7 +240,43 @@ cageo_status enqueue_fast(cageo_pipeline* p) {
   if ((st = enqueue_route(p))) return st;
   if ((st = enqueue_trace_border(p, (const int*)p->dscal + 1))) return st;
   realization_end_kernel<<<1, 32, 0, s>>>(p->dscal, (int*)p->dscal + 1, p->dscal + 3,
-                                          p->dscal + 2);
+                                          p->dscal + 2, 1u);
+  CAGEO_CUDA(cudaGetLastError());
+  return CAGEO_OK;
+}
+
+// Launch sequence of one batched step: `p->batch` realizations from the
+// device counter on.  Noise and the fused front run per realization, each
+// into its slab of the stacked q grid (with its own minimum); one fill
+// covers the whole stack (slabs cannot exchange values: see FillWork); then
+// routing, tracing and the border counts run per slab.  The results equal
+// `batch` single realizations bit for bit.
+cageo_status enqueue_batch(cageo_pipeline* p) {
+  cudaStream_t s = p->stream;
+  const cageo_pipeline_config& c = p->cfg;
+  const int K = p->batch;
+  cageo_status st;
+  if ((st = fill_reset_scalars(p->fwb, s))) return st;
+  CAGEO_CUDA(cudaMemsetAsync(p->slab_min, 0xff, sizeof(unsigned int) * K, s));
+  for (int k = 0; k < K; k++) {
+    if ((st = launch_noise(p->noise, p->N, c.seed, (uint32_t)k, p->dscal, c.error_mean,
+                           c.error_stddev, s)))
+      return st;
+    FrontParams fp = p->fp;
+    fp.q = p->qb + (size_t)k * p->N;
+    fp.min_ord = p->slab_min + k;
+    if ((st = launch_front(p->noise, p->W, p->H, c.filter_model, p->filter, p->radius, fp, s)))
+      return st;
+  }
+  if ((st = fill_run(p->qb, p->filledb, p->fwb, c.nodata_dem, s))) return st;
+  for (int k = 0; k < K; k++) {
+    if ((st = route_run(p->filledb + (size_t)k * p->N, p->dir, p->flatdist, p->rw, s,
+                        CAGEO_ROUTE_CPU_COMPAT, c.nodata_dem)))
+      return st;
+    if ((st = enqueue_trace_border(p, (const int*)p->dscal + 1))) return st;
+  }
+  realization_end_kernel<<<1, 32, 0, s>>>(p->dscal, (int*)p->dscal + 1, p->dscal + 3,
+                                          p->dscal + 2, (unsigned int)K);
   CAGEO_CUDA(cudaGetLastError());
   return CAGEO_OK;
 }
@@ -230,7 +293,7 @@ cageo_status run_learned(cageo_pipeline* p) {
   const cageo_pipeline_config& c = p->cfg;
   const unsigned eb = (unsigned)((p->N + 255) / 256);
   cageo_status st;
-  int64_t fs[14];
+  int64_t fs[kFillStats];
   if ((st = fill_reset_scalars(p->fw, s))) return st;
   if ((st = launch_noise(p->noise, p->N, c.seed, 0, p->dscal, c.error_mean, c.error_stddev, s)))
     return st;
@@ -266,7 +329,7 @@ cageo_status run_learned(cageo_pipeline* p) {
   if ((st = border_u32_gated(p->label, p->counts, p->W, p->H, (const int*)p->dscal + 1, s)))
     return st;
   realization_end_kernel<<<1, 32, 0, s>>>(p->dscal, (int*)p->dscal + 1, p->dscal + 3,
-                                          p->dscal + 2);
+                                          p->dscal + 2, 1u);
   CAGEO_CUDA(cudaGetLastError());
   return CAGEO_OK;
 }
@@ -420,11 +483,44 @@ static cageo_status pipeline_run(cageo_pipeline* p, uint32_t first, int count) {
   const bool stage_only = p->cfg.nodata_dem == 0.0f;
   const bool learned = p->ws_params != nullptr && !stage_only;
   int done = 0;
-  if (!stage_only && !learned && count > 0 && p->cfg.use_graphs && !p->graph_ok && !p->exec) {
+  // Whole batched steps first (cageo_pipeline_set_batch), then single
+  // realizations for the rest.  Both advance the same device counter.
+  const int K = p->batch;
+  const bool batched = !stage_only && !learned && K > 1 && count >= K;
+  const int in_batches = batched ? count / K * K : 0;
+  if (batched) {
+    const int nb = count / K;
+    int b = 0;
+    if (p->cfg.use_graphs && !p->exec_b && !p->graph_b) {
+      // Warm-up outside capture, then capture one batched step.
+      if ((st = enqueue_batch(p))) return st;
+      b = 1;
+      CAGEO_CUDA(cudaStreamSynchronize(s));
+      cudaGraph_t g = nullptr;
+      if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        cageo_status cst = enqueue_batch(p);
+        cudaError_t e = cudaStreamEndCapture(s, &g);
+        if (cst != CAGEO_OK || e != cudaSuccess ||
+            cudaGraphInstantiate(&p->exec_b, g, 0) != cudaSuccess) {
+          p->exec_b = nullptr;
+        }
+        cudaGetLastError();
+      }
+      // Kept even when the capture failed: it marks the capture as tried
+      // (batched steps then run as direct launches).
+      p->graph_b = g;
+    }
+    for (; b < nb; b++) {
+      if (p->exec_b) CAGEO_CUDA(cudaGraphLaunch(p->exec_b, s));
+      else if ((st = enqueue_batch(p))) return st;
+    }
+    done = nb * K;
+  }
+  if (!stage_only && !learned && count > done && p->cfg.use_graphs && !p->graph_ok && !p->exec) {
     // Warm-up outside capture (kernel attributes, occupancy caches), then
     // capture one realization.
     if ((st = enqueue_fast(p))) return st;
-    done = 1;
+    done += 1;
     CAGEO_CUDA(cudaStreamSynchronize(s));
     if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
       cageo_status cst = enqueue_fast(p);
@@ -455,8 +551,10 @@ static cageo_status pipeline_run(cageo_pipeline* p, uint32_t first, int count) {
     }
   }
   CAGEO_CUDA(cudaStreamSynchronize(s));
-  int64_t fs[14] = {}, rs[7] = {}, jumps = 0;
-  if ((st = fill_check_status(p->fw, fs))) return st;
+  int64_t fs[kFillStats] = {}, rs[7] = {}, jumps = 0;
+  p->last_batched = batched && in_batches == count;
+  if (batched && (st = fill_check_status(p->fwb, p->last_batched ? fs : nullptr))) return st;
+  if ((st = fill_check_status(p->fw, p->last_batched ? nullptr : fs))) return st;
   if ((st = route_check_status(p->rw, rs))) return st;
   if ((st = trace_check_status(p->tw, &jumps))) return st;
   uint32_t nredo = 0;
@@ -484,6 +582,8 @@ static cageo_status pipeline_run(cageo_pipeline* p, uint32_t first, int count) {
   p->stats[15] = rs[2];
   for (int k = 0; k < 3; k++) p->stats[16 + k] = fs[11 + k];
   for (int k = 0; k < 4; k++) p->stats[19 + k] = rs[3 + k];
+  p->stats[23] = fs[14];
+  p->stats[24] = fs[15];
   return CAGEO_OK;
 }
 
@@ -502,8 +602,9 @@ extern "C" cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t reali
   CAGEO_CHECK_ARG(p->cfg.nodata_dem != 0.0f, "profiling needs the fused path (NODATA != 0)");
   cudaStream_t s = p->stream;
   const cageo_pipeline_config& c = p->cfg;
-  cudaEvent_t ev[7];
+  cudaEvent_t ev[7], fm[4];
   for (auto& e : ev) CAGEO_CUDA(cudaEventCreate(&e));
+  for (auto& e : fm) CAGEO_CUDA(cudaEventCreate(&e));
   cageo_status st = CAGEO_OK;
   do {
     if (cudaMemcpyAsync(p->dscal, &realization, 4, cudaMemcpyHostToDevice, s) != cudaSuccess) {
@@ -518,7 +619,10 @@ extern "C" cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t reali
     if ((st = launch_front(p->noise, p->W, p->H, c.filter_model, p->filter, p->radius, p->fp, s)))
       break;
     cudaEventRecord(ev[2], s);
-    if ((st = enqueue_fill(p))) break;
+    if (!exact_mode(p)) p->fw.marks = fm;
+    st = enqueue_fill(p);
+    p->fw.marks = nullptr;
+    if (st) break;
     cudaEventRecord(ev[3], s);
     if ((st = enqueue_route(p))) break;
     cudaEventRecord(ev[4], s);
@@ -528,14 +632,21 @@ extern "C" cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t reali
                                     (const int*)p->dscal + 1, trace_mode(p), s)))
       break;
     realization_end_kernel<<<1, 32, 0, s>>>(p->dscal, (int*)p->dscal + 1, p->dscal + 3,
-                                            p->dscal + 2);
+                                            p->dscal + 2, 1u);
     cudaEventRecord(ev[6], s);
     if (cudaStreamSynchronize(s) != cudaSuccess) {
       st = cuda_fail(cudaGetLastError(), "cudaStreamSynchronize");
       break;
     }
     for (int i = 0; i < 6 && i < n; i++) cudaEventElapsedTime(&h_ms[i], ev[i], ev[i + 1]);
-    int64_t fs[14], rs[7];
+    // The fill's parts (CPU-compatible mode): set-up, flood A, flood B with
+    // the undecided-cell kernels, confirmation phases, final pass.
+    const cudaEvent_t fill_marks[6] = {ev[2], fm[0], fm[1], fm[2], fm[3], ev[3]};
+    for (int i = 0; i < 5 && 6 + i < n; i++) {
+      if (exact_mode(p)) h_ms[6 + i] = 0.0f;
+      else cudaEventElapsedTime(&h_ms[6 + i], fill_marks[i], fill_marks[i + 1]);
+    }
+    int64_t fs[kFillStats], rs[7];
     if ((st = fill_check_status(p->fw, fs))) break;
     p->stats[0] = fs[0];
     p->stats[1] = fs[1];
@@ -546,9 +657,12 @@ extern "C" cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t reali
     p->stats[15] = rs[2];
     for (int k = 0; k < 3; k++) p->stats[16 + k] = fs[11 + k];
     for (int k = 0; k < 4; k++) p->stats[19 + k] = rs[3 + k];
+    p->stats[23] = fs[14];
+    p->stats[24] = fs[15];
     st = trace_check_status(p->tw, &p->stats[3]);
   } while (0);
   for (auto& e : ev) cudaEventDestroy(e);
+  for (auto& e : fm) cudaEventDestroy(e);
   return st;
 }
 
@@ -573,11 +687,15 @@ static cageo_status pipeline_run_filter(cageo_pipeline* p, uint32_t first, int c
   p->cfg.error_mean = error_mean;
   p->cfg.error_stddev = error_stddev;
   p->radius = r;
-  // The captured graph holds the old filter's launch shapes: drop it.
+  // The captured graphs hold the old filter's launch shapes: drop them.
   if (p->exec) cudaGraphExecDestroy(p->exec);
   if (p->graph) cudaGraphDestroy(p->graph);
+  if (p->exec_b) cudaGraphExecDestroy(p->exec_b);
+  if (p->graph_b) cudaGraphDestroy(p->graph_b);
   p->exec = nullptr;
   p->graph = nullptr;
+  p->exec_b = nullptr;
+  p->graph_b = nullptr;
   p->graph_ok = false;
   p->cfg.use_graphs = 0;
   return pipeline_run(p, first, count);
@@ -764,8 +882,10 @@ extern "C" cageo_status cageo_pipeline_last_stages(cageo_pipeline* p, float* h_f
                                                    int8_t* h_dir, int* h_label) {
   CAGEO_CHECK_ARG(p, "null pipeline");
   cudaStream_t s = p->stream;
+  // After a batched step the last realization's filled grid is its top slab.
+  const float* filled = p->last_batched ? p->filledb + (size_t)(p->batch - 1) * p->N : p->filled;
   if (h_filled)
-    CAGEO_CUDA(cudaMemcpyAsync(h_filled, p->filled, 4 * p->N, cudaMemcpyDeviceToHost, s));
+    CAGEO_CUDA(cudaMemcpyAsync(h_filled, filled, 4 * p->N, cudaMemcpyDeviceToHost, s));
   if (h_dir) CAGEO_CUDA(cudaMemcpyAsync(h_dir, p->dir, 2 * p->N, cudaMemcpyDeviceToHost, s));
   if (h_label) CAGEO_CUDA(cudaMemcpyAsync(h_label, p->label, 4 * p->N, cudaMemcpyDeviceToHost, s));
   CAGEO_CUDA(cudaStreamSynchronize(s));
@@ -796,9 +916,19 @@ extern "C" int cageo_autotune_candidates(cageo_tuning* h_out, int n) {
 static void drop_graph(cageo_pipeline* p) {
   if (p->exec) cudaGraphExecDestroy(p->exec);
   if (p->graph) cudaGraphDestroy(p->graph);
+  if (p->exec_b) cudaGraphExecDestroy(p->exec_b);
+  if (p->graph_b) cudaGraphDestroy(p->graph_b);
   p->exec = nullptr;
   p->graph = nullptr;
+  p->exec_b = nullptr;
+  p->graph_b = nullptr;
   p->graph_ok = false;
+}
+
+// The batched fill runs with the single fill's tuning.
+static void sync_batch_tuning(cageo_pipeline* p) {
+  p->fwb.max_rounds = p->fw.max_rounds;
+  p->fwb.flood_warps = p->fw.flood_warps;
 }
 
 extern "C" cageo_status cageo_pipeline_set_tuning(cageo_pipeline* p, const cageo_tuning* t) {
@@ -808,6 +938,7 @@ extern "C" cageo_status cageo_pipeline_set_tuning(cageo_pipeline* p, const cageo
   CAGEO_CUDA(cudaStreamSynchronize(p->stream));
   p->fw.max_rounds = t->fill_rounds;
   p->fw.flood_warps = t->fill_warps;
+  sync_batch_tuning(p);
   drop_graph(p);  // captured with the old launch shapes
   return CAGEO_OK;
 }
@@ -868,11 +999,40 @@ extern "C" cageo_status cageo_pipeline_autotune(cageo_pipeline* p, uint32_t firs
   if (st) return st;
   p->fw.max_rounds = best.fill_rounds;
   p->fw.flood_warps = best.fill_warps;
+  sync_batch_tuning(p);
   drop_graph(p);
   if (h_best) *h_best = best;
   CAGEO_CUDA(cudaMemsetAsync(p->counts, 0, 4 * (size_t)p->N, s));
   CAGEO_CUDA(cudaMemsetAsync(p->dscal + 1, 0, 2 * sizeof(uint32_t), s));
   CAGEO_CUDA(cudaStreamSynchronize(s));
+  return CAGEO_OK;
+}
+
+extern "C" cageo_status cageo_pipeline_set_batch(cageo_pipeline* p, int batch) {
+  CAGEO_CHECK_ARG(p, "null pipeline");
+  CAGEO_CHECK_ARG(batch >= 1 && batch <= 64, "batch must be 1..64 realizations");
+  if (batch > 1) {
+    CAGEO_CHECK_ARG(p->cfg.fill_mode == CAGEO_FILL_CPU_COMPAT,
+                    "batched steps need the CPU-compatible fill mode");
+    CAGEO_CHECK_ARG((int64_t)batch * p->N < kMaxCells, "batch * grid cells must stay below 2^31");
+  }
+  CAGEO_CUDA(cudaStreamSynchronize(p->stream));
+  free_batch(p);
+  p->last_batched = false;
+  if (batch == 1) return CAGEO_OK;
+  const size_t nb = (size_t)batch * p->N;
+  cageo_status st;
+  if ((st = dalloc(&p->qb, sizeof(float) * nb)) || (st = dalloc(&p->filledb, sizeof(float) * nb)) ||
+      (st = dalloc(&p->fill_ws_b, fill_workspace_bytes(p->W, batch * p->H))) ||
+      (st = dalloc(&p->slab_min, sizeof(unsigned int) * 64))) {
+    free_batch(p);
+    return st;
+  }
+  p->fwb = fill_carve(p->fill_ws_b, p->W, batch * p->H);
+  p->fwb.slab_h = p->H;
+  p->fwb.slab_min = p->slab_min;
+  sync_batch_tuning(p);
+  p->batch = batch;
   return CAGEO_OK;
 }
 
@@ -906,11 +1066,13 @@ extern "C" cageo_status cageo_pipeline_warmstart_stats(cageo_pipeline* p, int64_
 
 extern "C" cageo_status cageo_pipeline_graph_kernels(cageo_pipeline* p, int64_t* h_count) {
   CAGEO_CHECK_ARG(p && h_count, "null argument");
-  CAGEO_CHECK_ARG(p->graph_ok && p->graph, "no realization has been captured in a CUDA graph");
+  // The batched step's graph when batching is on and it was captured.
+  cudaGraph_t g = (p->batch > 1 && p->exec_b) ? p->graph_b : (p->graph_ok ? p->graph : nullptr);
+  CAGEO_CHECK_ARG(g, "no step has been captured in a CUDA graph");
   size_t n = 0;
-  CAGEO_CUDA(cudaGraphGetNodes(p->graph, nullptr, &n));
+  CAGEO_CUDA(cudaGraphGetNodes(g, nullptr, &n));
   std::vector<cudaGraphNode_t> nodes(n);
-  CAGEO_CUDA(cudaGraphGetNodes(p->graph, nodes.data(), &n));
+  CAGEO_CUDA(cudaGraphGetNodes(g, nodes.data(), &n));
   int64_t kernels = 0;
   for (size_t i = 0; i < n; i++) {
     cudaGraphNodeType t;
@@ -925,7 +1087,7 @@ extern "C" cudaStream_t cageo_pipeline_stream(cageo_pipeline* p) { return p ? p-
 
 extern "C" cageo_status cageo_pipeline_stats(cageo_pipeline* p, int64_t* h_stats, int n) {
   CAGEO_CHECK_ARG(p && h_stats, "null argument");
-  for (int i = 0; i < n && i < 23; i++) h_stats[i] = p->stats[i];
+  for (int i = 0; i < n && i < 25; i++) h_stats[i] = p->stats[i];
   return CAGEO_OK;
 }
 

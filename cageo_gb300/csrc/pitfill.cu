@@ -69,6 +69,8 @@ enum : int {
   S_KCYC_LOAD = 100,   // kilo-cycles (summed over tile visits) staging tiles
   S_KCYC_SWEEP = 101,  // kilo-cycles sweeping
   S_KCYC_STORE = 102,  // kilo-cycles writing back and queueing
+  S_KCYC_IDLE_A = 103, // kilo-cycles warps of flood A waited for a tile (tail included)
+  S_KCYC_IDLE_B = 104, // the same for flood B's drains
   S_HEAD = 128,      // work-queue tickets handed out (own 128-byte line)
   S_TAIL = 160,      // work-queue entries pushed (own line)
   S_PENDING = 192,   // tiles queued or being processed (own line)
@@ -257,17 +259,18 @@ __device__ __forceinline__ float col3_min(const S& s, int rx, int y) {
 // visits and when a drain ends: one atomic per counter and flush instead of
 // five atomics on one cache line per visit.
 struct VisitStats {
-  unsigned int tiles = 0, rounds = 0, kload = 0, ksweep = 0, kstore = 0;
+  unsigned int tiles = 0, rounds = 0, kload = 0, ksweep = 0, kstore = 0, kidle = 0;
 };
 
 template <int MODE>
 __device__ __forceinline__ void flush_stats(const FillWork& w, VisitStats& st) {
-  if (!st.tiles) return;
+  if (!st.tiles && !st.kidle) return;
   atomicAdd(&w.scal[MODE != 1 ? S_TILES_A : S_TILES_B], st.tiles);
   atomicAdd(&w.scal[MODE != 1 ? S_ROUNDS_A : S_ROUNDS_B], st.rounds);
   atomicAdd(&w.scal[S_KCYC_LOAD], st.kload);
   atomicAdd(&w.scal[S_KCYC_SWEEP], st.ksweep);
   atomicAdd(&w.scal[S_KCYC_STORE], st.kstore);
+  if (st.kidle) atomicAdd(&w.scal[MODE != 1 ? S_KCYC_IDLE_A : S_KCYC_IDLE_B], st.kidle);
   st = VisitStats{};
 }
 
@@ -576,11 +579,14 @@ __device__ bool drain(WarpSmem<MODE>& s, const FloodArgs& a, int lane, int ntile
   unsigned int ns = 32;
   VisitStats st;
   bool ok = true;
+  long long idle_from = -1;  // clock when this warp last found no tile (-1: busy)
   for (long long idle = 0;;) {
     int t = -1;
     if (lane == 0) t = tq_try_dequeue(fill_queue(w), &ticket);
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= 0) {
+      if (lane == 0 && idle_from >= 0) st.kidle += (unsigned int)((clock64() - idle_from) >> 10);
+      idle_from = -1;
       const bool done = process_tile<MODE>(s, a, t, lane, st);
       if (lane == 0) {
         tq_finish(fill_queue(w), t, done);
@@ -601,10 +607,14 @@ __device__ bool drain(WarpSmem<MODE>& s, const FloodArgs& a, int lane, int ntile
       ok = false;
       break;
     }
+    if (idle_from < 0) idle_from = clock64();
     __nanosleep(ns);
     if (ns < 1024) ns <<= 1;
   }
-  if (lane == 0) flush_stats<MODE>(w, st);
+  if (lane == 0) {
+    if (idle_from >= 0) st.kidle += (unsigned int)((clock64() - idle_from) >> 10);
+    flush_stats<MODE>(w, st);
+  }
   __syncwarp();
   return ok;
 }
@@ -746,11 +756,14 @@ constexpr int kCellsPerThread = 4;
 __global__ void fill_init_kernel(const float* __restrict__ q, float* __restrict__ Wg,
                                  uint8_t* __restrict__ F, const unsigned int* minslot,
                                  uint8_t* __restrict__ tseed, int tiles_x, int W, int H,
-                                 float nodata) {
-  // One block row per grid row (no division to find a cell's x and y);
-  // kCellsPerThread cells a block-width apart per thread (coalesced).
-  const int y = blockIdx.y;
-  const float minE = ordered_to_float(*minslot);
+                                 int slab_h, float nodata) {
+  // Block rows step over the grid's rows (no division to find a cell's x
+  // and y); kCellsPerThread cells a block-width apart per thread
+  // (coalesced).  A stack of realizations takes each slab's borders and
+  // minimum.
+  for (int y = blockIdx.y; y < H; y += gridDim.y) {
+  const int slab = y / slab_h, ys = y - slab * slab_h;
+  const float minE = ordered_to_float(minslot[slab]);
 #pragma unroll
   for (int k = 0; k < kCellsPerThread; k++) {
     const int x = (blockIdx.x * kCellsPerThread + k) * blockDim.x + threadIdx.x;
@@ -763,11 +776,12 @@ __global__ void fill_init_kernel(const float* __restrict__ q, float* __restrict_
     } else {
       if (!passable_quantized(qv, minE)) f |= FNONPASS;
       // Outlets keep q in both floods: clean from the start.
-      if (x == 0 || y == 0 || x == W - 1 || y == H - 1 || qv == 0.0f) f |= FOUTLET | FCLEAN;
+      if (x == 0 || ys == 0 || x == W - 1 || ys == slab_h - 1 || qv == 0.0f) f |= FOUTLET | FCLEAN;
     }
     F[i] = f;
     Wg[i] = (f & (FNODATA | FOUTLET)) ? qv : kInf;
     if ((f & FOUTLET) && !(f & FNONPASS)) tseed[(y / kTile) * tiles_x + x / kTile] = 1;
+  }
   }
 }
 
@@ -1038,15 +1052,19 @@ cageo_status fill_run(const float* q, float* filled, const FillWork& w, float no
   CAGEO_CUDA(cudaMemsetAsync(w.tseed, 0, nt, s));
   const dim3 rows((unsigned)((w.W + 256 * kCellsPerThread - 1) / (256 * kCellsPerThread)),
                    (unsigned)w.H);
-  fill_init_kernel<<<rows, 256, 0, s>>>(q, filled, w.flags, w.scal + S_MIN, w.tseed, w.tiles_x,
-                                        w.W, w.H, nodata);
+  const dim3 init_rows(rows.x, std::min(rows.y, 65535u));
+  fill_init_kernel<<<init_rows, 256, 0, s>>>(q, filled, w.flags,
+                                             w.slab_min ? w.slab_min : w.scal + S_MIN, w.tseed,
+                                             w.tiles_x, w.W, w.H, w.slab_h ? w.slab_h : w.H, nodata);
   CAGEO_CUDA(cudaGetLastError());
   FloodArgs a{q, filled, w};
   CAGEO_CUDA(cudaMemsetAsync(w.queued, 0, sizeof(int) * nt, s));  // all idle
   CAGEO_CUDA(cudaMemsetAsync(w.tconv, 0, nt, s));
   CAGEO_CUDA(cudaMemsetAsync(w.lists, 0xff, (2 * nt + kRingSlack) * sizeof(int), s));  // empty ring
+  if (w.marks) CAGEO_CUDA(cudaEventRecord(w.marks[0], s));
   cageo_status st = launch_flood<2>(a, s);  // flood A with clean marks
   if (st) return st;
+  if (w.marks) CAGEO_CUDA(cudaEventRecord(w.marks[1], s));
   CAGEO_CUDA(cudaMemsetAsync(w.tseed, 0, nt, s));
   const unsigned cblocks = (unsigned)((n + 4 * 256 - 1) / (4 * 256));
   fill_classify_kernel<<<cblocks, 256, 0, s>>>(filled, w.flags, w.aux, w.scal, w.tseed,
@@ -1064,9 +1082,11 @@ cageo_status fill_run(const float* q, float* filled, const FillWork& w, float no
   fill_unite_kernel<<<ublocks, 256, 0, s>>>(w.cand, w.scal, w.flags, w.aux, w.W);
   fill_flatten_kernel<<<ublocks, 256, 0, s>>>(w.cand, w.scal, w.aux);
   CAGEO_CUDA(cudaGetLastError());
+  if (w.marks) CAGEO_CUDA(cudaEventRecord(w.marks[2], s));
   a.stage = 2;  // the confirmation phases
   st = launch_flood<1>(a, s);
   if (st) return st;
+  if (w.marks) CAGEO_CUDA(cudaEventRecord(w.marks[3], s));
   fill_final_kernel<<<(unsigned)nt, 256, 0, s>>>(q, filled, w.tseed, w.tiles_x, w.W, w.H);
   CAGEO_CUDA(cudaGetLastError());
   return CAGEO_OK;
@@ -1121,6 +1141,8 @@ cageo_status fill_check_status(const FillWork& w, int64_t* stats) {
     stats[11] = h[S_KCYC_LOAD];
     stats[12] = h[S_KCYC_SWEEP];
     stats[13] = h[S_KCYC_STORE];
+    stats[14] = h[S_KCYC_IDLE_A];
+    stats[15] = h[S_KCYC_IDLE_B];
   }
   if (h[S_ERR]) {
     set_error(h[S_ERR] == 1   ? "pit filling: a grid-wide wait hit its limit"

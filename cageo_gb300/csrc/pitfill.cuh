@@ -23,6 +23,19 @@ struct FillWork {
   unsigned int* scal = nullptr;  // scalar block (see pitfill.cu)
   int max_rounds = 64;           // sweep rounds per tile visit before the tile re-queues itself
   int flood_warps = 20;          // warps per block (per SM) of flood A: 16, 20 or 22
+  // Stacked realizations (CPU-compatible fill only): the grid holds
+  // H / slab_h realizations of slab_h rows each, one above the other.
+  // Every slab's first and last rows are its border (outlets), so no flood
+  // value crosses from one slab to another: a cell that is not on a border
+  // has all 8 neighbours in its own slab, and border cells never change.
+  // slab_min holds each slab's ordered minimum of q (the passability test's
+  // minE).  slab_h = 0: one realization, minimum in the scalar block.
+  int slab_h = 0;
+  const unsigned int* slab_min = nullptr;
+  // Profiling only: when set, fill_run records marks[0] after the set-up,
+  // [1] after flood A, [2] after flood B's main drain and the undecided-cell
+  // kernels, [3] after the confirmation phases.
+  const cudaEvent_t* marks = nullptr;
 };
 
 // Whether `warps` is a block size flood A is built for.
@@ -51,11 +64,13 @@ cageo_status fill_quantize_min(float* d, const FillWork& w, float nodata,
 cageo_status fill_reset_scalars(const FillWork& w, cudaStream_t s);
 unsigned int* fill_min_slot(const FillWork& w);
 // Copies the device status (0 ok) and stats into host memory; the stream
-// must have been synchronized.  stats (14 entries): last pass number,
-// phases, passes of flood A, passes of flood B before the first phase,
-// microseconds of flood A, of flood B to convergence, of the phase loop,
-// tiles and sweep rounds of flood A, tiles and rounds of flood B, and
-// kilo-cycles summed over tile visits spent staging, sweeping, storing.
+// must have been synchronized.  stats (kFillStats entries): last pass
+// number, phases, passes of flood A, passes of flood B before the first
+// phase, microseconds of flood A, of flood B to convergence, of the phase
+// loop, tiles and sweep rounds of flood A, tiles and rounds of flood B,
+// kilo-cycles summed over tile visits spent staging, sweeping, storing, and
+// kilo-cycles warps of flood A and of flood B spent waiting for a tile.
+constexpr int kFillStats = 16;
 cageo_status fill_check_status(const FillWork& w, int64_t* stats);
 
 }  // namespace cageo

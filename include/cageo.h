@@ -167,7 +167,7 @@ cageo_status cageo_pitfill(float* d_dem, float* d_filled, int W, int H,
  * is >= the exact fill's value (a start of +inf always is); a start below
  * it leaves a lower fixpoint in which some cells do not drain, so callers
  * must verify the result (every cell drains to an outlet) and rerun cold
- * where it fails.  h_stats (may be NULL) receives the fill's 14
+ * where it fails.  h_stats (may be NULL) receives the fill's 16
  * statistics (passes, tiles, sweep rounds ...). */
 cageo_status cageo_pitfill_exact_warm(const float* d_dem, const float* d_warm,
                                       float* d_filled, int W, int H,
@@ -320,6 +320,21 @@ cageo_status cageo_pipeline_run(cageo_pipeline* p, uint32_t first_realization,
 cageo_status cageo_pipeline_run_filter(cageo_pipeline* p, uint32_t first_realization,
                                        int count, int model, float practical_range,
                                        float error_mean, float error_stddev);
+/* Batched steps (no counterpart in the reference, whose Monte Carlo loop
+ * runs one realization after another, src/main.cpp:180-283): with batch > 1
+ * cageo_pipeline_run processes realizations `batch` at a time.  Their noise
+ * and fused front run one after another into the slabs of a stacked grid,
+ * one pit fill covers the whole stack (the slabs' borders are outlets, so no
+ * value crosses between them), and routing, tracing and the border counts
+ * run per realization; a batched step is captured in a CUDA graph of its own.
+ * The counts and every stage output equal single realizations bit for bit;
+ * batching only shares the fill's persistent launches (their grid barriers
+ * and the idle tail of each flood) among the realizations of a step.  A run
+ * of `count` realizations takes count / batch batched steps and the rest
+ * singly.  1 <= batch <= 64, batch * cells < 2^31, CPU-compatible fill
+ * mode only.  Allocates 2 stacked grids and a fill workspace for them
+ * (about 21 bytes per cell per realization); batch = 1 frees them. */
+cageo_status cageo_pipeline_set_batch(cageo_pipeline* p, int batch);
 /* Border counts so far as float (the reference's CatchmentBorderType). */
 cageo_status cageo_pipeline_counts(cageo_pipeline* p, float* h_out);
 cageo_status cageo_pipeline_counts_device(cageo_pipeline* p, float* d_out);
@@ -345,14 +360,19 @@ cageo_status cageo_pipeline_save(cageo_pipeline* p, const char* path,
 cageo_status cageo_pipeline_load(cageo_pipeline* p, const char* path,
                                  uint32_t* next_realization);
 cudaStream_t cageo_pipeline_stream(cageo_pipeline* p);
-/* Kernel launches in the CUDA graph that one realization replays (the
- * graph's kernel nodes; memset nodes are not counted).  CAGEO_ERR_ARGUMENT
- * until a run has captured the graph.  No counterpart in the reference. */
+/* Kernel launches in the CUDA graph that one step replays (the graph's
+ * kernel nodes; memset nodes are not counted): the batched step's graph when
+ * batching is on and captured, else the single realization's.
+ * CAGEO_ERR_ARGUMENT until a run has captured one.  No counterpart in the
+ * reference. */
 cageo_status cageo_pipeline_graph_kernels(cageo_pipeline* p, int64_t* h_count);
 /* One realization with CUDA events between stages (fused path, no graph);
  * it is accumulated like any other.  h_ms[0..5]: noise, front
  * (convolution + realistic DEM + burning + quantization), pit fill,
- * routing, tracing, border (milliseconds). */
+ * routing, tracing, border (milliseconds); with n >= 11, h_ms[6..10]: the
+ * pit fill's parts -- set-up, lower-bound flood, walled flood with the
+ * undecided-cell kernels, confirmation phases, final pass (0 in exact
+ * mode). */
 cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t realization,
                                     float* h_ms, int n);
 /* Counters of the last run: [0] fill work-queue drains, [1] confirmation
@@ -363,8 +383,10 @@ cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t realization,
  * the two floods, [14] flat cells, [15] microseconds of the flat BFS,
  * [16..18] kilo-cycles summed over the fill's tile visits spent staging,
  * sweeping and storing, [19] tile visits of the flat BFS, [20..22]
- * kilo-cycles summed over them spent staging, searching and storing
- * (last realization). */
+ * kilo-cycles summed over them spent staging, searching and storing,
+ * [23..24] kilo-cycles the warps of the fill's lower-bound flood and of its
+ * walled flood spent waiting for a tile, end of the queue included (last
+ * realization). */
 cageo_status cageo_pipeline_stats(cageo_pipeline* p, int64_t* h_stats, int n);
 /* Tuning of the persistent fill kernels (no counterpart in the reference).
  * The results never depend on it.  fill_rounds: sweep rounds a fill tile

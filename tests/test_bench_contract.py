@@ -39,7 +39,10 @@ def test_gpu_arm_line():
                "--no-batched", "--cpu-steps", "1")
     assert BASE_KEYS <= set(d) and "impl" not in d
     assert d["value"] > 0 and d["steps"] == 3 and d["warmup"] == 3 and d["n_gpus"] == 1
-    assert abs(d["ms_per_step"] - 1000.0 / d["value"]) < 1e-6 * d["ms_per_step"] + 1e-9
+    per_step = d["config"]["realizations_per_step"]
+    assert per_step == d["batch_steps"]["realizations_per_step"] >= 1
+    assert abs(d["ms_per_step"] - 1000.0 * per_step / d["value"]) < 1e-6 * d["ms_per_step"] + 1e-9
+    assert d["batch_steps"]["plain_value"] > 0
     rf = d["roofline"]
     assert rf["bound"] in ("hbm", "tensor") and rf["peak"] > 0
     assert abs(rf["frac"] - rf["achieved"] / rf["peak"]) < 1e-9

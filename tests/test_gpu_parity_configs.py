@@ -3,8 +3,10 @@ pipeline against the oracle's realization loop on the same Philox noise --
 border counts, filled surface, flow directions and basin labels bit-exact.
 
 * plain-4096: 4096^2 fBm DEM (seed 1, Hurst 0.75, 0-300 m, 2000 pits),
-  streams at accumulation 2000, Gaussian 60 m, sd 1.5 m; 3 realizations.
-* eval-8192: 8192^2 (Hurst 0.8, 20000 pits), Gaussian 60 m; 2 realizations.
+  streams at accumulation 2000, Gaussian 60 m, sd 1.5 m; 3 realizations,
+  single and as one batched step of 3.
+* eval-8192: 8192^2 (Hurst 0.8, 20000 pits), Gaussian 60 m; 2 realizations,
+  single and as one batched step of 2.
 * the batched workload's four grids at full size (2048^2, 257x1013,
   1500x733, 3001x401) with exponential filters of radius 8, 19 and 30.
 * stress-16384: 16384^2 with 20 % flat lake plateaus (discs of 50-400
@@ -43,30 +45,35 @@ def _oracle_run(oracle, dem, streams, seed, reals, model, rng_m, sigma):
     return mc, last
 
 
-def _check_workload(oracle, name, reals, seed):
+def _check_workload(oracle, name, reals, seed, batch=1):
+    """The pipeline (single realizations, and with batch > 1 also in batched
+    steps of `batch`) against the oracle."""
     from cageo_gb300 import api, synth
     dem, streams, p = synth.workload(name, ids="components")
-    pipe = api.Pipeline(dem, streams, cell_size=p["cell"], filter_model=api.FILTER_GAUSSIAN,
-                        practical_range=p["range_m"], error_stddev=p["sigma"], seed=seed)
-    pipe.run(0, reals)
-    got = pipe.counts()
-    f, d, lab = pipe.last_stages()
-    pipe.close()
+    runs = []
+    for b in sorted({1, batch}):
+        pipe = api.Pipeline(dem, streams, cell_size=p["cell"], filter_model=api.FILTER_GAUSSIAN,
+                            practical_range=p["range_m"], error_stddev=p["sigma"], seed=seed)
+        pipe.set_batch(b)
+        pipe.run(0, reals)
+        runs.append((b, pipe.counts(), pipe.last_stages()))
+        pipe.close()
     ref, (rf, rd, rl) = _oracle_run(oracle, dem, streams, seed, range(reals), 1, p["range_m"],
                                     p["sigma"])
-    assert np.array_equal(bits(f), bits(rf)), "filled surface"
-    assert np.array_equal(d, rd), "flow directions"
-    assert np.array_equal(lab, rl), "basin labels"
-    assert np.array_equal(got, ref), "border counts"
+    for b, got, (f, d, lab) in runs:
+        assert np.array_equal(bits(f), bits(rf)), "filled surface (batch %d)" % b
+        assert np.array_equal(d, rd), "flow directions (batch %d)" % b
+        assert np.array_equal(lab, rl), "basin labels (batch %d)" % b
+        assert np.array_equal(got, ref), "border counts (batch %d)" % b
     return dem, streams, rd
 
 
 def test_plain_4096(cuda, oracle):
-    _check_workload(oracle, "plain-4096", 3, seed=1)
+    _check_workload(oracle, "plain-4096", 3, seed=1, batch=3)
 
 
 def test_eval_8192(cuda, oracle):
-    _check_workload(oracle, "eval-8192", 2, seed=3)
+    _check_workload(oracle, "eval-8192", 2, seed=3, batch=2)
 
 
 # (grid index in the batched workload, practical range in m -> radius)
