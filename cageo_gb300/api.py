@@ -249,12 +249,13 @@ def pitfill(dem, nodata_dem=-9999.0, workspace=None, mode=FILL_CPU_COMPAT):
 
 FILL_STATS = ("last_pass", "phases", "passes", "passes_b", "us", "us_b", "us_phases", "tiles",
               "rounds", "tiles_b", "rounds_b", "kcyc_load", "kcyc_sweep", "kcyc_store",
-              "kcyc_idle", "kcyc_idle_b")
+              "kcyc_idle", "kcyc_idle_b", "reset_cells")
 
 
 def pitfill_exact_warm(dem, warm=None, nodata_dem=-9999.0, workspace=None):
-    """Exact fill relaxed down from `warm` (None: +inf).  Returns (filled,
-    stats dict).  Exact only where warm >= the exact fill; verify otherwise."""
+    """Exact fill relaxed down from `warm` (None: +inf), verified and repaired
+    by the fill itself (the result is the exact fill for any start).  Returns
+    (filled, stats dict)."""
     import torch
     _grid(dem, torch.float32, "dem")
     if warm is not None:
@@ -479,10 +480,10 @@ class Pipeline:
                                                   threshold))
 
     def warmstart_stats(self):
-        s = np.zeros(8, np.int64)
-        _check(lib().cageo_pipeline_warmstart_stats(self._p, s.ctypes.data_as(_vp), 8))
-        keys = ("realizations", "repaired", "undrained_cells", "warm_tiles", "warm_rounds",
-                "repair_rounds", "warm_fill_us", "repair_fill_us")
+        s = np.zeros(9, np.int64)
+        _check(lib().cageo_pipeline_warmstart_stats(self._p, s.ctypes.data_as(_vp), 9))
+        keys = ("realizations", "repaired", "reset_cells", "warm_tiles", "warm_rounds",
+                "repair_rounds", "warm_fill_us", "repair_fill_us", "repair_tiles")
         return {k: int(v) for k, v in zip(keys, s)}
 
     FILL_PARTS = ("fill_setup", "flood_a", "flood_b", "phases", "fill_final")

@@ -48,31 +48,6 @@ cageo_status launch_to_bytes(const float* in, uint8_t* out, int64_t n, unsigned 
 cageo_status ws_infer(const float* params, const float* v, float* warm, float* depth, int W,
                       int H, float nodata, float threshold, cudaStream_t s);
 
-// Learned warm start: cells whose trace ends without an outlet (ERROR) are
-// the cells the warm-started fill left too low; count them (one atomic per
-// block) and restart those from +inf, the others from the fill's values.
-__global__ void count_error_kernel(const int* __restrict__ label, int64_t n,
-                                   unsigned int* counter) {
-  unsigned int c = 0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    c += label[i] == kError;
-  c = __reduce_add_sync(0xffffffffu, c);
-  __shared__ unsigned int bc;
-  if (threadIdx.x == 0) bc = 0;
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0 && c) atomicAdd(&bc, c);
-  __syncthreads();
-  if (threadIdx.x == 0 && bc) atomicAdd(counter, bc);
-}
-
-__global__ void repair_start_kernel(const int* __restrict__ label,
-                                    const float* __restrict__ filled, float* __restrict__ warm,
-                                    int64_t n) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) warm[i] = label[i] == kError ? kInf : filled[i];
-}
-
 // End of a step of `count` realizations: record the realizations of a
 // flagged step (none of them was counted), clear the flag and advance the
 // device realization counter.
@@ -141,12 +116,13 @@ struct cageo_pipeline {
   cudaGraphExec_t exec = nullptr;
   bool graph_ok = false;
   int64_t stats[25] = {};
-  // Learned warm start (exact mode only): parameters, warm surface, counter.
+  // Learned warm start (exact mode only): parameters, warm surface, and the
+  // fill's warm-start counters accumulated on the device (9 entries, see
+  // fill_accumulate_warm_stats).
   float* ws_params = nullptr;
   float* warm = nullptr;
-  unsigned int* ws_count = nullptr;
+  unsigned long long* ws_acc = nullptr;
   float ws_threshold = 0.0f;
-  int64_t ws_stats[8] = {};
   // Digest of the DEM and stream grids (grid_digest_kernel), for checkpoints.
   unsigned long long input_digest = 0;
   // Batched steps (cageo_pipeline_set_batch): `batch` realizations share one
@@ -184,7 +160,7 @@ void free_all(cageo_pipeline* p) {
   if (p->graph) cudaGraphDestroy(p->graph);
   void* bufs[] = {p->dem, p->streams, p->noise, p->q, p->filled, p->filter, p->tmp, p->code,
                   p->dir, p->flatdist, p->label, p->counts, p->fill_ws, p->route_ws,
-                  p->trace_ws, p->dscal, p->ws_params, p->warm, p->ws_count};
+                  p->trace_ws, p->dscal, p->ws_params, p->warm, p->ws_acc};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (p->stream) cudaStreamDestroy(p->stream);
@@ -194,10 +170,18 @@ bool exact_mode(const cageo_pipeline* p) { return p->cfg.fill_mode == CAGEO_FILL
 
 // Fill, routing and tracing of the current realization in the pipeline's
 // mode; p->q holds the (quantized or raw) burned realistic DEM.
+// With the learned warm start (exact mode), the network's warm surface is
+// inferred from q first; the fill verifies and repairs it itself.
 cageo_status enqueue_fill(cageo_pipeline* p) {
-  if (exact_mode(p))
+  if (!exact_mode(p)) return fill_run(p->q, p->filled, p->fw, p->cfg.nodata_dem, p->stream);
+  if (!p->ws_params)
     return fill_run_exact(p->q, p->filled, p->fw, p->cfg.nodata_dem, nullptr, p->stream);
-  return fill_run(p->q, p->filled, p->fw, p->cfg.nodata_dem, p->stream);
+  cageo_status st = ws_infer(p->ws_params, p->q, p->warm, nullptr, p->W, p->H, p->cfg.nodata_dem,
+                             p->ws_threshold, p->stream);
+  if (st) return st;
+  if ((st = fill_run_exact(p->q, p->filled, p->fw, p->cfg.nodata_dem, p->warm, p->stream)))
+    return st;
+  return fill_accumulate_warm_stats(p->fw, p->ws_acc, p->stream);
 }
 
 cageo_status enqueue_route(cageo_pipeline* p) {
@@ -277,59 +261,6 @@ cageo_status enqueue_batch(cageo_pipeline* p) {
   }
   realization_end_kernel<<<1, 32, 0, s>>>(p->dscal, (int*)p->dscal + 1, p->dscal + 3,
                                           p->dscal + 2, (unsigned int)K);
-  CAGEO_CUDA(cudaGetLastError());
-  return CAGEO_OK;
-}
-
-// One realization with the learned warm start (exact mode), run from the
-// host because its repair is data-dependent.  The fill starts from the
-// network's warm surface; a cell whose trace then ends without an outlet
-// was left too low (every cell that drains holds the exact fill's value,
-// which no fill relaxed from above can undershoot), so those cells restart
-// from +inf, the rest from their values, and the fill, routing and tracing
-// run again: the result equals the plain exact fill's.
-cageo_status run_learned(cageo_pipeline* p) {
-  cudaStream_t s = p->stream;
-  const cageo_pipeline_config& c = p->cfg;
-  const unsigned eb = (unsigned)((p->N + 255) / 256);
-  cageo_status st;
-  int64_t fs[kFillStats];
-  if ((st = fill_reset_scalars(p->fw, s))) return st;
-  if ((st = launch_noise(p->noise, p->N, c.seed, 0, p->dscal, c.error_mean, c.error_stddev, s)))
-    return st;
-  if ((st = launch_front(p->noise, p->W, p->H, c.filter_model, p->filter, p->radius, p->fp, s)))
-    return st;
-  if ((st = ws_infer(p->ws_params, p->q, p->warm, nullptr, p->W, p->H, c.nodata_dem,
-                     p->ws_threshold, s)))
-    return st;
-  if ((st = fill_run_exact(p->q, p->filled, p->fw, c.nodata_dem, p->warm, s))) return st;
-  if ((st = enqueue_route(p)) || (st = enqueue_trace(p))) return st;
-  CAGEO_CUDA(cudaMemsetAsync(p->ws_count, 0, sizeof(unsigned int), s));
-  count_error_kernel<<<1024, 256, 0, s>>>(p->label, p->N, p->ws_count);
-  unsigned int bad = 0;
-  CAGEO_CUDA(cudaMemcpyAsync(&bad, p->ws_count, sizeof(bad), cudaMemcpyDeviceToHost, s));
-  CAGEO_CUDA(cudaStreamSynchronize(s));
-  if ((st = fill_check_status(p->fw, fs))) return st;
-  p->ws_stats[0]++;
-  p->ws_stats[3] += fs[7];
-  p->ws_stats[4] += fs[8];
-  p->ws_stats[6] += fs[4];
-  if (bad) {
-    p->ws_stats[1]++;
-    p->ws_stats[2] += bad;
-    repair_start_kernel<<<eb, 256, 0, s>>>(p->label, p->filled, p->warm, p->N);
-    if ((st = fill_reset_scalars(p->fw, s))) return st;
-    if ((st = fill_run_exact(p->q, p->filled, p->fw, c.nodata_dem, p->warm, s))) return st;
-    if ((st = enqueue_route(p)) || (st = enqueue_trace(p))) return st;
-    CAGEO_CUDA(cudaStreamSynchronize(s));
-    if ((st = fill_check_status(p->fw, fs))) return st;
-    p->ws_stats[5] += fs[8];
-    p->ws_stats[7] += fs[4];
-  }
-  if ((st = border_u32_gated(p->label, p->counts, p->W, p->H, (const int*)p->dscal + 1, s)))
-    return st;
-  realization_end_kernel<<<1, 32, 0, s>>>(p->dscal, (int*)p->dscal + 1, p->dscal + 3,
-                                          p->dscal + 2, 1u);
   CAGEO_CUDA(cudaGetLastError());
   return CAGEO_OK;
 }
@@ -481,6 +412,7 @@ static cageo_status pipeline_run(cageo_pipeline* p, uint32_t first, int count) {
   CAGEO_CUDA(cudaMemcpyAsync(p->dscal, &first, sizeof(uint32_t), cudaMemcpyHostToDevice, s));
   CAGEO_CUDA(cudaMemsetAsync(p->dscal + 1, 0, 2 * sizeof(uint32_t), s));
   const bool stage_only = p->cfg.nodata_dem == 0.0f;
+  // Learned warm starts run on the fast path too (never batched).
   const bool learned = p->ws_params != nullptr && !stage_only;
   int done = 0;
   // Whole batched steps first (cageo_pipeline_set_batch), then single
@@ -516,7 +448,7 @@ static cageo_status pipeline_run(cageo_pipeline* p, uint32_t first, int count) {
     }
     done = nb * K;
   }
-  if (!stage_only && !learned && count > done && p->cfg.use_graphs && !p->graph_ok && !p->exec) {
+  if (!stage_only && count > done && p->cfg.use_graphs && !p->graph_ok && !p->exec) {
     // Warm-up outside capture (kernel attributes, occupancy caches), then
     // capture one realization.
     if ((st = enqueue_fast(p))) return st;
@@ -542,8 +474,6 @@ static cageo_status pipeline_run(cageo_pipeline* p, uint32_t first, int count) {
   for (int i = done; i < count; i++) {
     if (stage_only) {
       if ((st = run_stage_path(p, first + (uint32_t)i))) return st;
-    } else if (learned) {
-      if ((st = run_learned(p))) return st;
     } else if (p->graph_ok) {
       CAGEO_CUDA(cudaGraphLaunch(p->exec, s));
     } else {
@@ -1040,6 +970,7 @@ extern "C" cageo_status cageo_pipeline_set_warmstart(cageo_pipeline* p, const fl
                                                      int n, float threshold) {
   CAGEO_CHECK_ARG(p, "null pipeline");
   CAGEO_CUDA(cudaStreamSynchronize(p->stream));
+  drop_graph(p);  // the captured step holds the old fill
   if (!h_params) {
     if (p->ws_params) cudaFree(p->ws_params);
     p->ws_params = nullptr;
@@ -1050,17 +981,22 @@ extern "C" cageo_status cageo_pipeline_set_warmstart(cageo_pipeline* p, const fl
   CAGEO_CHECK_ARG(n == cageo_ws_param_count(), "parameter count");
   if (!p->ws_params) CAGEO_CUDA(cudaMalloc((void**)&p->ws_params, sizeof(float) * n));
   if (!p->warm) CAGEO_CUDA(cudaMalloc((void**)&p->warm, sizeof(float) * p->N));
-  if (!p->ws_count) CAGEO_CUDA(cudaMalloc((void**)&p->ws_count, 16));
+  if (!p->ws_acc) CAGEO_CUDA(cudaMalloc((void**)&p->ws_acc, sizeof(unsigned long long) * 9));
   CAGEO_CUDA(cudaMemcpy(p->ws_params, h_params, sizeof(float) * n, cudaMemcpyHostToDevice));
+  CAGEO_CUDA(cudaMemset(p->ws_acc, 0, sizeof(unsigned long long) * 9));
   p->ws_threshold = threshold;
-  for (auto& v : p->ws_stats) v = 0;
   return CAGEO_OK;
 }
 
 extern "C" cageo_status cageo_pipeline_warmstart_stats(cageo_pipeline* p, int64_t* h_stats,
                                                        int n) {
   CAGEO_CHECK_ARG(p && h_stats, "null argument");
-  for (int i = 0; i < n && i < 8; i++) h_stats[i] = p->ws_stats[i];
+  unsigned long long acc[9] = {};
+  if (p->ws_acc) {
+    CAGEO_CUDA(cudaStreamSynchronize(p->stream));
+    CAGEO_CUDA(cudaMemcpy(acc, p->ws_acc, sizeof(acc), cudaMemcpyDeviceToHost));
+  }
+  for (int i = 0; i < n && i < 9; i++) h_stats[i] = (int64_t)acc[i];
   return CAGEO_OK;
 }
 

@@ -60,6 +60,7 @@ enum : int {
   S_US_B = 16,     // microseconds of flood B up to its first convergence
   S_US_P = 17,     // microseconds of the phase loop
   S_PEND = 18,     // 3 slots: pending cells seen by a phase
+  S_RESET = 21,    // warm-started exact fill: cells restarted from +inf (unsupported)
   // Per-visit statistics, updated by every tile visit: a line of their own
   // (96..127), away from the error flag that idle warps poll.
   S_TILES_A = 96,   // tiles processed by flood A
@@ -186,7 +187,8 @@ struct FloodArgs {
   FillWork w;
   // Flood B runs as two launches: 1 = seeding and the main drain, 2 = the
   // confirmation phases (the undecided cells found and labelled by plain
-  // kernels in between).  Flood A ignores it.
+  // kernels in between).  3 = the repair flood of a warm-started exact fill
+  // (its statistics go to flood B's slots).  Flood A ignores 1 and 2.
   int stage = 0;
 };
 
@@ -263,14 +265,15 @@ struct VisitStats {
 };
 
 template <int MODE>
-__device__ __forceinline__ void flush_stats(const FillWork& w, VisitStats& st) {
+__device__ __forceinline__ void flush_stats(const FillWork& w, VisitStats& st, bool b_slots) {
   if (!st.tiles && !st.kidle) return;
-  atomicAdd(&w.scal[MODE != 1 ? S_TILES_A : S_TILES_B], st.tiles);
-  atomicAdd(&w.scal[MODE != 1 ? S_ROUNDS_A : S_ROUNDS_B], st.rounds);
+  b_slots = b_slots || MODE == 1;
+  atomicAdd(&w.scal[b_slots ? S_TILES_B : S_TILES_A], st.tiles);
+  atomicAdd(&w.scal[b_slots ? S_ROUNDS_B : S_ROUNDS_A], st.rounds);
   atomicAdd(&w.scal[S_KCYC_LOAD], st.kload);
   atomicAdd(&w.scal[S_KCYC_SWEEP], st.ksweep);
   atomicAdd(&w.scal[S_KCYC_STORE], st.kstore);
-  if (st.kidle) atomicAdd(&w.scal[MODE != 1 ? S_KCYC_IDLE_A : S_KCYC_IDLE_B], st.kidle);
+  if (st.kidle) atomicAdd(&w.scal[b_slots ? S_KCYC_IDLE_B : S_KCYC_IDLE_A], st.kidle);
   st = VisitStats{};
 }
 
@@ -590,7 +593,7 @@ __device__ bool drain(WarpSmem<MODE>& s, const FloodArgs& a, int lane, int ntile
       const bool done = process_tile<MODE>(s, a, t, lane, st);
       if (lane == 0) {
         tq_finish(fill_queue(w), t, done);
-        if (st.tiles >= 64) flush_stats<MODE>(w, st);
+        if (st.tiles >= 64) flush_stats<MODE>(w, st, a.stage == 3);
       }
       __syncwarp();
       idle = 0;
@@ -602,7 +605,8 @@ __device__ bool drain(WarpSmem<MODE>& s, const FloodArgs& a, int lane, int ntile
       break;
     }
     if (vs[S_PENDING] == 0u) break;
-    if (++idle > (1LL << 24) || vs[MODE != 1 ? S_TILES_A : S_TILES_B] > visit_cap) {
+    if (++idle > (1LL << 24) ||
+        vs[(MODE == 1 || a.stage == 3) ? S_TILES_B : S_TILES_A] > visit_cap) {
       if (lane == 0) atomicCAS((int*)(w.scal + S_ERR), 0, 2);
       ok = false;
       break;
@@ -613,7 +617,7 @@ __device__ bool drain(WarpSmem<MODE>& s, const FloodArgs& a, int lane, int ntile
   }
   if (lane == 0) {
     if (idle_from >= 0) st.kidle += (unsigned int)((clock64() - idle_from) >> 10);
-    flush_stats<MODE>(w, st);
+    flush_stats<MODE>(w, st, a.stage == 3);
   }
   __syncwarp();
   return ok;
@@ -720,7 +724,9 @@ fill_flood_kernel(FloodArgs a) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     vs[S_PASS] = (unsigned int)p;
     const unsigned int us = (unsigned int)((global_ns() - t_start) / 1000);
-    if (MODE != 1) {
+    if (MODE != 1 && a.stage == 3) {
+      vs[S_US_B] = us;
+    } else if (MODE != 1) {
       vs[S_PASSES_A] = (unsigned int)(p - p0 + 1);
       vs[S_US_A] = us;
     } else if (!phases) {
@@ -802,11 +808,58 @@ __global__ void fill_init_exact_kernel(const float* __restrict__ v, float* __res
     const float e = v[i];
     uint8_t f = 0;
     if (e == nodata) f = FNODATA;
-    else if (x == 0 || y == 0 || x == W - 1 || y == H - 1 || e == 0.0f) f = FOUTLET;
+    else if (x == 0 || y == 0 || x == W - 1 || y == H - 1 || e == 0.0f) f = FOUTLET | FCLEAN;
     F[i] = f;
     Wg[i] = f ? e : (warm ? fmaxf(warm[i], e) : kInf);
-    if (f == FOUTLET) tseed[(y / kTile) * tiles_x + x / kTile] = 1;
+    if (f & FOUTLET) tseed[(y / kTile) * tiles_x + x / kTile] = 1;
   }
+}
+
+// Verification of a warm-started exact fill.  The warm flood keeps clean
+// marks: in exact mode every reached cell relays, so a marked cell's level
+// is supported -- a chain of relays from an outlet reaches it with no step
+// above its level -- and such a level is never below the exact fill (the
+// chain is a path whose highest elevation it covers).  At the flood's
+// fixpoint no cell is above the exact fill either (induction along its
+// optimal path), so a supported cell holds the answer.  Every other cell
+// (started too low, pulled down by one that was, or unreached) restarts
+// from +inf and marks its tile for the repair flood; with every start an
+// upper bound again, the repair flood ends at the exact fill.  Four
+// consecutive cells per thread; the flags are workspace (aligned).  Also
+// resets the work queue's positions.
+__global__ void fill_unsupported_kernel(float* __restrict__ Wg, uint8_t* __restrict__ F,
+                                        uint8_t* __restrict__ tseed, unsigned int* scal,
+                                        int tiles_x, int W, int64_t n) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    scal[S_HEAD] = 0u;
+    scal[S_TAIL] = 0u;
+    scal[S_PENDING] = 0u;
+  }
+  const int64_t b4 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+  unsigned int reset = 0;
+  if (b4 < n) {
+    uint8_t fv[4];
+    if (b4 + 4 <= n) {
+      const uchar4 f4 = *reinterpret_cast<const uchar4*>(F + b4);
+      fv[0] = f4.x; fv[1] = f4.y; fv[2] = f4.z; fv[3] = f4.w;
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; k++) fv[k] = b4 + k < n ? F[b4 + k] : FNODATA;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const uint8_t f = fv[k];
+      if (f & (FNODATA | FOUTLET | FCLEAN)) continue;
+      const int64_t i = b4 + k;
+      Wg[i] = kInf;
+      F[i] = f & (uint8_t)~FBELOW;
+      const int y = (int)(i / W), x = (int)(i - (int64_t)y * W);
+      tseed[(y / kTile) * tiles_x + x / kTile] = 1;
+      reset++;
+    }
+  }
+  reset = __reduce_add_sync(0xffffffffu, reset);
+  if ((threadIdx.x & 31) == 0 && reset) atomicAdd(&scal[S_RESET], reset);
 }
 
 // Cells no outlet reaches keep the reference's initial value.
@@ -1109,8 +1162,24 @@ cageo_status fill_run_exact(const float* v, float* filled, const FillWork& w, fl
   CAGEO_CUDA(cudaMemsetAsync(w.tconv, 0, nt, s));
   CAGEO_CUDA(cudaMemsetAsync(w.lists, 0xff, (2 * nt + kRingSlack) * sizeof(int), s));  // empty ring
   FloodArgs a{v, filled, w};
-  cageo_status st = launch_flood<0>(a, s);
-  if (st) return st;
+  if (!warm) {
+    cageo_status st = launch_flood<0>(a, s);
+    if (st) return st;
+  } else {
+    // Warm flood with support marks, then the unsupported cells restart
+    // from +inf and the repair flood visits their tiles (the others keep
+    // their states: a tile done in the warm flood holds the answer).
+    cageo_status st = launch_flood<2>(a, s);
+    if (st) return st;
+    CAGEO_CUDA(cudaMemsetAsync(w.tseed, 0, nt, s));
+    const unsigned ublocks = (unsigned)((n + 4 * 256 - 1) / (4 * 256));
+    fill_unsupported_kernel<<<ublocks, 256, 0, s>>>(filled, w.flags, w.tseed, w.scal,
+                                                    w.tiles_x, w.W, n);
+    CAGEO_CUDA(cudaGetLastError());
+    CAGEO_CUDA(cudaMemsetAsync(w.tconv, 0, nt, s));
+    a.stage = 3;
+    if ((st = launch_flood<0>(a, s))) return st;
+  }
   fill_final_exact_kernel<<<blocks, 256, 0, s>>>(filled, n);
   CAGEO_CUDA(cudaGetLastError());
   return CAGEO_OK;
@@ -1119,6 +1188,32 @@ cageo_status fill_run_exact(const float* v, float* filled, const FillWork& w, fl
 cageo_status fill_quantize_min(float* d, const FillWork& w, float nodata, cudaStream_t s) {
   const int64_t n = (int64_t)w.W * w.H;
   quantize_min_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d, n, nodata, w.scal + S_MIN);
+  CAGEO_CUDA(cudaGetLastError());
+  return CAGEO_OK;
+}
+
+// Adds a warm-started exact fill's counters to acc (device, 9 entries):
+// fills, fills that restarted any cell, cells restarted, tile visits and
+// sweep rounds of the warm flood, sweep rounds of the repair flood,
+// microseconds of the warm and of the repair flood, repair tile visits.
+__global__ void fill_warm_stats_kernel(const unsigned int* __restrict__ scal,
+                                       unsigned long long* acc) {
+  if (threadIdx.x != 0) return;
+  const unsigned int reset = scal[S_RESET];
+  acc[0] += 1;
+  acc[1] += reset ? 1 : 0;
+  acc[2] += reset;
+  acc[3] += scal[S_TILES_A];
+  acc[4] += scal[S_ROUNDS_A];
+  acc[5] += scal[S_ROUNDS_B];
+  acc[6] += scal[S_US_A];
+  acc[7] += scal[S_US_B];
+  acc[8] += scal[S_TILES_B];
+}
+
+cageo_status fill_accumulate_warm_stats(const FillWork& w, unsigned long long* acc,
+                                        cudaStream_t s) {
+  fill_warm_stats_kernel<<<1, 32, 0, s>>>(w.scal, acc);
   CAGEO_CUDA(cudaGetLastError());
   return CAGEO_OK;
 }
@@ -1143,6 +1238,7 @@ cageo_status fill_check_status(const FillWork& w, int64_t* stats) {
     stats[13] = h[S_KCYC_STORE];
     stats[14] = h[S_KCYC_IDLE_A];
     stats[15] = h[S_KCYC_IDLE_B];
+    stats[16] = h[S_RESET];
   }
   if (h[S_ERR]) {
     set_error(h[S_ERR] == 1   ? "pit filling: a grid-wide wait hit its limit"

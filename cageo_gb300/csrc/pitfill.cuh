@@ -50,10 +50,10 @@ FillWork fill_carve(void* base, int W, int H);
 cageo_status fill_run(const float* q, float* filled, const FillWork& w,
                       float nodata, cudaStream_t s);
 // Exact float fill of v (the reference's GPU path): no quantization, no
-// minimum needed.  `warm` (may be null): per-cell start values; a start
-// below the answer anywhere gives a lower fixpoint, so callers verify a
-// warm-started result (every cell must drain to an outlet) and rerun cold
-// where it fails.
+// minimum needed.  `warm` (may be null): per-cell start values.  The fill
+// verifies a warm start itself: after the warm flood, cells whose level no
+// chain of relays from an outlet supports restart from +inf and a repair
+// flood visits their tiles, so the result is the exact fill for any start.
 cageo_status fill_run_exact(const float* v, float* filled, const FillWork& w, float nodata,
                             const float* warm, cudaStream_t s);
 // Quantize d in place (the reference's step (i)) and reduce its minimum
@@ -69,8 +69,15 @@ unsigned int* fill_min_slot(const FillWork& w);
 // phase, microseconds of flood A, of flood B to convergence, of the phase
 // loop, tiles and sweep rounds of flood A, tiles and rounds of flood B,
 // kilo-cycles summed over tile visits spent staging, sweeping, storing, and
-// kilo-cycles warps of flood A and of flood B spent waiting for a tile.
-constexpr int kFillStats = 16;
+// kilo-cycles warps of flood A and of flood B spent waiting for a tile,
+// and the cells a warm-started exact fill restarted from +inf.
+constexpr int kFillStats = 17;
 cageo_status fill_check_status(const FillWork& w, int64_t* stats);
+// Adds the last warm-started exact fill's counters to acc (9 device
+// uint64: fills, fills that restarted cells, cells restarted, warm-flood
+// tile visits and sweep rounds, repair sweep rounds, warm and repair
+// microseconds, repair tile visits).  Stream-ordered, no synchronization.
+cageo_status fill_accumulate_warm_stats(const FillWork& w, unsigned long long* acc,
+                                        cudaStream_t s);
 
 }  // namespace cageo

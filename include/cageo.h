@@ -163,12 +163,13 @@ cageo_status cageo_pitfill(float* d_dem, float* d_filled, int W, int H,
 /* Exact fill (CAGEO_FILL_EXACT semantics) relaxed down from per-cell start
  * values d_warm (NULL: +inf, the plain fill) instead of +inf.  No
  * counterpart in the reference: it is the building block of the learned
- * warm start.  The result equals the exact fill whenever every start value
- * is >= the exact fill's value (a start of +inf always is); a start below
- * it leaves a lower fixpoint in which some cells do not drain, so callers
- * must verify the result (every cell drains to an outlet) and rerun cold
- * where it fails.  h_stats (may be NULL) receives the fill's 16
- * statistics (passes, tiles, sweep rounds ...). */
+ * warm start.  The fill verifies the start itself: after the warm-started
+ * flood, a cell's level counts only if a chain of relaying cells from an
+ * outlet supports it (no step above the level); every other cell (started
+ * too low, pulled down by one that was, or unreached) restarts from +inf and
+ * a repair flood visits the tiles holding them.  The result is the exact
+ * fill for any start.  h_stats (may be NULL) receives the fill's 17
+ * statistics (passes, tiles, sweep rounds ..., [16] cells restarted). */
 cageo_status cageo_pitfill_exact_warm(const float* d_dem, const float* d_warm,
                                       float* d_filled, int W, int H,
                                       float nodata_dem, void* d_workspace,
@@ -414,18 +415,20 @@ cageo_status cageo_pipeline_autotune(cageo_pipeline* p, uint32_t first_realizati
                                      int trials, cageo_tuning* h_best, float* h_ms,
                                      int n_ms);
 /* Learned warm start for an exact-mode pipeline (no counterpart in the
- * reference): realizations then start the fill from the network's warm
- * surface (cells predicted shallower than `threshold` metres at their
- * elevation, the rest at +inf), verify it by tracing, and repair the cells
- * that do not drain; the counts equal the plain exact fill's.  Each such
- * realization synchronizes the stream once (no CUDA graph).  h_params:
- * cageo_ws_param_count() floats, or NULL to switch the warm start off. */
+ * reference): each realization infers a warm surface from its burned
+ * realistic DEM (cells predicted shallower than `threshold` metres start at
+ * their elevation, the rest at +inf) and fills from it with
+ * cageo_pitfill_exact_warm's verification and repair, all on the device (the
+ * step is captured in a CUDA graph like a plain one); the counts equal the
+ * plain exact fill's.  h_params: cageo_ws_param_count() floats, or NULL to
+ * switch the warm start off. */
 cageo_status cageo_pipeline_set_warmstart(cageo_pipeline* p, const float* h_params, int n,
                                           float threshold);
 /* Counters since set_warmstart: [0] warm-started realizations, [1] of them
- * repaired, [2] cells that did not drain before repair, [3] tile visits and
- * [4] sweep rounds of the warm-started fills, [5] sweep rounds of the repair
- * fills, [6] microseconds of the warm-started fills, [7] of the repairs. */
+ * with cells restarted from +inf, [2] cells restarted, [3] tile visits and
+ * [4] sweep rounds of the warm-started floods, [5] sweep rounds of the
+ * repair floods, [6] microseconds of the warm floods, [7] of the repairs,
+ * [8] tile visits of the repairs.  Synchronizes the pipeline's stream. */
 cageo_status cageo_pipeline_warmstart_stats(cageo_pipeline* p, int64_t* h_stats, int n);
 void cageo_pipeline_destroy(cageo_pipeline* p);
 

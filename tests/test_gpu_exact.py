@@ -101,3 +101,30 @@ def test_exact_pipeline(cuda, oracle, W, H, model, graphs):
     assert np.array_equal(d, rd)
     assert np.array_equal(lab, rl)
     p.close()
+
+
+@pytest.mark.parametrize("start", ["all_dry", "random", "answer", "above"])
+def test_warm_exact_fill_verifies_itself(cuda, oracle, start):
+    """Any warm start gives the exact fill: cells whose level no chain of
+    relays from an outlet supports restart from +inf inside the fill."""
+    import torch
+    from cageo_gb300 import api
+    from cases import make_case
+    dem, _ = make_case(300, 220, seed=71, plateaus=0.2)
+    v = torch.from_numpy(dem).to(cuda)
+    ref = oracle.pitfill_exact(dem)
+    rng = np.random.default_rng(5)
+    if start == "all_dry":
+        warm = v.clone()  # every cell at its own elevation: every pit too low
+    elif start == "random":
+        warm = v + torch.from_numpy(rng.uniform(-3, 3, dem.shape).astype(np.float32)).to(cuda)
+    elif start == "answer":
+        warm = torch.from_numpy(ref).to(cuda)
+    else:
+        warm = torch.from_numpy(ref + 1.0).to(cuda)
+    filled, st = api.pitfill_exact_warm(v, warm)
+    assert np.array_equal(filled.cpu().numpy().view(np.int32), ref.view(np.int32))
+    if start in ("answer", "above"):
+        assert st["reset_cells"] == 0  # every start is supported once relaxed
+    if start == "all_dry":
+        assert st["reset_cells"] > 0

@@ -114,7 +114,7 @@ def test_learned_pipeline_equals_plain_exact(cuda, which):
     st = lp.warmstart_stats()
     assert st["realizations"] == 4
     if which == "untrained":
-        assert st["repaired"] >= 1 and st["undrained_cells"] > 0
+        assert st["repaired"] >= 1 and st["reset_cells"] > 0
     lp.set_warmstart(None, 0.0)
     lp.run(4, 1)
     plain.run(4, 1)
