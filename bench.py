@@ -54,7 +54,7 @@ PIPE_BYTES = 75
 # (dram__bytes_read.sum + dram__bytes_write.sum of that launch divided by
 # its 16.8 M cells), applied per cell to the benchmark grid.
 FLOOD_A_BYTES_PER_CELL = 8
-FLOOD_A_TRAFFIC_PER_CELL = 776.6e6 / (4096 * 4096)
+FLOOD_A_TRAFFIC_PER_CELL = 792.8e6 / (4096 * 4096)
 
 
 def peak_hbm():
