@@ -133,6 +133,12 @@ struct cageo_pipeline {
   void* fill_ws_b = nullptr;
   unsigned int* slab_min = nullptr;
   FillWork fwb;
+  // Routing over the stack as well: directions and flat distances of all
+  // slabs, routing workspace for W x batch*H.
+  int8_t* dirb = nullptr;
+  int* flatdistb = nullptr;
+  void* route_ws_b = nullptr;
+  RouteWork rwb;
   cudaGraph_t graph_b = nullptr;
   cudaGraphExec_t exec_b = nullptr;
   bool last_batched = false;  // the last realization ran in a batched step
@@ -145,12 +151,16 @@ void free_batch(cageo_pipeline* p) {
   if (p->graph_b) cudaGraphDestroy(p->graph_b);
   p->exec_b = nullptr;
   p->graph_b = nullptr;
-  void* bufs[] = {p->qb, p->filledb, p->fill_ws_b, p->slab_min};
+  void* bufs[] = {p->qb, p->filledb, p->fill_ws_b, p->slab_min, p->dirb, p->flatdistb,
+                  p->route_ws_b};
   for (void* b : bufs)
     if (b) cudaFree(b);
   p->qb = p->filledb = nullptr;
   p->fill_ws_b = nullptr;
   p->slab_min = nullptr;
+  p->dirb = nullptr;
+  p->flatdistb = nullptr;
+  p->route_ws_b = nullptr;
   p->batch = 1;
 }
 
@@ -232,9 +242,10 @@ cageo_status enqueue_fast(cageo_pipeline* p) {
 // Launch sequence of one batched step: `p->batch` realizations from the
 // device counter on.  Noise and the fused front run per realization, each
 // into its slab of the stacked q grid (with its own minimum); one fill
-// covers the whole stack (slabs cannot exchange values: see FillWork); then
-// routing, tracing and the border counts run per slab.  The results equal
-// `batch` single realizations bit for bit.
+// covers the whole stack (slabs cannot exchange values: see FillWork), and
+// so does the routing (flat cells are interior: their neighbours lie in
+// their own slab); tracing and the border counts run per slab.  The results
+// equal `batch` single realizations bit for bit.
 cageo_status enqueue_batch(cageo_pipeline* p) {
   cudaStream_t s = p->stream;
   const cageo_pipeline_config& c = p->cfg;
@@ -253,11 +264,16 @@ cageo_status enqueue_batch(cageo_pipeline* p) {
       return st;
   }
   if ((st = fill_run(p->qb, p->filledb, p->fwb, c.nodata_dem, s))) return st;
+  if ((st = route_run(p->filledb, p->dirb, p->flatdistb, p->rwb, s, CAGEO_ROUTE_CPU_COMPAT,
+                      c.nodata_dem)))
+    return st;
   for (int k = 0; k < K; k++) {
-    if ((st = route_run(p->filledb + (size_t)k * p->N, p->dir, p->flatdist, p->rw, s,
-                        CAGEO_ROUTE_CPU_COMPAT, c.nodata_dem)))
+    const int8_t* dir = p->dirb + 2 * (size_t)k * p->N;
+    if ((st = trace_run(dir, p->streams, p->label, p->tw, s, CAGEO_TRACE_CPU_COMPAT, false)))
       return st;
-    if ((st = enqueue_trace_border(p, (const int*)p->dscal + 1))) return st;
+    if ((st = border_u32_from_state(p->tw, p->label, p->counts, (const int*)p->dscal + 1,
+                                    CAGEO_TRACE_CPU_COMPAT, s)))
+      return st;
   }
   realization_end_kernel<<<1, 32, 0, s>>>(p->dscal, (int*)p->dscal + 1, p->dscal + 3,
                                           p->dscal + 2, (unsigned int)K);
@@ -484,8 +500,9 @@ static cageo_status pipeline_run(cageo_pipeline* p, uint32_t first, int count) {
   int64_t fs[kFillStats] = {}, rs[7] = {}, jumps = 0;
   p->last_batched = batched && in_batches == count;
   if (batched && (st = fill_check_status(p->fwb, p->last_batched ? fs : nullptr))) return st;
+  if (batched && (st = route_check_status(p->rwb, p->last_batched ? rs : nullptr))) return st;
   if ((st = fill_check_status(p->fw, p->last_batched ? nullptr : fs))) return st;
-  if ((st = route_check_status(p->rw, rs))) return st;
+  if ((st = route_check_status(p->rw, p->last_batched ? nullptr : rs))) return st;
   if ((st = trace_check_status(p->tw, &jumps))) return st;
   uint32_t nredo = 0;
   CAGEO_CUDA(cudaMemcpy(&nredo, p->dscal + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost));
@@ -816,7 +833,8 @@ extern "C" cageo_status cageo_pipeline_last_stages(cageo_pipeline* p, float* h_f
   const float* filled = p->last_batched ? p->filledb + (size_t)(p->batch - 1) * p->N : p->filled;
   if (h_filled)
     CAGEO_CUDA(cudaMemcpyAsync(h_filled, filled, 4 * p->N, cudaMemcpyDeviceToHost, s));
-  if (h_dir) CAGEO_CUDA(cudaMemcpyAsync(h_dir, p->dir, 2 * p->N, cudaMemcpyDeviceToHost, s));
+  const int8_t* dir = p->last_batched ? p->dirb + 2 * (size_t)(p->batch - 1) * p->N : p->dir;
+  if (h_dir) CAGEO_CUDA(cudaMemcpyAsync(h_dir, dir, 2 * p->N, cudaMemcpyDeviceToHost, s));
   if (h_label) CAGEO_CUDA(cudaMemcpyAsync(h_label, p->label, 4 * p->N, cudaMemcpyDeviceToHost, s));
   CAGEO_CUDA(cudaStreamSynchronize(s));
   return CAGEO_OK;
@@ -954,10 +972,14 @@ extern "C" cageo_status cageo_pipeline_set_batch(cageo_pipeline* p, int batch) {
   cageo_status st;
   if ((st = dalloc(&p->qb, sizeof(float) * nb)) || (st = dalloc(&p->filledb, sizeof(float) * nb)) ||
       (st = dalloc(&p->fill_ws_b, fill_workspace_bytes(p->W, batch * p->H))) ||
-      (st = dalloc(&p->slab_min, sizeof(unsigned int) * 64))) {
+      (st = dalloc(&p->slab_min, sizeof(unsigned int) * 64)) ||
+      (st = dalloc(&p->dirb, 2 * nb)) || (st = dalloc(&p->flatdistb, sizeof(int) * nb)) ||
+      (st = dalloc(&p->route_ws_b, route_workspace_bytes(p->W, batch * p->H)))) {
     free_batch(p);
     return st;
   }
+  p->rwb = route_carve(p->route_ws_b, p->W, batch * p->H);
+  p->rwb.slab_h = p->H;
   p->fwb = fill_carve(p->fill_ws_b, p->W, batch * p->H);
   p->fwb.slab_h = p->H;
   p->fwb.slab_min = p->slab_min;

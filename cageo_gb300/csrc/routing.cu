@@ -76,6 +76,7 @@ __global__ void __launch_bounds__(256) d8_kernel(const float* __restrict__ dem,
                                                  char2* __restrict__ dir,
                                                  int* __restrict__ fd, RouteWork w, float nodata) {
   const int W = w.W, H = w.H;
+  const int slab_h = w.slab_h ? w.slab_h : H;
   const int x = blockIdx.x * kFT + threadIdx.x;
   // The tile's elevations and a one-cell halo in shared memory.
   __shared__ float E[34 * 35];
@@ -100,8 +101,9 @@ __global__ void __launch_bounds__(256) d8_kernel(const float* __restrict__ dem,
     if (x >= W || y >= H) continue;
     const int64_t i = (int64_t)y * W + x;
     int dxi = 0, dyi = 0;
+    const int ys = y % slab_h;  // row within its realization's slab
     if (x == 0) dxi = -1; else if (x == W - 1) dxi = 1;
-    if (y == 0) dyi = -1; else if (y == H - 1) dyi = 1;
+    if (ys == 0) dyi = -1; else if (ys == slab_h - 1) dyi = 1;
     if (dxi || dyi) {
       dir[i] = make_char2((signed char)dxi, (signed char)dyi);
       fd[i] = -1;

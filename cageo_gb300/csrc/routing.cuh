@@ -14,6 +14,11 @@ struct RouteWork {
   int* queued = nullptr;         // per tile: last pass it was queued for
   int* lists = nullptr;          // 2 * ntiles: tile worklists
   unsigned int* scal = nullptr;  // counters, barrier, error
+  // Stacked realizations: H / slab_h grids of slab_h rows each, one above
+  // the other; each slab's first and last rows are its border (0: one grid).
+  // Only the steepest-descent pass needs it: flat cells are interior, so
+  // their neighbours lie in their own slab.
+  int slab_h = 0;
 };
 size_t route_workspace_bytes(int W, int H);
 RouteWork route_carve(void* base, int W, int H);

@@ -326,15 +326,17 @@ cageo_status cageo_pipeline_run_filter(cageo_pipeline* p, uint32_t first_realiza
  * cageo_pipeline_run processes realizations `batch` at a time.  Their noise
  * and fused front run one after another into the slabs of a stacked grid,
  * one pit fill covers the whole stack (the slabs' borders are outlets, so no
- * value crosses between them), and routing, tracing and the border counts
- * run per realization; a batched step is captured in a CUDA graph of its own.
+ * value crosses between them), so does the routing (flat cells are interior
+ * to their slab), and tracing and the border counts run per realization; a
+ * batched step is captured in a CUDA graph of its own.
  * The counts and every stage output equal single realizations bit for bit;
- * batching only shares the fill's persistent launches (their grid barriers
- * and the idle tail of each flood) among the realizations of a step.  A run
+ * batching only shares the persistent launches of the fill and the flat
+ * BFS (their grid barriers and idle tails) among the realizations of a step.  A run
  * of `count` realizations takes count / batch batched steps and the rest
  * singly.  1 <= batch <= 64, batch * cells < 2^31, CPU-compatible fill
- * mode only.  Allocates 2 stacked grids and a fill workspace for them
- * (about 21 bytes per cell per realization); batch = 1 frees them. */
+ * mode only.  Allocates the stacked grids and the fill and routing
+ * workspaces for them (about 27 bytes per cell per realization); batch = 1
+ * frees them. */
 cageo_status cageo_pipeline_set_batch(cageo_pipeline* p, int batch);
 /* Border counts so far as float (the reference's CatchmentBorderType). */
 cageo_status cageo_pipeline_counts(cageo_pipeline* p, float* h_out);
