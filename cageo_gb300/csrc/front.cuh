@@ -5,6 +5,7 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include "fillflags.cuh"
 #include "stage_math.cuh"
 
 namespace cageo {
@@ -26,13 +27,25 @@ struct FrontParams {
   int* anomaly;            // set when the precomputed burn factor may not apply
   float nodata_dem;
   int quantize;            // 1: the CPU fill's 1 mm quantization; 0: raw (exact fill)
+  // The pit fill's set-up, fused (CPU-compatible mode; flags null: not
+  // fused): each cell's flags and start value, and the seed mark of a tile
+  // holding a relaying outlet, computed with minE = 0.  That is the minimum
+  // whenever a stream cell is burned to 0; the fill checks the real minimum
+  // of each realization and redoes the set-up where it differs.
+  uint8_t* flags;          // W*H fill flags
+  float* start;            // W*H fill start values (the filled grid)
+  uint8_t* tseed;          // fill tile seeds (of the whole, possibly stacked, grid)
+  int tiles_x;             // fill tiles per row
+  int row0;                // this grid's first row in the stacked grid
+  int W, H;                // this grid's size (its border)
   float factor[kMaxBurnClasses + 1];  // factor[0] unused
 };
 
-// Writes one output of the fused front from the convolved value and the
-// cell's DEM value and static code; returns q for the min reduction.
-__device__ inline float front_epilogue(const FrontParams& p, int64_t i, float conv, float dem,
-                                       uint8_t c) {
+// Writes one output of the fused front (cell i at column x, row y) from the
+// convolved value and the cell's DEM value and static code; returns q for
+// the min reduction.
+__device__ inline float front_epilogue(const FrontParams& p, int64_t i, int x, int y, float conv,
+                                       float dem, uint8_t c) {
   float v = realistic_value(dem, conv, p.nodata_dem);
   if (c & kCodeBurnStream) {
     // The reference tests a stream neighbour's elevation against NODATA;
@@ -44,6 +57,13 @@ __device__ inline float front_epilogue(const FrontParams& p, int64_t i, float co
   if (k) v = __fmul_rn(v, p.factor[k]);
   float q = p.quantize ? fill_quantize(v, p.nodata_dem) : v;
   p.q[i] = q;
+  if (p.flags) {
+    const uint8_t f =
+        fill_init_flags(q, p.nodata_dem, 0.0f, x == 0 || y == 0 || x == p.W - 1 || y == p.H - 1);
+    p.flags[i] = f;
+    p.start[i] = (f & (FNODATA | FOUTLET)) ? q : __builtin_huge_valf();
+    if ((f & (FOUTLET | FNONPASS)) == FOUTLET) p.tseed[((p.row0 + y) >> 5) * p.tiles_x + (x >> 5)] = 1;
+  }
   return q;
 }
 

@@ -75,7 +75,7 @@ struct StoreEpilogue {
   float* out;
   struct Pre {};
   __device__ inline Pre pre(int64_t) const { return {}; }
-  __device__ inline float operator()(int64_t i, float v, Pre) const {
+  __device__ inline float operator()(int64_t i, int, int, float v, Pre) const {
     out[i] = v;
     return v;
   }
@@ -88,8 +88,8 @@ struct FrontEpilogue {
     uint8_t code;
   };
   __device__ inline Pre pre(int64_t i) const { return {p.dem[i], p.code[i]}; }
-  __device__ inline float operator()(int64_t i, float v, Pre pr) const {
-    return front_epilogue(p, i, v, pr.dem, pr.code);
+  __device__ inline float operator()(int64_t i, int x, int y, float v, Pre pr) const {
+    return front_epilogue(p, i, x, y, v, pr.dem, pr.code);
   }
 };
 
@@ -299,7 +299,7 @@ conv_sep_kernel(const float* __restrict__ in, int W, int H,
 #pragma unroll
     for (int j = 0; j < 8; j++) {
       const int gx = x0 + 8 * g + j;
-      if (gx < W) local_min = fminf(local_min, epi((int64_t)gy * W + gx, acc[j], pre[j]));
+      if (gx < W) local_min = fminf(local_min, epi((int64_t)gy * W + gx, gx, gy, acc[j], pre[j]));
     }
   }
   block_min_out(local_min, epi);
@@ -373,7 +373,7 @@ conv_2d_kernel(const float* __restrict__ in, int W, int H,
 #pragma unroll
     for (int j = 0; j < 8; j++) {
       const int gx = x0 + ox + j;
-      if (gx < W) local_min = fminf(local_min, epi((int64_t)gy * W + gx, acc[j], pre[j]));
+      if (gx < W) local_min = fminf(local_min, epi((int64_t)gy * W + gx, gx, gy, acc[j], pre[j]));
     }
   }
   block_min_out(local_min, epi);

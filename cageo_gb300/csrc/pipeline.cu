@@ -226,6 +226,7 @@ cageo_status enqueue_fast(cageo_pipeline* p) {
   const cageo_pipeline_config& c = p->cfg;
   cageo_status st;
   if ((st = fill_reset_scalars(p->fw, s))) return st;
+  if (p->fw.front_init && (st = fill_clear_seeds(p->fw, s))) return st;
   if ((st = launch_noise(p->noise, p->N, c.seed, 0, p->dscal, c.error_mean, c.error_stddev, s)))
     return st;
   if ((st = launch_front(p->noise, p->W, p->H, c.filter_model, p->filter, p->radius, p->fp, s)))
@@ -252,6 +253,7 @@ cageo_status enqueue_batch(cageo_pipeline* p) {
   const int K = p->batch;
   cageo_status st;
   if ((st = fill_reset_scalars(p->fwb, s))) return st;
+  if ((st = fill_clear_seeds(p->fwb, s))) return st;
   CAGEO_CUDA(cudaMemsetAsync(p->slab_min, 0xff, sizeof(unsigned int) * K, s));
   for (int k = 0; k < K; k++) {
     if ((st = launch_noise(p->noise, p->N, c.seed, (uint32_t)k, p->dscal, c.error_mean,
@@ -260,6 +262,11 @@ cageo_status enqueue_batch(cageo_pipeline* p) {
     FrontParams fp = p->fp;
     fp.q = p->qb + (size_t)k * p->N;
     fp.min_ord = p->slab_min + k;
+    fp.flags = p->fwb.flags + (size_t)k * p->N;
+    fp.start = p->filledb + (size_t)k * p->N;
+    fp.tseed = p->fwb.tseed;
+    fp.tiles_x = p->fwb.tiles_x;
+    fp.row0 = k * p->H;
     if ((st = launch_front(p->noise, p->W, p->H, c.filter_model, p->filter, p->radius, fp, s)))
       return st;
   }
@@ -296,7 +303,12 @@ cageo_status run_stage_path(cageo_pipeline* p, uint32_t r) {
                               c.nodata_stream, s)))
     return st;
   if (!exact_mode(p) && (st = fill_quantize_min(p->q, p->fw, c.nodata_dem, s))) return st;
-  if ((st = enqueue_fill(p))) return st;
+  // The stage kernels do not set up the fill: fill_run does it in full.
+  const bool fused = p->fw.front_init;
+  p->fw.front_init = false;
+  st = enqueue_fill(p);
+  p->fw.front_init = fused;
+  if (st) return st;
   if ((st = enqueue_route(p))) return st;
   if ((st = enqueue_trace_border(p, nullptr))) return st;
   return CAGEO_OK;
@@ -396,6 +408,17 @@ cageo_status create_common(cageo_pipeline** out, const cageo_pipeline_config* cf
   p->fp.anomaly = (int*)p->dscal + 1;
   p->fp.nodata_dem = cfg->nodata_dem;
   p->fp.quantize = cfg->fill_mode == CAGEO_FILL_EXACT ? 0 : 1;
+  // The CPU-compatible fill's set-up runs in the front's epilogue.
+  if (p->fp.quantize) {
+    p->fp.flags = p->fw.flags;
+    p->fp.start = p->filled;
+    p->fp.tseed = p->fw.tseed;
+    p->fp.tiles_x = p->fw.tiles_x;
+    p->fp.row0 = 0;
+    p->fp.W = W;
+    p->fp.H = H;
+    p->fw.front_init = true;
+  }
   PCUDA(cudaStreamSynchronize(s));
 #undef PCUDA
   *out = p;
@@ -559,6 +582,7 @@ extern "C" cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t reali
       break;
     }
     if ((st = fill_reset_scalars(p->fw, s))) break;
+    if (p->fw.front_init && (st = fill_clear_seeds(p->fw, s))) break;
     cudaEventRecord(ev[0], s);
     if ((st = launch_noise(p->noise, p->N, c.seed, 0, p->dscal, c.error_mean, c.error_stddev, s)))
       break;
@@ -983,6 +1007,7 @@ extern "C" cageo_status cageo_pipeline_set_batch(cageo_pipeline* p, int batch) {
   p->fwb = fill_carve(p->fill_ws_b, p->W, batch * p->H);
   p->fwb.slab_h = p->H;
   p->fwb.slab_min = p->slab_min;
+  p->fwb.front_init = true;
   sync_batch_tuning(p);
   p->batch = batch;
   return CAGEO_OK;

@@ -34,17 +34,12 @@
 #include <algorithm>
 #include <type_traits>
 #include "common.cuh"
+#include "fillflags.cuh"
 #include "pitfill.cuh"
 #include "stage_math.cuh"
 #include "tilequeue.cuh"
 
 namespace cageo {
-
-// Per-cell flag bits.  FCLEAN (flood A with clean marks): the cell's level
-// is reached by a path of passable relays from an outlet, so flood B, whose
-// walls are non-passable cells only, gives it the same value.
-constexpr uint8_t FNODATA = 0x01, FOUTLET = 0x02, FNONPASS = 0x04, FCONF = 0x08,
-                  FBELOW = 0x10, FBELOWA = 0x20, FCLEAN = 0x40, FUNSURE = 0x80;
 
 // Scalar block layout (unsigned ints).
 enum : int {
@@ -739,30 +734,13 @@ fill_flood_kernel(FloodArgs a) {
   }
 }
 
-// fill_passable() of a quantized value q = RN(k / 1000) (k an integer, as
-// fill_quantize makes every value the fill sees).  With minE = 0 and
-// 0 <= q < 4096, p = RN(1000 q) lies within 0.25 of k: |q - k/1000| is at
-// most half an ulp of q (<= 2^-13), so |1000 q - k| <= 0.123, and rounding
-// 1000 q (< 2^22) moves it by at most 0.125.  Then toIndex(q) = trunc(p)
-// equals k exactly when p >= k = rint(p), and toElev(k) = RN(k / 1000) = q,
-// while toElev of any other index differs from q (values 0.001 apart are
-// distinct floats below 8192): passable <=> p >= rint(p), no division.
-// Other values take the general test.
-__device__ __forceinline__ bool passable_quantized(float q, float minE) {
-  if (minE == 0.0f && q >= 0.0f && q < 4096.0f) {
-    const float p = __fmul_rn(1000.0f, q);
-    return p >= rintf(p);
-  }
-  return fill_passable(q, minE);
-}
-
 // Cells per thread of the elementwise fill kernels (fewer, longer blocks).
 constexpr int kCellsPerThread = 4;
 
 __global__ void fill_init_kernel(const float* __restrict__ q, float* __restrict__ Wg,
                                  uint8_t* __restrict__ F, const unsigned int* minslot,
                                  uint8_t* __restrict__ tseed, int tiles_x, int W, int H,
-                                 int slab_h, float nodata) {
+                                 int slab_h, float nodata, int check_only) {
   // Block rows step over the grid's rows (no division to find a cell's x
   // and y); kCellsPerThread cells a block-width apart per thread
   // (coalesced).  A stack of realizations takes each slab's borders and
@@ -770,20 +748,16 @@ __global__ void fill_init_kernel(const float* __restrict__ q, float* __restrict_
   for (int y = blockIdx.y; y < H; y += gridDim.y) {
   const int slab = y / slab_h, ys = y - slab * slab_h;
   const float minE = ordered_to_float(minslot[slab]);
+  // After a fused front: its set-up assumed minE = 0.
+  if (check_only && minE == 0.0f) continue;
 #pragma unroll
   for (int k = 0; k < kCellsPerThread; k++) {
     const int x = (blockIdx.x * kCellsPerThread + k) * blockDim.x + threadIdx.x;
     if (x >= W) break;
     const int64_t i = (int64_t)y * W + x;
     const float qv = q[i];
-    uint8_t f = 0;
-    if (qv == nodata) {
-      f = FNODATA;
-    } else {
-      if (!passable_quantized(qv, minE)) f |= FNONPASS;
-      // Outlets keep q in both floods: clean from the start.
-      if (x == 0 || ys == 0 || x == W - 1 || ys == slab_h - 1 || qv == 0.0f) f |= FOUTLET | FCLEAN;
-    }
+    const uint8_t f =
+        fill_init_flags(qv, nodata, minE, x == 0 || ys == 0 || x == W - 1 || ys == slab_h - 1);
     F[i] = f;
     Wg[i] = (f & (FNODATA | FOUTLET)) ? qv : kInf;
     if ((f & FOUTLET) && !(f & FNONPASS)) tseed[(y / kTile) * tiles_x + x / kTile] = 1;
@@ -1090,6 +1064,11 @@ static cageo_status launch_flood(const FloodArgs& a, cudaStream_t s) {
   return CAGEO_ERR_ARGUMENT;
 }
 
+cageo_status fill_clear_seeds(const FillWork& w, cudaStream_t s) {
+  CAGEO_CUDA(cudaMemsetAsync(w.tseed, 0, (size_t)w.tiles_x * w.tiles_y, s));
+  return CAGEO_OK;
+}
+
 cageo_status fill_reset_scalars(const FillWork& w, cudaStream_t s) {
   fill_scalars_kernel<<<1, 32, 0, s>>>(w.scal);
   CAGEO_CUDA(cudaGetLastError());
@@ -1102,13 +1081,16 @@ cageo_status fill_run(const float* q, float* filled, const FillWork& w, float no
   const int64_t n = (int64_t)w.W * w.H;
   const unsigned blocks = (unsigned)((n + 256 * kCellsPerThread - 1) / (256 * kCellsPerThread));
   const size_t nt = (size_t)w.tiles_x * w.tiles_y;
-  CAGEO_CUDA(cudaMemsetAsync(w.tseed, 0, nt, s));
+  if (!w.front_init) CAGEO_CUDA(cudaMemsetAsync(w.tseed, 0, nt, s));
   const dim3 rows((unsigned)((w.W + 256 * kCellsPerThread - 1) / (256 * kCellsPerThread)),
                    (unsigned)w.H);
-  const dim3 init_rows(rows.x, std::min(rows.y, 65535u));
+  // After a fused front, a few block rows check the slabs' minima and
+  // exit (the set-up is redone only where a minimum is not 0).
+  const dim3 init_rows(rows.x, std::min(rows.y, w.front_init ? 1024u : 65535u));
   fill_init_kernel<<<init_rows, 256, 0, s>>>(q, filled, w.flags,
                                              w.slab_min ? w.slab_min : w.scal + S_MIN, w.tseed,
-                                             w.tiles_x, w.W, w.H, w.slab_h ? w.slab_h : w.H, nodata);
+                                             w.tiles_x, w.W, w.H, w.slab_h ? w.slab_h : w.H, nodata,
+                                             w.front_init ? 1 : 0);
   CAGEO_CUDA(cudaGetLastError());
   FloodArgs a{q, filled, w};
   CAGEO_CUDA(cudaMemsetAsync(w.queued, 0, sizeof(int) * nt, s));  // all idle

@@ -32,6 +32,10 @@ struct FillWork {
   // minE).  slab_h = 0: one realization, minimum in the scalar block.
   int slab_h = 0;
   const unsigned int* slab_min = nullptr;
+  // The fused front has set up the flags, the start values and the tile
+  // seeds (with minE = 0; fill_clear_seeds must run before it): fill_run
+  // only redoes the set-up of the slabs whose minimum of q is not 0.
+  bool front_init = false;
   // Profiling only: when set, fill_run records marks[0] after the set-up,
   // [1] after flood A, [2] after flood B's main drain and the undecided-cell
   // kernels, [3] after the confirmation phases.
@@ -60,6 +64,8 @@ cageo_status fill_run_exact(const float* v, float* filled, const FillWork& w, fl
 // into the scalar block.
 cageo_status fill_quantize_min(float* d, const FillWork& w, float nodata,
                                cudaStream_t s);
+// Clears the tile seeds before a fused front sets them (FillWork::front_init).
+cageo_status fill_clear_seeds(const FillWork& w, cudaStream_t s);
 // Launch-time setup of the scalar block and the ordered minimum of q.
 cageo_status fill_reset_scalars(const FillWork& w, cudaStream_t s);
 unsigned int* fill_min_slot(const FillWork& w);

@@ -216,3 +216,27 @@ def test_autotune_keeps_counts(cuda):
         assert np.array_equal(bits(fc[0]), bits(fb[0])) and np.array_equal(fc[2], fb[2])
     with pytest.raises(api.CageoError):
         c.set_tuning(32, 18)
+
+
+@pytest.mark.parametrize("batch", [1, 3])
+def test_pipeline_nodata_cells(cuda, oracle, batch):
+    """NODATA DEM cells make the fill's minimum -9999: the set-up the fused
+    front makes (which assumes a minimum of 0) is redone by the fill."""
+    import torch
+    from cageo_gb300 import api
+    dem, streams = make_case(150, 110, seed=43, nodata_cells=40)
+    p = api.Pipeline(dem, streams, error_stddev=1.5, seed=12)
+    p.set_batch(batch)
+    p.run(0, 6)
+    got = p.counts()
+    f, d, lab = p.last_stages()
+    r = api.filter_radius(60.0, 10.0)
+    taps = api.filter_build(1, 60.0, 10.0, r)
+    mc = np.zeros_like(dem)
+    noise = torch.empty(dem.shape, dtype=torch.float32, device="cuda")
+    for k in range(6):
+        api.noise_philox(noise, 12, k, 0.0, 1.5)
+        mc, rf, rd, rl = oracle.realization(dem, streams, noise.cpu().numpy(), taps, r, 1, mc)
+    assert np.array_equal(got, mc)
+    assert np.array_equal(bits(f), bits(rf)) and np.array_equal(d, rd)
+    assert np.array_equal(lab, rl)
