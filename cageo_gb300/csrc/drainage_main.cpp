@@ -18,7 +18,8 @@
 // reference has no flag for it), --no-graphs, --fill cpu|exact (cpu: the
 // reference CPU path's semantics, the default; exact: its GPU path's exact
 // float fill, flat order and dead-end handling), --checkpoint FILE,
-// --resume FILE.  Output files go to the
+// --resume FILE, --batch K (realizations per batched step; 1).  Output
+// files go to the
 // working directory under the stem of -o (the reference keeps only the
 // stem).  This driver runs on the GPU only; --cpu
 // is refused rather than silently using another implementation.
@@ -37,7 +38,7 @@ struct Options {
   std::string dem = "dem10", stream = "streams", dem_path = "DEM", stream_path = "DEM";
   std::string filter = "Gaussian", output_file, output_option, checkpoint, resume, fill = "cpu";
   float range = 60.0f, mean = 0.0f, sd = 1.0f;
-  int iterations = 10, bevel = 2;
+  int iterations = 10, bevel = 2, batch = 1;
   bool gpu = true, cpu = false, graphs = true, have_seed = false;
   unsigned long long seed = 0;
 };
@@ -64,7 +65,8 @@ void usage() {
       "  --no-graphs                  Launch kernels directly instead of a CUDA graph\n"
       "  --fill arg (=cpu)            cpu: CPU-path semantics; exact: GPU-path exact float fill\n"
       "  --checkpoint arg             Save counts + next realization here after each output\n"
-      "  --resume arg                 Continue from a checkpoint (same grid and --seed)\n");
+      "  --resume arg                 Continue from a checkpoint (same grid and --seed)\n"
+      "  --batch arg (=1)             Realizations per batched step (CPU-path fill; same results)\n");
 }
 
 bool parse_bool(const std::string& v) { return !(v == "0" || v == "false" || v == "off"); }
@@ -103,6 +105,7 @@ int parse(int argc, char** argv, Options* o) {
     else if (a == "--seed") { if (!next(&v)) return 1; o->seed = std::strtoull(v.c_str(), nullptr, 10); o->have_seed = true; }
     else if (a == "--bevel-radius") { if (!next(&v)) return 1; o->bevel = std::atoi(v.c_str()); }
     else if (a == "--no-graphs") { o->graphs = false; }
+    else if (a == "--batch") { if (!next(&v)) return 1; o->batch = std::atoi(v.c_str()); }
     else if (a == "--fill") {
       if (!next(&o->fill)) return 1;
       if (o->fill != "cpu" && o->fill != "exact") {
@@ -209,6 +212,10 @@ int main(int argc, char** argv) {
   std::printf("Seed: %llu\n", (unsigned long long)cfg.seed);
   cageo_pipeline* p = nullptr;
   if (cageo_pipeline_create(&p, &cfg, dem.data(), streams.data())) return fail("pipeline");
+  if (o.batch != 1 && cageo_pipeline_set_batch(p, o.batch)) {
+    cageo_pipeline_destroy(p);
+    return fail("batch");
+  }
   int start = 0;
   if (!o.resume.empty()) {
     uint32_t nxt = 0;

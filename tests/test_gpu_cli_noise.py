@@ -133,6 +133,25 @@ def test_drainage_cli_jpeg(cuda, tmp_path):
     assert np.mean(np.abs(back.astype(int) - img.astype(int))) < 12
 
 
+def test_drainage_cli_batch(cuda, tmp_path):
+    """--batch K: the same counts as one realization at a time; a batch the
+    fill mode does not allow is refused."""
+    from cageo_gb300 import _build, api
+    dem, streams = make_case(90, 70, seed=25)
+    d = _write_inputs(tmp_path, dem, streams)
+    base = [_build.DRAINAGE, "--dem-path", str(d), "--seed", "9", "-i", "7"]
+    one = subprocess.run(base + ["-o", "one.bin"], cwd=tmp_path, capture_output=True)
+    four = subprocess.run(base + ["--batch", "4", "-o", "four.bin"], cwd=tmp_path,
+                          capture_output=True)
+    assert one.returncode == 0 and four.returncode == 0
+    a = api.read_raster(str(tmp_path / "one.bin"), dem.shape)
+    b = api.read_raster(str(tmp_path / "four.bin"), dem.shape)
+    assert np.array_equal(a, b) and a.max() > 0
+    bad = subprocess.run(base + ["--batch", "2", "--fill", "exact"], cwd=tmp_path,
+                         capture_output=True, text=True)
+    assert bad.returncode != 0 and "CPU-compatible" in bad.stderr
+
+
 def test_drainage_cli_checkpoint_resume(cuda, tmp_path):
     from cageo_gb300 import _build, api
     dem, streams = make_case(80, 64, seed=24)
