@@ -57,6 +57,14 @@ FLOOD_A_BYTES_PER_CELL = 8
 FLOOD_A_TRAFFIC_PER_CELL = 792.8e6 / (4096 * 4096)
 
 
+_T0 = time.time()
+
+
+def progress(what):
+    """One line on stderr per phase of the run, with the elapsed seconds."""
+    print("[bench %7.1f s] %s" % (time.time() - _T0, what), file=sys.stderr, flush=True)
+
+
 def peak_hbm():
     try:
         with open(PEAKS) as f:
@@ -337,6 +345,7 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
     dem, streams, p = workload(args.workload)
+    progress("workload %s ready" % args.workload)
     H, W = dem.shape
     N = H * W
     cfg = dict(cell_size=p["cell"], filter_model=api.FILTER_GAUSSIAN,
@@ -362,12 +371,14 @@ def main():
     # timed steps), then warm-up (graph capture) and the stage profile.
     # None of it is timed.
     tuned, tune_ms = pipe.autotune(base + 900_000, trials=3)
+    progress("autotuned: %s" % tuned)
     batch_ms = {}
     for b in args.batch_candidates:
         pipe.set_batch(b)
         pipe.run(base + 800_000, b)
         batch_ms[b] = timed(base + 800_000 + 100 * b, 3 * b) / (3 * b)
     batch = min(batch_ms, key=batch_ms.get)
+    progress("batch sizes timed: %s" % batch_ms)
     pipe.set_batch(batch)
     pipe.run(base, args.warmup * batch)
     prof = pipe.profile(base + args.warmup * batch, fill_parts=True)
@@ -375,6 +386,7 @@ def main():
     fill_parts_ms = {k: prof[k] for k in pipe.FILL_PARTS}
     stats = pipe.stats()
     pipe.reset_counts()
+    progress("warm-up and stage profile done")
 
     def barrier():
         if world > 1:
@@ -394,6 +406,7 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = world * args.steps * batch / (ms / 1000.0)
+    progress("timed region: %.1f ms" % ms)
     gpu_launches = args.steps * pipe.graph_kernels()
     # The same realizations one at a time (the plain pipeline), for the
     # batching gain; not part of the headline.
@@ -401,6 +414,7 @@ def main():
     pipe.run(base + 40_000, args.warmup)
     plain_ms = timed(base + 50_000, args.steps * batch)
     plain_value = world * args.steps * batch / (plain_ms / 1000.0)
+    progress("one at a time: %.1f ms" % plain_ms)
 
     # End to end through the C ABI from pinned host memory.
     dem_h = torch.from_numpy(dem).pin_memory()
@@ -425,6 +439,7 @@ def main():
         e2e_s = float(t.item())
     pe.close()
     e2e_value = world * args.steps * batch / e2e_s
+    progress("end to end: %.2f s" % e2e_s)
 
     if rank != 0:
         pipe.close()
@@ -484,8 +499,10 @@ def main():
         "note": "plain: the same number of realizations one at a time (batch 1), same pipeline"}
     if not args.no_exact:
         line["exact_mode"] = exact_mode(dem, streams, cfg, args.steps, args.warmup, base)
+        progress("exact mode done")
     if not args.no_batched:
         line["batched"] = batched()
+        progress("uneven-tile batch done")
     if not args.no_cpu_baseline:
         rate, threads, sec = cpu_rate(dem, streams, p, args.cpu_steps, 50_000)
         line["cpu_baseline"] = {"value": rate, "unit": "realizations/s", "cores": threads,
