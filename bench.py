@@ -379,6 +379,7 @@ def main():
         batch_ms[b] = timed(base + 800_000 + 100 * b, 3 * b) / (3 * b)
     batch = min(batch_ms, key=batch_ms.get)
     progress("batch sizes timed: %s" % batch_ms)
+    free_b, total_b = torch.cuda.mem_get_info()
     pipe.set_batch(batch)
     pipe.run(base, args.warmup * batch)
     prof = pipe.profile(base + args.warmup * batch, fill_parts=True)
@@ -492,6 +493,9 @@ def main():
     }
     # Kernel nodes of the captured batched-step graph, replayed once per step.
     line["gpu_launches"] = gpu_launches
+    # Device memory in use with the benchmark pipeline set up for its
+    # largest batch candidate (every allocation of the library included).
+    line["hbm_used_gb"] = round((total_b - free_b) / 1e9, 2)
     line["batch_steps"] = {
         "realizations_per_step": batch,
         "ms_per_realization": {str(b): round(v, 4) for b, v in batch_ms.items()},

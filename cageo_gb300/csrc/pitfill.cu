@@ -678,12 +678,15 @@ fill_flood_kernel(FloodArgs a) {
         if (w.aux[c] == c) w.cmin[c] = 0xffffffffu;
       }
       if (!grid_barrier(gs, nblocks)) break;
+      // Flags and levels were written by other SMs' drains, the minima by
+      // atomics: all are read from L2 (an L1 line could hold an older value
+      // across the grid barrier).
       unsigned int pend = 0;
       for (int64_t j = tid0; j < nu; j += tstride) {
         uint32_t c = w.cand[j];
-        uint8_t f = w.flags[c];
+        uint8_t f = __ldcg(w.flags + c);
         if ((f & FNONPASS) && !(f & (FCONF | FBELOW))) {
-          float wv = a.Wg[c];
+          float wv = __ldcg(a.Wg + c);
           if (wv < kInf) {
             atomicMin(&w.cmin[w.aux[c]], float_to_ordered(wv));
             pend = 1;
@@ -694,14 +697,21 @@ fill_flood_kernel(FloodArgs a) {
       if (lane == 0 && pend) atomicOr(&w.scal[S_PEND + ph % 3], 1u);
       if (!grid_barrier(gs, nblocks)) break;
       if (vs[S_PEND + ph % 3] == 0u) break;
+      // Each phase confirms at least one cell of every component with a
+      // pending cell (the one holding its minimum level), so there are at
+      // most as many phases as undecided cells.
+      if (ph > (int)min(nu, 0x7fffff00u) + 8) {
+        if (threadIdx.x == 0) atomicCAS((int*)(w.scal + S_ERR), 0, 2);
+        break;
+      }
       for (int64_t j = tid0; j < nu; j += tstride) {
         uint32_t c = w.cand[j];
-        uint8_t f = w.flags[c];
+        uint8_t f = __ldcg(w.flags + c);
         if (!(f & FNONPASS) || (f & (FCONF | FBELOW))) continue;
-        const unsigned int mo = w.cmin[w.aux[c]];
+        const unsigned int mo = __ldcg(w.cmin + w.aux[c]);
         if (mo == 0xffffffffu || !(a.q[c] <= ordered_to_float(mo))) continue;
         w.flags[c] = f | FCONF;
-        if (a.Wg[c] < kInf) {
+        if (__ldcg(a.Wg + c) < kInf) {
           // The cell now relays: every tile whose halo holds it must rerun.
           int cx = (int)(c % (uint32_t)w.W), cy = (int)(c / (uint32_t)w.W);
           w.tconv[(cy / kTile) * w.tiles_x + cx / kTile] = 0;  // its neighbours inside must rerun

@@ -190,21 +190,26 @@ __device__ void flat_tile(FlatSmem& s, const float* __restrict__ dem, int* fd, c
   const int tx = t % w.tiles_x, ty = t / w.tiles_x;
   const int x0 = tx * kFT, y0 = ty * kFT;
   const long long c0 = clock64();
-  // Stage the raw codes and elevations with asynchronous copies (all of the
-  // tile's loads in flight at once).
+  // Stage the raw codes and elevations.  The elevations never change: they
+  // come by asynchronous copies (all in flight at once).  The codes hold
+  // distances other SMs wrote in earlier passes: they are read from L2 (an
+  // L1 line could hold an older value across the grid barrier), in a loop
+  // of their own so that the copies' memory clobber does not keep each load
+  // from being issued before the previous iteration's copy.
   for (int idx = lane; idx < 34 * 34; idx += 32) {
     const int hy = idx / 34, hx = idx - hy * 34;
     const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
-    int* dr = &s.R[hy * kFRS + hx];
     float* de = &s.E[hy * kFRS + hx];
-    if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
-      const int64_t i = (int64_t)gy * W + gx;
-      cp_async4(dr, fd + i);
-      cp_async4(de, dem + i);
-    } else {
-      *dr = kOffGrid;
-      *de = 0.0f;
-    }
+    if (gx >= 0 && gx < W && gy >= 0 && gy < H) cp_async4(de, dem + (int64_t)gy * W + gx);
+    else *de = 0.0f;
+  }
+#pragma unroll 12
+  for (int idx = lane; idx < 34 * 34; idx += 32) {
+    const int hy = idx / 34, hx = idx - hy * 34;
+    const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
+    int code = kOffGrid;
+    if (gx >= 0 && gx < W && gy >= 0 && gy < H) code = __ldcg(fd + (int64_t)gy * W + gx);
+    s.R[hy * kFRS + hx] = code;
   }
   cp_async_wait();
   __syncwarp();
@@ -447,7 +452,8 @@ flat_relax_kernel(const float* __restrict__ dem, int* fd, RouteWork w, int gpu, 
         if (lane == 0) i = (int)atomicAdd(&w.scal[R_NEXT + p % 3], 1u);
         i = __shfl_sync(0xffffffffu, i, 0);
         if (i >= n) break;
-        flat_tile(s, dem, fd, w, list[i], p, lane, gpu != 0, nodata);
+        // The list was written by other SMs in the previous pass: from L2.
+        flat_tile(s, dem, fd, w, __ldcg(list + i), p, lane, gpu != 0, nodata);
       }
     }
     if (!grid_barrier(gs, gridDim.x)) break;
