@@ -44,7 +44,7 @@ namespace cageo {
 // Scalar block layout (unsigned ints).
 enum : int {
   S_MIN = 0,       // ordered min of q (minE)
-  S_ERR = 3,       // 0 ok, 1 barrier wait limit, 2 pass limit
+  S_ERR = 3,       // 0 ok; 1 barrier wait; 2 idle wait; 3 queue state; 4 visits; 5 phases; 6 union
   S_M = 7,         // 3 slots: ordered phase minima
   S_CAND = 10,     // number of undecided cells
   S_PASS = 11,     // drains run so far in this fill (a drain empties the work queue)
@@ -56,6 +56,7 @@ enum : int {
   S_US_P = 17,     // microseconds of the phase loop
   S_PEND = 18,     // 3 slots: pending cells seen by a phase
   S_RESET = 21,    // warm-started exact fill: cells restarted from +inf (unsupported)
+  S_DBG = 24,      // 8 slots: the phase loop's state when it passed its limit (see below)
   // Per-visit statistics, updated by every tile visit: a line of their own
   // (96..127), away from the error flag that idle warps poll.
   S_TILES_A = 96,   // tiles processed by flood A
@@ -354,6 +355,18 @@ __device__ bool process_tile(WarpSmem<MODE>& s, const FloodArgs& a, int t, int l
   const int tx = t % w.tiles_x, ty = t / w.tiles_x;
   const int x0 = tx * kTile, y0 = ty * kTile;
   const long long c0 = clock64();
+  if constexpr (MODE != 1) {
+    // Flood A needs q only for the tile's own cells (an outlet's W is its q,
+    // which is all its relay needs), and q never changes: asynchronous
+    // copies, all in flight while the loop below loads W and the flags.
+    for (int idx = lane; idx < kTile * kTile; idx += 32) {
+      const int ty_ = idx >> 5, tx_ = idx & 31;
+      const int gx = x0 + tx_, gy = y0 + ty_;
+      float* dq = &s.Q[ty_ * kWS + tx_];
+      if (gx < W && gy < H) cp_async4(dq, a.q + (int64_t)gy * W + gx);
+      else *dq = 0.0f;
+    }
+  }
 #pragma unroll 12
   for (int idx = lane; idx < 34 * 34; idx += 32) {
     int hy = idx / 34, hx = idx - hy * 34;
@@ -363,16 +376,16 @@ __device__ bool process_tile(WarpSmem<MODE>& s, const FloodArgs& a, int t, int l
     if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
       int64_t i = (int64_t)gy * W + gx;
       wv = __ldcg(a.Wg + i);  // L2: written by other SMs with no barrier in between
-      qv = a.q[i];
+      if constexpr (MODE == 1) qv = a.q[i];
       fv = __ldcg(w.flags + i);
     }
-    s.R[hy * kRS + hx] = relay<MODE>(wv, fv, qv);
+    s.R[hy * kRS + hx] = relay<MODE>(wv, fv, MODE == 1 ? qv : wv);
     if (hx >= 1 && hx <= kTile && hy >= 1 && hy <= kTile) {
       if constexpr (MODE == 1) s.WQ[(hy - 1) * kWS + hx - 1] = make_float2(wv, qv);
-      else s.Q[(hy - 1) * kWS + hx - 1] = qv;
       s.F[(hy - 1) * kFS + hx - 1] = fv;
     }
   }
+  if constexpr (MODE != 1) cp_async_wait();
   if constexpr (MODE == 2) {
     // Clean relays of the halo: strips of 34 cells (row above, row below,
     // column left, column right), flags read again from L2.  A loop of its
@@ -553,6 +566,20 @@ __device__ __forceinline__ uint32_t uf_find(uint32_t* lab, uint32_t x) {
   return x;
 }
 
+// The root without path halving: the flattening pass writes each cell's
+// root while other threads walk the same paths, and a halving store that
+// landed after such a write would replace the root by an ancestor below
+// it -- leaving a cell labelled with a non-root, outside its component's
+// minimum.  Plain reads only, so every store of that pass is a root.
+__device__ __forceinline__ uint32_t uf_root(const uint32_t* lab, uint32_t x) {
+  for (int it = 0; it < (1 << 20); it++) {
+    const uint32_t p = ((const volatile uint32_t*)lab)[x];
+    if (p == x) return x;
+    x = p;
+  }
+  return x;
+}
+
 __device__ __forceinline__ bool uf_unite(uint32_t* lab, uint32_t a, uint32_t b) {
   for (int it = 0; it < (1 << 16); it++) {
     uint32_t ra = uf_find(lab, a), rb = uf_find(lab, b);
@@ -600,9 +627,9 @@ __device__ bool drain(WarpSmem<MODE>& s, const FloodArgs& a, int lane, int ntile
       break;
     }
     if (vs[S_PENDING] == 0u) break;
-    if (++idle > (1LL << 24) ||
-        vs[(MODE == 1 || a.stage == 3) ? S_TILES_B : S_TILES_A] > visit_cap) {
-      if (lane == 0) atomicCAS((int*)(w.scal + S_ERR), 0, 2);
+    const bool idle_limit = ++idle > (1LL << 24);
+    if (idle_limit || vs[(MODE == 1 || a.stage == 3) ? S_TILES_B : S_TILES_A] > visit_cap) {
+      if (lane == 0) atomicCAS((int*)(w.scal + S_ERR), 0, idle_limit ? 2 : 4);
       ok = false;
       break;
     }
@@ -674,14 +701,17 @@ fill_flood_kernel(FloodArgs a) {
       const unsigned int nu = vs[S_CAND];
       if (blockIdx.x == 0 && threadIdx.x == 0) vs[S_PEND + (ph + 1) % 3] = 0u;
       for (int64_t j = tid0; j < nu; j += tstride) {
-        uint32_t c = w.cand[j];
-        if (w.aux[c] == c) w.cmin[c] = 0xffffffffu;
+        const uint32_t c = w.cand[j], r = w.aux[c];
+        if (r == c) w.cmin[c] = 0xffffffffu;
+        // Every label is a root: a cell labelled otherwise would take a
+        // minimum nothing resets.
+        if (ph == 0 && w.aux[r] != r) atomicCAS((int*)(w.scal + S_ERR), 0, 6);
       }
       if (!grid_barrier(gs, nblocks)) break;
       // Flags and levels were written by other SMs' drains, the minima by
       // atomics: all are read from L2 (an L1 line could hold an older value
       // across the grid barrier).
-      unsigned int pend = 0;
+      unsigned int pend = 0, npend = 0;
       for (int64_t j = tid0; j < nu; j += tstride) {
         uint32_t c = w.cand[j];
         uint8_t f = __ldcg(w.flags + c);
@@ -690,9 +720,12 @@ fill_flood_kernel(FloodArgs a) {
           if (wv < kInf) {
             atomicMin(&w.cmin[w.aux[c]], float_to_ordered(wv));
             pend = 1;
+            npend++;
           }
         }
       }
+      npend = __reduce_add_sync(0xffffffffu, npend);
+      if (lane == 0 && npend) atomicAdd(&w.scal[S_DBG], npend);
       pend = __reduce_or_sync(0xffffffffu, pend);
       if (lane == 0 && pend) atomicOr(&w.scal[S_PEND + ph % 3], 1u);
       if (!grid_barrier(gs, nblocks)) break;
@@ -701,15 +734,39 @@ fill_flood_kernel(FloodArgs a) {
       // pending cell (the one holding its minimum level), so there are at
       // most as many phases as undecided cells.
       if (ph > (int)min(nu, 0x7fffff00u) + 8) {
-        if (threadIdx.x == 0) atomicCAS((int*)(w.scal + S_ERR), 0, 2);
+        // Record one pending cell whose level is its component's recorded
+        // minimum: [26] cell, [27] level, [28] q, [29] the minimum read
+        // back, [30] its label, [31] the label's own label ([24] pending
+        // cells counted over the phases, [25] confirmations of the last).
+        for (int64_t j = tid0; j < nu; j += tstride) {
+          const uint32_t c = w.cand[j];
+          const uint8_t f = __ldcg(w.flags + c);
+          if (!(f & FNONPASS) || (f & (FCONF | FBELOW))) continue;
+          const float wv = __ldcg(a.Wg + c);
+          const uint32_t r = w.aux[c];
+          const unsigned int mo = __ldcg(w.cmin + r);
+          if (wv < kInf && float_to_ordered(wv) == mo &&
+              atomicCAS(&w.scal[S_DBG + 2], 0u, c + 1u) == 0u) {
+            w.scal[S_DBG + 3] = __float_as_uint(wv);
+            w.scal[S_DBG + 4] = __float_as_uint(a.q[c]);
+            w.scal[S_DBG + 5] = mo;
+            w.scal[S_DBG + 6] = r;
+            w.scal[S_DBG + 7] = w.aux[r];
+          }
+        }
+        if (threadIdx.x == 0) atomicCAS((int*)(w.scal + S_ERR), 0, 5);
         break;
       }
+      if (blockIdx.x == 0 && threadIdx.x == 0) w.scal[S_DBG + 1] = 0u;
+      if (!grid_barrier(gs, nblocks)) break;
+      unsigned int nconf = 0;
       for (int64_t j = tid0; j < nu; j += tstride) {
         uint32_t c = w.cand[j];
         uint8_t f = __ldcg(w.flags + c);
         if (!(f & FNONPASS) || (f & (FCONF | FBELOW))) continue;
         const unsigned int mo = __ldcg(w.cmin + w.aux[c]);
         if (mo == 0xffffffffu || !(a.q[c] <= ordered_to_float(mo))) continue;
+        nconf++;
         w.flags[c] = f | FCONF;
         if (__ldcg(a.Wg + c) < kInf) {
           // The cell now relays: every tile whose halo holds it must rerun.
@@ -721,6 +778,8 @@ fill_flood_kernel(FloodArgs a) {
             for (int tx = tx0; tx <= tx1; tx++) enqueue(w, ty * w.tiles_x + tx);
         }
       }
+      nconf = __reduce_add_sync(0xffffffffu, nconf);
+      if (lane == 0 && nconf) atomicAdd(&w.scal[S_DBG + 1], nconf);
       ph++;
       if (!grid_barrier(gs, nblocks)) break;
     }
@@ -979,7 +1038,7 @@ __global__ void fill_unite_kernel(const uint32_t* __restrict__ cand, unsigned in
       if (F[nb] & FUNSURE) ok &= uf_unite(aux, c, nb);
     }
   }
-  if (!ok) atomicCAS((int*)(scal + S_ERR), 0, 2);
+  if (!ok) atomicCAS((int*)(scal + S_ERR), 0, 6);
 }
 
 // Every undecided cell's label becomes its component's root.
@@ -989,7 +1048,7 @@ __global__ void fill_flatten_kernel(const uint32_t* __restrict__ cand,
   for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nu;
        j += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t c = cand[j];
-    aux[c] = uf_find(aux, c);
+    aux[c] = uf_root(aux, c);
   }
 }
 
@@ -1233,9 +1292,24 @@ cageo_status fill_check_status(const FillWork& w, int64_t* stats) {
     stats[16] = h[S_RESET];
   }
   if (h[S_ERR]) {
-    set_error(h[S_ERR] == 1   ? "pit filling: a grid-wide wait hit its limit"
-              : h[S_ERR] == 2 ? "pit filling: pass or loop limit reached without convergence"
-                              : "pit filling: internal worklist overflow");
+    static const char* what[] = {"",
+                                 "a grid-wide wait hit its limit",
+                                 "a warp waited for a tile past its limit",
+                                 "a tile's queue state kept changing",
+                                 "the tile visits passed their limit",
+                                 "the confirmation phases passed their limit",
+                                 "the labels of the undecided cells are not settled roots"};
+    const unsigned int e = h[S_ERR];
+    if (e == 5)
+      set_error("pit filling: %s (phases %u, undecided cells %u; pending counted %u, confirmed "
+                "in the last phase %u; a minimum cell %u: level %.9g, q %.9g, minimum read %.9g, "
+                "label %u, its label %u)",
+                what[e], h[S_PHASES], h[S_CAND], h[S_DBG], h[S_DBG + 1], h[S_DBG + 2] - 1,
+                __builtin_bit_cast(float, h[S_DBG + 3]), __builtin_bit_cast(float, h[S_DBG + 4]),
+                ordered_to_float(h[S_DBG + 5]), h[S_DBG + 6], h[S_DBG + 7]);
+    else
+      set_error("pit filling: %s (pending tiles %u, phases %u, undecided cells %u)",
+                e < 7 ? what[e] : "unknown error", h[S_PENDING], h[S_PHASES], h[S_CAND]);
     return CAGEO_ERR_NO_CONVERGENCE;
   }
   return CAGEO_OK;

@@ -1,8 +1,8 @@
-// tilequeue.cuh -- the asynchronous tile work queue of the pit fill's
-// persistent flood kernels.
+// tilequeue.cuh -- the asynchronous tile work queue of the persistent
+// relaxation kernels (the pit fill's floods and the flat-surface BFS).
 //
 // Tiles are processed as soon as they are queued, by whichever warp is free:
-// no grid-wide pass barriers.  The floods are monotone relaxations (values
+// no grid-wide pass barriers.  Both users run monotone relaxations (values
 // only fall), so the order of the updates does not change their limit; what
 // must not happen is two warps processing one tile at once (a slower warp's
 // write-back could undo a faster one's lower values).  Each tile therefore
