@@ -48,13 +48,13 @@ FALLBACK_HBM = 6800.0
 STAGE_BYTES = {"noise": 4, "front": 40, "fill": 8, "route": 5, "trace": 6, "border": 12}
 PIPE_BYTES = 75
 # The dominant kernel is the pit fill's lower-bound flood (fill_flood_kernel
-# with clean marks, 34% of a realization).  Its algorithmic bytes are those
+# with clean marks, 35% of a realization).  Its algorithmic bytes are those
 # of one fill pass: read q (4 B) and write the filled value (4 B) per cell.
 # Its DRAM bytes per launch come from an ncu capture of the 4096^2 workload
 # (dram__bytes_read.sum + dram__bytes_write.sum of that launch divided by
 # its 16.8 M cells), applied per cell to the benchmark grid.
 FLOOD_A_BYTES_PER_CELL = 8
-FLOOD_A_TRAFFIC_PER_CELL = 792.8e6 / (4096 * 4096)
+FLOOD_A_TRAFFIC_PER_CELL = 614.9e6 / (4096 * 4096)
 
 
 _T0 = time.time()
