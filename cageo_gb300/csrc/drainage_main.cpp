@@ -11,7 +11,8 @@
 //
 // Outputs: .bin = raw float32 counts; .jpg (the reference's default type) =
 // the counts scaled to bytes as (uint8)rintf(255*((v-min)/max)) and written
-// as a baseline grayscale JPEG of quality 85.
+// as the reference's jpge encoder writes them with its default parameters
+// (quality 85; the same file bytes).
 //
 // Additive options: --seed N (default: the current time, like the
 // reference's time(NULL)+iteration seeding), --bevel-radius N (2; the

@@ -452,8 +452,10 @@ typedef struct {
  * whose max is 0 gives 0 everywhere. */
 cageo_status cageo_to_bytes(const float* d_in, uint8_t* d_out, int W, int H,
                             cudaStream_t stream);
-/* Baseline grayscale JFIF writer (quality 1..100; the reference uses jpge's
- * default 85, src/main.cpp:265-270).  Host only. */
+/* JPEG file of a byte image, byte-identical to what the reference's jpge
+ * encoder writes for it with its default parameters and the given quality
+ * (src/main.cpp:265-270 passes jpge::params(): quality 85, YCbCr H2V2 with
+ * neutral chroma, standard tables).  Quality 1..100.  Host only. */
 cageo_status cageo_write_jpeg(const char* path, const uint8_t* h_gray, int W, int H,
                               int quality);
 cageo_status cageo_read_header(const char* path, cageo_raster_info* info);

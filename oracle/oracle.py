@@ -211,6 +211,26 @@ class Reference(_Base):
     prefix = "ref_"
     path = os.path.join(HERE, "_ref", "libref.so")
 
+    def to_bytes(self, mc):
+        """The driver's JPEG byte image of a count grid (reference CPU code)."""
+        m = np.ascontiguousarray(mc, np.float32)
+        H, W = m.shape
+        out = np.empty((H, W), np.uint8)
+        self.lib.ref_to_bytes(_p(m, _f32p), out.ctypes.data_as(ctypes.c_void_p), W, H)
+        return out
+
+    def jpeg(self, img, path, quality=0):
+        """The reference's JPEG file of a byte image (the jpge encoder with
+        its default parameters, one channel; quality 0 keeps the default
+        85); returns the file's bytes."""
+        g = np.ascontiguousarray(img, np.uint8)
+        H, W = g.shape
+        if self.lib.ref_write_jpeg(os.fsencode(path), g.ctypes.data_as(ctypes.c_void_p), W, H,
+                                   quality):
+            raise IOError("jpge could not write " + str(path))
+        with open(path, "rb") as f:
+            return f.read()
+
     def convolve(self, field, filt, r, model):
         x = np.ascontiguousarray(field, np.float32)
         H, W = x.shape

@@ -33,6 +33,9 @@
 #include "FlowDirClass.h"
 #include "FlowTraceDataClass.h"
 #include "CatchmentBorderClass.h"
+#include "ToByteArrayAlgorithm.h"
+#include "ToByteArrayAlgorithmCPUOpenMP.h"
+#include "jpge.h"
 
 namespace {
 
@@ -185,6 +188,26 @@ void ref_border_accumulate(const int* label, float* mc, int W, int H) {
   ZeroedBorder alg;
   alg.execute(&m, &t);
   std::memcpy(mc, m.getData(), sizeof(float) * (size_t)W * H);
+}
+
+// The JPEG output: the count grid as bytes (ToByteArrayAlgorithm on the
+// CPU, src/utils/tobytearray/ToByteArrayAlgorithmCPUOpenMP.h:33-52), then
+// the jpge encoder on one channel with its default parameters, as the
+// driver calls both (src/main.cpp:258-271); `quality` replaces the
+// default 85 when it is not 0.
+void ref_to_bytes(const float* mc, uint8_t* out, int W, int H) {
+  CellGrid<float> m(W, H, HOST);
+  load(m, mc, sizeof(float) * (size_t)W * H);
+  CellGrid<Byte_t> bytes(m, AS_TEMPLATE);
+  ToByteArrayAlgorithm_CPU_OpenMP<float> alg;
+  alg.execute(&bytes, &m);
+  std::memcpy(out, bytes.getData(), (size_t)W * H);
+}
+
+int ref_write_jpeg(const char* path, const uint8_t* img, int W, int H, int quality) {
+  jpge::params p;
+  if (quality) p.m_quality = quality;
+  return jpge::compress_image_to_jpeg_file(path, W, H, 1, (const jpge::uint8*)img, p) ? 0 : 1;
 }
 
 }  // extern "C"

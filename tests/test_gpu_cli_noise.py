@@ -117,6 +117,20 @@ def test_to_bytes_matches_reference_formula(cuda):
     assert np.all(zero == 0)
 
 
+def test_to_bytes_matches_reference_fixture(cuda):
+    """The reference's own byte images (ToByteArrayAlgorithm on the CPU,
+    tests/golden/jpeg/cases.npz), rounding ties included."""
+    import os
+    import torch
+    from cageo_gb300 import api
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "jpeg", "cases.npz"))
+    n = sum(1 for k in g.files if k.startswith("counts_"))
+    assert n >= 4
+    for i in range(n):
+        got = api.to_bytes(torch.from_numpy(g["counts_%d" % i]).to(cuda)).cpu().numpy()
+        assert np.array_equal(got, g["bytes_%d" % i]), str(g["cname_%d" % i])
+
+
 def test_drainage_cli_jpeg(cuda, tmp_path):
     import torch
     from cageo_gb300 import _build, api
@@ -128,6 +142,10 @@ def test_drainage_cli_jpeg(cuda, tmp_path):
     assert subprocess.run(base + ["-o", "c.jpg"], cwd=tmp_path, capture_output=True).returncode == 0
     counts = api.read_raster(str(tmp_path / "c.bin"), dem.shape)
     img = api.to_bytes(torch.from_numpy(counts).to(cuda)).cpu().numpy()
+    # The CLI's file is the writer's file of the byte image (the writer's
+    # bytes are pinned to the reference encoder by the CPU tests).
+    api.write_jpeg(str(tmp_path / "w.jpg"), img)
+    assert (tmp_path / "c.jpg").read_bytes() == (tmp_path / "w.jpg").read_bytes()
     back = decode(str(tmp_path / "c.jpg"))
     assert back.shape == img.shape
     assert np.mean(np.abs(back.astype(int) - img.astype(int))) < 12
