@@ -322,7 +322,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-exact", action="store_true", help="skip the exact-mode measurement")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched measurement")
-    ap.add_argument("--batch-candidates", default="1,4,8",
+    ap.add_argument("--batch-candidates", default="1,4,8,16",
                     help="realizations per batched step to choose from (by timing)")
     ap.add_argument("--workload", default="eval-8192",
                     help="eval-8192 (the benchmark) or a smaller case for profiling (plain-4096)")
