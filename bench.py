@@ -424,7 +424,7 @@ def main():
     barrier()
     t0 = time.perf_counter()
     pe = api.Pipeline(dem_h.numpy(), st_h.numpy(), **cfg)
-    pe.set_tuning(tuned["fill_rounds"], tuned["fill_warps"])
+    pe.set_tuning(tuned["fill_rounds"], tuned["fill_warps"], tuned["conv_tile"])
     pe.set_batch(batch)
     pe.run(base + 20_000, args.steps * batch)
     pe.counts(out=counts_h)

@@ -45,10 +45,17 @@ class PipelineConfig(ctypes.Structure):
 
 
 class Tuning(ctypes.Structure):
-    _fields_ = [("fill_rounds", ctypes.c_int), ("fill_warps", ctypes.c_int)]
+    _fields_ = [("fill_rounds", ctypes.c_int), ("fill_warps", ctypes.c_int),
+                ("conv_tile", ctypes.c_int)]
 
     def as_dict(self):
-        return {"fill_rounds": self.fill_rounds, "fill_warps": self.fill_warps}
+        return {"fill_rounds": self.fill_rounds, "fill_warps": self.fill_warps,
+                "conv_tile": self.conv_tile}
+
+
+# Output tile (columns, rows) of the fused front's separable convolution per
+# cageo_tuning.conv_tile value.
+CONV_TILES = ((64, 32), (128, 32), (64, 64), (96, 32))
 
 
 def autotune_candidates():
@@ -451,9 +458,11 @@ class Pipeline:
     STAGES = ("noise", "front", "fill", "route", "trace", "border")
 
     def autotune(self, first, trials=3):
-        """Pick the fill's tuning (sweep rounds per tile visit, warps per SM
-        of the lower-bound flood) by timing every candidate; resets the
-        counts.  Returns (chosen tuning, [(candidate, ms per realization)])."""
+        """Pick the tuning (the fill's sweep rounds per tile visit and warps
+        per SM of its lower-bound flood, then the front's convolution tile)
+        by timing every candidate; resets the counts.  Returns (chosen
+        tuning, [(candidate, ms per realization)]); a convolution tile that
+        does not apply has 0 ms."""
         cands = autotune_candidates()
         best = Tuning()
         ms = np.zeros(len(cands), np.float32)
@@ -461,9 +470,12 @@ class Pipeline:
                                              ms.ctypes.data_as(_vp), len(cands)))
         return best.as_dict(), [(c, float(v)) for c, v in zip(cands, ms)]
 
-    def set_tuning(self, fill_rounds, fill_warps):
-        _check(lib().cageo_pipeline_set_tuning(self._p, ctypes.byref(Tuning(fill_rounds,
-                                                                            fill_warps))))
+    def set_tuning(self, fill_rounds, fill_warps, conv_tile=None):
+        """Set the tuning; conv_tile None keeps the current tile."""
+        if conv_tile is None:
+            conv_tile = self.tuning()["conv_tile"]
+        _check(lib().cageo_pipeline_set_tuning(
+            self._p, ctypes.byref(Tuning(fill_rounds, fill_warps, conv_tile))))
 
     def tuning(self):
         t = Tuning()

@@ -19,6 +19,11 @@ constexpr uint8_t kCodeTraceStream = 0x40;
 constexpr uint8_t kCodeBurnStream = 0x80;
 constexpr int kMaxBurnClasses = 31;
 
+// Tile shapes of the fused front's separable convolution (output columns x
+// rows per block), chosen per pipeline by its autotuner; the outputs never
+// depend on the shape.
+constexpr int kConvTiles = 4;
+
 struct FrontParams {
   const float* dem;        // W*H
   const uint8_t* code;     // W*H static codes

@@ -6,6 +6,7 @@
 // add), so they equal ConvolutionAlgorithm_CPU_OpenMP bit for bit.  The
 // same kernels, instantiated with the FrontEpilogue, fuse the realistic-DEM,
 // burning and quantization steps of a realization into their store.
+#include <type_traits>
 #include "common.cuh"
 #include "front.cuh"
 #include "stage_math.cuh"
@@ -53,7 +54,18 @@ __global__ void noise_kernel(float* __restrict__ out, int64_t n, uint32_t k0,
 }
 
 // ---- A3 separable (Gaussian) ----------------------------------------------
-constexpr int kSepTW = 64, kSepTH = 32, kSepThreads = 256;
+// Output tile of a block (columns x rows), 256 threads.  A wider or taller
+// tile stages less halo per output but leaves fewer blocks per SM, and the
+// column pass (items of 8 rows x 2 columns over the tile's width plus the
+// halo) and the row pass (8 outputs per item) fill the 256 threads
+// differently for each shape and radius: at radius 15, 64 x 32 gives the
+// column pass 188 items, 96 x 32 gives it 252.  The cageo_convolve stage
+// uses the first shape; the fused front takes the pipeline's choice.
+struct SepTile {
+  int tw, th;
+};
+constexpr SepTile kSepTiles[kConvTiles] = {{64, 32}, {128, 32}, {64, 64}, {96, 32}};
+constexpr int kSepThreads = 256;
 
 // Periodic index: one period either way by compare-and-add (every index a
 // valid output reads is within one period, since r < W and r < H); the
@@ -240,17 +252,18 @@ __device__ __forceinline__ void conv_line8x2(const float* __restrict__ v0,
   }
 }
 
-template <class Epi, int LC>
+template <class Epi, int LC, int TW, int TH>
 __global__ void __launch_bounds__(kSepThreads)
 conv_sep_kernel(const float* __restrict__ in, int W, int H,
                 const float* __restrict__ taps, int r, Epi epi) {
+  static_assert(TW % 8 == 0 && TH % 8 == 0, "items are 8 outputs wide / 8 rows tall");
   extern __shared__ float sm[];
   const int L = 2 * r + 1;
-  const int IW = kSepTW + 2 * r, IH = kSepTH + 2 * r;
+  const int IW = TW + 2 * r, IH = TH + 2 * r;
   float* s_taps = sm;
   float* s_in = sm + ((L + 3) & ~3);
   float* s_tmp = s_in + IW * IH;
-  const int x0 = blockIdx.x * kSepTW, y0 = blockIdx.y * kSepTH;
+  const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
   for (int t = threadIdx.x; t < L; t += blockDim.x) s_taps[t] = taps[t];
   {
     // Row and column of this thread's element, stepped by blockDim.x.
@@ -273,7 +286,7 @@ conv_sep_kernel(const float* __restrict__ in, int W, int H,
   // Column pass: tmp[y][ix] = sum_t in[y+t][ix] * taps[t]; an item is 8
   // rows of two adjacent columns (IW is even).
   const int IW2 = IW / 2;
-  for (int item = threadIdx.x; item < IW2 * (kSepTH / 8); item += blockDim.x) {
+  for (int item = threadIdx.x; item < IW2 * (TH / 8); item += blockDim.x) {
     const int g = item / IW2, ix = 2 * (item - g * IW2);
     float a0[8], a1[8];
     conv_line8x2<LC, true>(s_in + (8 * g) * IW + ix, nullptr, IW, s_taps, L, a0, a1);
@@ -284,8 +297,8 @@ conv_sep_kernel(const float* __restrict__ in, int W, int H,
   __syncthreads();
   // Row pass (8 consecutive outputs per item) and store.
   float local_min = kInf;
-  for (int item = threadIdx.x; item < kSepTH * (kSepTW / 8); item += blockDim.x) {
-    const int y = item / (kSepTW / 8), g = item - y * (kSepTW / 8);
+  for (int item = threadIdx.x; item < TH * (TW / 8); item += blockDim.x) {
+    const int y = item / (TW / 8), g = item - y * (TW / 8);
     const int gy = y0 + y;
     typename Epi::Pre pre[8];
 #pragma unroll
@@ -379,20 +392,58 @@ conv_2d_kernel(const float* __restrict__ in, int W, int H,
   block_min_out(local_min, epi);
 }
 
-size_t conv_smem_bytes(int model, int r) {
+size_t conv_smem_bytes(int model, int r, int tile) {
   int L = 2 * r + 1;
   if (model == CAGEO_FILTER_GAUSSIAN) {
-    int IW = kSepTW + 2 * r, IH = kSepTH + 2 * r;
-    return sizeof(float) * (((L + 3) & ~3) + (size_t)IW * IH + (size_t)IW * kSepTH);
+    const SepTile t = kSepTiles[tile];
+    int IW = t.tw + 2 * r, IH = t.th + 2 * r;
+    return sizeof(float) * (((L + 3) & ~3) + (size_t)IW * IH + (size_t)IW * t.th);
   }
   int IW = kTwoDTW + 2 * r, IH = kTwoDTH + 2 * r;
   return sizeof(float) * (((L * L + 3) & ~3) + (size_t)IW * IH);
 }
 
+// Whether a tile shape of the fused front applies: Gaussian filters (the
+// separable kernel) whose staged block fits the device's shared memory.
+bool conv_tile_applies(int model, int r, int tile) {
+  if (model != CAGEO_FILTER_GAUSSIAN || tile < 0 || tile >= kConvTiles) return tile == 0;
+  int optin = 0, dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+    return tile == 0;
+  // The kernels' own static shared memory (the block minimum) is small.
+  return conv_smem_bytes(model, r, tile) + 1024 <= (size_t)optin;
+}
+
+// The separable kernel for a tile shape and radius: fully unrolled for the
+// 60 m and 90 m ranges at 10 m cells (radius 15 and 23).
+template <class Epi>
+using SepKernel = void (*)(const float*, int, int, const float*, int, Epi);
+
+template <class Epi, int TW, int TH>
+SepKernel<Epi> sep_kernel_for(int r) {
+  return r == 15 ? conv_sep_kernel<Epi, 31, TW, TH>
+                 : r == 23 ? conv_sep_kernel<Epi, 47, TW, TH> : conv_sep_kernel<Epi, 0, TW, TH>;
+}
+
+template <class Epi>
+SepKernel<Epi> sep_kernel(int r, int tile) {
+  if constexpr (std::is_same<Epi, FrontEpilogue>::value) {
+    switch (tile) {
+      case 1: return sep_kernel_for<Epi, kSepTiles[1].tw, kSepTiles[1].th>(r);
+      case 2: return sep_kernel_for<Epi, kSepTiles[2].tw, kSepTiles[2].th>(r);
+      case 3: return sep_kernel_for<Epi, kSepTiles[3].tw, kSepTiles[3].th>(r);
+      default: break;
+    }
+  }
+  return sep_kernel_for<Epi, kSepTiles[0].tw, kSepTiles[0].th>(r);
+}
+
 template <class Epi>
 cageo_status launch_conv(const float* in, int W, int H, int model,
                          const float* filt, int r, const Epi& epi,
-                         cudaStream_t s) {
+                         cudaStream_t s, int tile = 0) {
+  if (!std::is_same<Epi, FrontEpilogue>::value || tile < 0 || tile >= kConvTiles) tile = 0;
   // The kernels' dynamic shared-memory limit is raised to the most the
   // device allows (its opt-in maximum less the kernel's static shared
   // memory), the same value on every call: pipelines on other host threads
@@ -409,11 +460,9 @@ cageo_status launch_conv(const float* in, int W, int H, int model,
     CAGEO_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, *limit));
     return CAGEO_OK;
   };
-  const size_t smem = conv_smem_bytes(model, r);
+  const size_t smem = conv_smem_bytes(model, r, tile);
   if (model == CAGEO_FILTER_GAUSSIAN) {
-    // Fully unrolled kernels for the 60 m and 90 m ranges at 10 m cells.
-    auto fn = r == 15 ? conv_sep_kernel<Epi, 31> : r == 23 ? conv_sep_kernel<Epi, 47>
-                                                            : conv_sep_kernel<Epi, 0>;
+    const SepKernel<Epi> fn = sep_kernel<Epi>(r, tile);
     int limit = 0;
     cageo_status st = raise_limit((const void*)fn, &limit);
     if (st) return st;
@@ -421,7 +470,8 @@ cageo_status launch_conv(const float* in, int W, int H, int model,
       set_error("filter radius %d needs %zu bytes of shared memory (%d available)", r, smem, limit);
       return CAGEO_ERR_ARGUMENT;
     }
-    dim3 grid((W + kSepTW - 1) / kSepTW, (H + kSepTH - 1) / kSepTH);
+    const SepTile t = kSepTiles[tile];
+    dim3 grid((W + t.tw - 1) / t.tw, (H + t.th - 1) / t.th);
     fn<<<grid, kSepThreads, smem, s>>>(in, W, H, filt, r, epi);
   } else {
     int limit = 0;
@@ -452,9 +502,9 @@ cageo_status launch_noise(float* d, int64_t n, uint64_t seed, uint32_t realizati
 
 cageo_status launch_front(const float* noise, int W, int H, int model,
                           const float* filt, int r, const FrontParams& fp,
-                          cudaStream_t s) {
+                          cudaStream_t s, int tile) {
   FrontEpilogue e{fp};
-  return launch_conv(noise, W, H, model, filt, r, e, s);
+  return launch_conv(noise, W, H, model, filt, r, e, s, tile);
 }
 
 }  // namespace cageo

@@ -34,7 +34,8 @@ namespace cageo {
 cageo_status launch_noise(float* d, int64_t n, uint64_t seed, uint32_t realization,
                           const uint32_t* dreal, float mean, float sd, cudaStream_t s);
 cageo_status launch_front(const float* noise, int W, int H, int model, const float* filt,
-                          int r, const FrontParams& fp, cudaStream_t s);
+                          int r, const FrontParams& fp, cudaStream_t s, int tile);
+bool conv_tile_applies(int model, int r, int tile);
 cageo_status launch_burn_code(const float* streams, uint8_t* code, int W, int H,
                               float nodata_stream, int bevel, float* factor_out,
                               cudaStream_t s);
@@ -129,6 +130,7 @@ struct cageo_pipeline {
   // fill over a stack of their q grids (qb, filledb: batch * N floats, fill
   // workspace fwb for W x batch*H), each slab's minimum of q in slab_min.
   int batch = 1;
+  int conv_tile = 0;  // the fused front's convolution tile shape (kConvTiles)
   float *qb = nullptr, *filledb = nullptr;
   void* fill_ws_b = nullptr;
   unsigned int* slab_min = nullptr;
@@ -229,7 +231,8 @@ cageo_status enqueue_fast(cageo_pipeline* p) {
   if (p->fw.front_init && (st = fill_clear_seeds(p->fw, s))) return st;
   if ((st = launch_noise(p->noise, p->N, c.seed, 0, p->dscal, c.error_mean, c.error_stddev, s)))
     return st;
-  if ((st = launch_front(p->noise, p->W, p->H, c.filter_model, p->filter, p->radius, p->fp, s)))
+  if ((st = launch_front(p->noise, p->W, p->H, c.filter_model, p->filter, p->radius, p->fp, s,
+                         p->conv_tile)))
     return st;
   if ((st = enqueue_fill(p))) return st;
   if ((st = enqueue_route(p))) return st;
@@ -267,7 +270,8 @@ cageo_status enqueue_batch(cageo_pipeline* p) {
     fp.tseed = p->fwb.tseed;
     fp.tiles_x = p->fwb.tiles_x;
     fp.row0 = k * p->H;
-    if ((st = launch_front(p->noise, p->W, p->H, c.filter_model, p->filter, p->radius, fp, s)))
+    if ((st = launch_front(p->noise, p->W, p->H, c.filter_model, p->filter, p->radius, fp, s,
+                           p->conv_tile)))
       return st;
   }
   if ((st = fill_run(p->qb, p->filledb, p->fwb, c.nodata_dem, s))) return st;
@@ -587,7 +591,8 @@ extern "C" cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t reali
     if ((st = launch_noise(p->noise, p->N, c.seed, 0, p->dscal, c.error_mean, c.error_stddev, s)))
       break;
     cudaEventRecord(ev[1], s);
-    if ((st = launch_front(p->noise, p->W, p->H, c.filter_model, p->filter, p->radius, p->fp, s)))
+    if ((st = launch_front(p->noise, p->W, p->H, c.filter_model, p->filter, p->radius, p->fp, s,
+                           p->conv_tile)))
       break;
     cudaEventRecord(ev[2], s);
     if (!exact_mode(p)) p->fw.marks = fm;
@@ -872,15 +877,22 @@ extern "C" cageo_status cageo_pipeline_reset_counts(cageo_pipeline* p) {
 }
 
 // Candidate settings of the autotuner: sweep rounds per fill tile visit x
-// warps per SM of the fill's lower-bound flood.
+// warps per SM of the fill's lower-bound flood (with the first convolution
+// tile), then the other convolution tiles with the fill setting chosen
+// among those (fill fields 0).  The front and the fill are separate stages,
+// so tuning them one after the other finds the best of the product.
 static const int kTuneRounds[3] = {16, 32, 64};
 static const int kTuneWarps[3] = {16, 20, 22};
-constexpr int kTuneCandidates = 9;
+constexpr int kTuneFill = 9;
+constexpr int kTuneCandidates = kTuneFill + kConvTiles - 1;
 
 extern "C" int cageo_autotune_candidates(cageo_tuning* h_out, int n) {
   for (int k = 0; h_out && k < n && k < kTuneCandidates; k++) {
-    h_out[k].fill_rounds = kTuneRounds[k % 3];
-    h_out[k].fill_warps = kTuneWarps[k / 3];
+    if (k < kTuneFill) {
+      h_out[k] = cageo_tuning{kTuneRounds[k % 3], kTuneWarps[k / 3], 0};
+    } else {
+      h_out[k] = cageo_tuning{0, 0, k - kTuneFill + 1};
+    }
   }
   return kTuneCandidates;
 }
@@ -907,9 +919,14 @@ extern "C" cageo_status cageo_pipeline_set_tuning(cageo_pipeline* p, const cageo
   CAGEO_CHECK_ARG(p && t, "null argument");
   CAGEO_CHECK_ARG(t->fill_rounds >= 1 && t->fill_rounds <= 1024, "fill rounds must be 1..1024");
   CAGEO_CHECK_ARG(fill_flood_warps_valid(t->fill_warps), "fill warps must be 16, 20 or 22");
+  CAGEO_CHECK_ARG(t->conv_tile >= 0 && t->conv_tile < kConvTiles,
+                  "convolution tile must be 0..3");
+  CAGEO_CHECK_ARG(conv_tile_applies(p->cfg.filter_model, p->radius, t->conv_tile),
+                  "the convolution tile does not fit this filter radius in shared memory");
   CAGEO_CUDA(cudaStreamSynchronize(p->stream));
   p->fw.max_rounds = t->fill_rounds;
   p->fw.flood_warps = t->fill_warps;
+  p->conv_tile = t->conv_tile;
   sync_batch_tuning(p);
   drop_graph(p);  // captured with the old launch shapes
   return CAGEO_OK;
@@ -919,6 +936,7 @@ extern "C" cageo_status cageo_pipeline_get_tuning(cageo_pipeline* p, cageo_tunin
   CAGEO_CHECK_ARG(p && t, "null argument");
   t->fill_rounds = p->fw.max_rounds;
   t->fill_warps = p->fw.flood_warps;
+  t->conv_tile = p->conv_tile;
   return CAGEO_OK;
 }
 
@@ -937,12 +955,27 @@ extern "C" cageo_status cageo_pipeline_autotune(cageo_pipeline* p, uint32_t firs
   CAGEO_CUDA(cudaEventCreate(&e1));
   cageo_status st = CAGEO_OK;
   float best_ms = 0.0f;
-  cageo_tuning best{p->fw.max_rounds, p->fw.flood_warps};
+  cageo_tuning best{p->fw.max_rounds, p->fw.flood_warps, p->conv_tile};
   cageo_tuning cand[kTuneCandidates];
   cageo_autotune_candidates(cand, kTuneCandidates);
   for (int c = 0; c < kTuneCandidates && st == CAGEO_OK; c++) {
-    p->fw.max_rounds = cand[c].fill_rounds;
-    p->fw.flood_warps = cand[c].fill_warps;
+    if (c < kTuneFill) {
+      p->fw.max_rounds = cand[c].fill_rounds;
+      p->fw.flood_warps = cand[c].fill_warps;
+    } else {
+      // Another convolution tile with the fill setting chosen above; a tile
+      // that does not apply (exponential filters use the 2D kernel) or does
+      // not fit the radius is skipped (0 ms).
+      cand[c].fill_rounds = best.fill_rounds;
+      cand[c].fill_warps = best.fill_warps;
+      if (!conv_tile_applies(p->cfg.filter_model, p->radius, cand[c].conv_tile)) {
+        if (h_ms && c < n_ms) h_ms[c] = 0.0f;
+        continue;
+      }
+      p->fw.max_rounds = best.fill_rounds;
+      p->fw.flood_warps = best.fill_warps;
+    }
+    p->conv_tile = cand[c].conv_tile;
     uint32_t r0 = first + (uint32_t)(c * (trials + 1));
     if (cudaMemcpyAsync(p->dscal, &r0, sizeof(r0), cudaMemcpyHostToDevice, s) != cudaSuccess) {
       st = cuda_fail(cudaGetLastError(), "cudaMemcpyAsync");
@@ -971,6 +1004,7 @@ extern "C" cageo_status cageo_pipeline_autotune(cageo_pipeline* p, uint32_t firs
   if (st) return st;
   p->fw.max_rounds = best.fill_rounds;
   p->fw.flood_warps = best.fill_warps;
+  p->conv_tile = best.conv_tile;
   sync_batch_tuning(p);
   drop_graph(p);
   if (h_best) *h_best = best;

@@ -391,19 +391,26 @@ cageo_status cageo_pipeline_profile(cageo_pipeline* p, uint32_t realization,
  * walled flood spent waiting for a tile, end of the queue included (last
  * realization). */
 cageo_status cageo_pipeline_stats(cageo_pipeline* p, int64_t* h_stats, int n);
-/* Tuning of the persistent fill kernels (no counterpart in the reference).
- * The results never depend on it.  fill_rounds: sweep rounds a fill tile
- * visit may run before the tile queues itself again (1..1024; default 64).
+/* Tuning of the pipeline's kernels (no counterpart in the reference).  The
+ * results never depend on it.  fill_rounds: sweep rounds a fill tile visit
+ * may run before the tile queues itself again (1..1024; default 64).
  * fill_warps: warps per SM of the fill's lower-bound flood (16, 20 or 22;
  * more warps hide more latency, fewer leave more registers to each; default
- * 20).  The tile shape is fixed at 32 x 32 cells, the warp width: a warp
- * owns a tile and holds its rows as 32-bit lane masks. */
+ * 20).  The fill's tile shape is fixed at 32 x 32 cells, the warp width: a
+ * warp owns a tile and holds its rows as 32-bit lane masks.  conv_tile:
+ * output tile of the fused front's separable (Gaussian) convolution per
+ * block, 0 = 64 x 32 (default), 1 = 128 x 32, 2 = 64 x 64, 3 = 96 x 32
+ * (columns x rows); only 0 applies to exponential filters, and a tile whose
+ * staged block does not fit shared memory for the radius is refused. */
 typedef struct {
   int fill_rounds;
   int fill_warps;
+  int conv_tile;
 } cageo_tuning;
 /* The autotuner's candidates: writes up to n of them to h_out (may be NULL)
- * and returns how many there are. */
+ * and returns how many there are: the fill settings (with conv_tile 0),
+ * then the other convolution tiles, whose fill fields are 0 (they run with
+ * the fill setting chosen among the first ones). */
 int cageo_autotune_candidates(cageo_tuning* h_out, int n);
 cageo_status cageo_pipeline_set_tuning(cageo_pipeline* p, const cageo_tuning* t);
 cageo_status cageo_pipeline_get_tuning(cageo_pipeline* p, cageo_tuning* t);
@@ -411,8 +418,8 @@ cageo_status cageo_pipeline_get_tuning(cageo_pipeline* p, cageo_tuning* t);
  * realizations from `first_realization` on, timed with CUDA events on the
  * pipeline's stream, and keeps the fastest.  h_best (may be NULL) receives
  * the choice, h_ms (may be NULL) up to n_ms milliseconds per realization,
- * one per candidate in cageo_autotune_candidates() order.  Resets the
- * counts to zero. */
+ * one per candidate in cageo_autotune_candidates() order (0 for a
+ * convolution tile that does not apply).  Resets the counts to zero. */
 cageo_status cageo_pipeline_autotune(cageo_pipeline* p, uint32_t first_realization,
                                      int trials, cageo_tuning* h_best, float* h_ms,
                                      int n_ms);

@@ -191,31 +191,77 @@ def test_checkpoint_survives_an_interrupted_save(cuda, tmp_path):
 
 
 def test_autotune_keeps_counts(cuda):
-    """The autotuner only changes launch settings of the fill (sweep rounds
-    per tile visit, warps per SM of the lower-bound flood): counts, filled
-    surface and labels equal an untuned pipeline's under every setting."""
+    """The autotuner only changes launch settings (the fill's sweep rounds
+    per tile visit and warps per SM of its lower-bound flood, the front's
+    convolution tile): counts, filled surface and labels equal an untuned
+    pipeline's under every setting."""
     from cageo_gb300 import api
     dem, streams = make_case(300, 200, seed=44)
     a = api.Pipeline(dem, streams, error_stddev=1.5, seed=9)
     best, ms = a.autotune(1000, trials=2)
     cands = api.autotune_candidates()
-    assert best in cands and len(ms) == len(cands) and all(v > 0 for _, v in ms)
-    assert {c["fill_warps"] for c in cands} == {16, 20, 22}
+    fill = [c for c in cands if c["fill_rounds"]]
+    assert len(ms) == len(cands) and all(v > 0 for _, v in ms)  # Gaussian: every tile applies
+    assert {c["fill_warps"] for c in fill} == {16, 20, 22}
+    assert {c["conv_tile"] for c in cands} == set(range(len(api.CONV_TILES)))
+    assert dict(best, conv_tile=0) in fill and 0 <= best["conv_tile"] < len(api.CONV_TILES)
     assert a.tuning() == best
     a.run(0, 3)
     b = api.Pipeline(dem, streams, error_stddev=1.5, seed=9)
     b.run(0, 3)
     assert np.array_equal(a.counts(), b.counts())
     fb = b.last_stages()
-    for rounds, warps in [(1, 16), (4, 22), (1024, 20)]:
+    for rounds, warps, tile in [(1, 16, 0), (4, 22, 1), (1024, 20, 2), (16, 20, 3)]:
         c = api.Pipeline(dem, streams, error_stddev=1.5, seed=9)
-        c.set_tuning(rounds, warps)
+        c.set_tuning(rounds, warps, tile)
         c.run(0, 3)
         assert np.array_equal(c.counts(), b.counts())
         fc = c.last_stages()
         assert np.array_equal(bits(fc[0]), bits(fb[0])) and np.array_equal(fc[2], fb[2])
     with pytest.raises(api.CageoError):
         c.set_tuning(32, 18)
+    with pytest.raises(api.CageoError):
+        c.set_tuning(32, 20, len(api.CONV_TILES))
+
+
+@pytest.mark.parametrize("range_m", [60.0, 90.0, 40.0])
+def test_conv_tiles_same_results(cuda, range_m):
+    """Every convolution tile shape of the fused front gives the same counts,
+    filled surface, directions and labels, single and in batched steps, for
+    the unrolled radii (15 and 23) and the generic kernel (10), on a grid
+    whose sides are multiples of no tile."""
+    from cageo_gb300 import api
+    dem, streams = make_case(333, 211, seed=46)
+    runs = []
+    for tile in range(len(api.CONV_TILES)):
+        for batch in (1, 3):
+            p = api.Pipeline(dem, streams, practical_range=range_m, error_stddev=1.5, seed=12)
+            p.set_tuning(64, 20, tile)
+            p.set_batch(batch)
+            p.run(0, 6)
+            runs.append(((tile, batch), p.counts(), p.last_stages()))
+            p.close()
+    (_, c0, (f0, d0, l0)) = runs[0]
+    assert c0.max() > 0
+    for key, c, (f, d, lab) in runs[1:]:
+        assert np.array_equal(c, c0), key
+        assert np.array_equal(bits(f), bits(f0)) and np.array_equal(d, d0), key
+        assert np.array_equal(lab, l0), key
+
+
+def test_conv_tiles_exponential(cuda):
+    """Exponential filters run the 2D kernel: only the first tile applies;
+    the autotuner skips the others (0 ms)."""
+    from cageo_gb300 import api
+    dem, streams = make_case(200, 150, seed=47)
+    p = api.Pipeline(dem, streams, filter_model=api.FILTER_EXPONENTIAL, practical_range=50.0,
+                     error_stddev=1.5, seed=3)
+    with pytest.raises(api.CageoError):
+        p.set_tuning(64, 20, 1)
+    best, ms = p.autotune(0, trials=1)
+    assert best["conv_tile"] == 0
+    assert [v for c, v in ms if c["conv_tile"]] == [0.0] * (len(api.CONV_TILES) - 1)
+    assert all(v > 0 for c, v in ms if not c["conv_tile"])
 
 
 @pytest.mark.parametrize("batch", [1, 3])

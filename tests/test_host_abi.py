@@ -163,3 +163,16 @@ def test_host_allocation_failure_is_a_status_not_an_abort(tmp_path):
     assert r.returncode == 0, r.stderr[-2000:]
     status, msg = r.stdout.strip().split(" ", 1)
     assert int(status) == 6 and "out of host memory" in msg, r.stdout
+
+
+def test_autotune_candidates_layout():
+    """Host-only: the fill settings (first convolution tile), then the other
+    convolution tiles with fill fields 0 (run with the chosen fill setting)."""
+    c = api.autotune_candidates()
+    fill = [x for x in c if x["fill_rounds"]]
+    assert len(fill) == 9 and all(x["conv_tile"] == 0 for x in fill)
+    assert {(x["fill_rounds"], x["fill_warps"]) for x in fill} == \
+        {(r, w) for r in (16, 32, 64) for w in (16, 20, 22)}
+    tiles = [x for x in c if not x["fill_rounds"]]
+    assert [x["conv_tile"] for x in tiles] == list(range(1, len(api.CONV_TILES)))
+    assert all(x["fill_warps"] == 0 for x in tiles) and len(c) == 9 + len(tiles)
