@@ -174,7 +174,14 @@ __device__ __forceinline__ float relay(float w, uint8_t f, float q) {
   if (MODE != 1 || !(f & FNONPASS)) return w;
   // A clean cell kept flood A's level, which is finite; it is confirmed
   // exactly when it is not below its q (what FCONF records for the others).
-  return ((f & (FCONF | FCLEAN)) && !(f & FBELOW)) ? w : kInf;
+  // Every level flood B relays is a passable value (it starts at a passable
+  // outlet's q and is only carried or raised to a passable cell's q), never
+  // a non-passable q, so a non-passable cell whose level equals its q was
+  // reached below it and is a wall: the store that lowered it to q also set
+  // FBELOW.  Testing w != q keeps a halo read that sees the new level but
+  // not yet the new flags (another SM's write-back stores the two with no
+  // order between them) from relaying q.
+  return ((f & (FCONF | FCLEAN)) && !(f & FBELOW) && w != q) ? w : kInf;
 }
 
 struct FloodArgs {
@@ -386,10 +393,17 @@ __device__ bool process_tile(WarpSmem<MODE>& s, const FloodArgs& a, int t, int l
     }
   }
   if constexpr (MODE != 1) cp_async_wait();
+  unsigned int clean0 = 0;  // MODE 2: this lane's column, rows clean when staged
   if constexpr (MODE == 2) {
     // Clean relays of the halo: strips of 34 cells (row above, row below,
-    // column left, column right), flags read again from L2.  A loop of its
-    // own keeps the staging loop above as it is in the other modes.
+    // column left, column right), flags read again from L2, after the
+    // levels and a fence.  A clean mark holds for the level it was derived
+    // at; a write-back that lowers a clean cell's level (withdrawing or
+    // re-deriving its mark) stores the flags, fences, then stores the level.
+    // So a halo level read above that is already the new one comes with a
+    // flag read here that is at least as new: never a stale clean mark with
+    // a lower level, which could mark a neighbour clean too low.
+    __threadfence();
     for (int k = lane; k < 4 * 34; k += 32) {
       const int strip = k / 34, j = k - strip * 34;
       const int hx = strip < 2 ? j : (strip == 2 ? 0 : 33);
@@ -399,6 +413,10 @@ __device__ bool process_tile(WarpSmem<MODE>& s, const FloodArgs& a, int t, int l
       if (gx >= 0 && gx < W && gy >= 0 && gy < H) fv = __ldcg(w.flags + (int64_t)gy * W + gx);
       s.HC[strip][j] = (fv & (FCLEAN | FNONPASS | FNODATA)) == FCLEAN;
     }
+    __syncwarp();
+#pragma unroll 8
+    for (int y = 0; y < kTile; y++)
+      clean0 |= (s.F[y * kFS + lane] & FCLEAN) ? (1u << y) : 0u;
   }
   __syncwarp();
   const long long c1 = clock64();
@@ -491,13 +509,25 @@ __device__ bool process_tile(WarpSmem<MODE>& s, const FloodArgs& a, int t, int l
   }
   // Write back the changed cells, row by row (coalesced); note which
   // borders changed.  Cells outside the grid are NODATA and never change.
+  // With clean marks, a changed cell that was clean when staged may have a
+  // lower level and a withdrawn or re-derived mark: flags first, a fence,
+  // then the levels (the readers' side is in the staging above).
   const unsigned int rows_changed = __reduce_or_sync(0xffffffffu, dc);
+  bool flags_first = false;
+  if constexpr (MODE == 2) flags_first = __any_sync(0xffffffffu, (dc & clean0) != 0u);
+  if (flags_first) {
+    for (unsigned int rows = rows_changed; rows; rows &= rows - 1) {
+      const int y = __ffs(rows) - 1;
+      if ((dc >> y) & 1u) w.flags[(int64_t)(y0 + y) * W + (x0 + lane)] = s.F[y * kFS + lane];
+    }
+    __threadfence();
+  }
   for (unsigned int rows = rows_changed; rows; rows &= rows - 1) {
     const int y = __ffs(rows) - 1;
     if ((dc >> y) & 1u) {
       const int64_t i = (int64_t)(y0 + y) * W + (x0 + lane);
       a.Wg[i] = staged_w(s, lane, y);
-      w.flags[i] = s.F[y * kFS + lane];
+      if (!flags_first) w.flags[i] = s.F[y * kFS + lane];
     }
   }
   // The write-back (and a "not converged" mark) is visible before any
