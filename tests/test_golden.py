@@ -59,3 +59,51 @@ def test_reference_harness_reproduces_fixtures():
     q, filled = R.pitfill(g["burned"])
     assert np.array_equal(bits(filled), bits(g["filled"]))
     assert np.array_equal(R.flow_route(filled), g["dirs"])
+
+
+def _passable(v, minE):
+    """The reference fill's round trip toElev(toIndex(v)) == v in float32
+    (src/pitfilling/PitFillingAlgorithmCPUOpenMP.h:56-60, 178)."""
+    v = np.asarray(v, np.float32)
+    p = np.float32(1000.0) * (v - np.float32(minE))
+    z = np.where(p > 0, np.where(p >= np.float32(4294967040.0), np.float32(4294967295.0),
+                                 np.trunc(p)), 0).astype(np.uint64)
+    back = z.astype(np.float32) / np.float32(1000.0) + np.float32(minE)
+    return back == v
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_raised_levels_are_passable(path):
+    """The invariant the GPU fill's walled flood relies on: a level the
+    reference's fill carries to another cell comes from a cell that
+    expands, so every cell raised above its own q holds a passable value,
+    never a non-passable q.  (A non-passable cell at its own q was reached
+    below it; the walled flood treats it as a wall.)"""
+    g = np.load(path)
+    q, filled = g["quantized"], g["filled"]
+    nodata = q == np.float32(-9999.0)
+    minE = np.float32(q.min())  # over every cell, NODATA included, as the reference's minmax
+    raised = (filled > q) & ~nodata
+    assert raised.sum() > 0
+    assert np.all(_passable(filled[raised], minE))
+    # Non-passable cells exist, so the check is not vacuous.
+    assert np.sum(~_passable(q[~nodata], minE)) > 0
+
+
+@pytest.mark.parametrize("W,H,seed,plateaus,lo", [(256, 200, 61, 0.0, 80.0),
+                                                   (300, 257, 62, 0.2, 80.0),
+                                                   (200, 180, 63, 0.0, 0.0)])
+def test_raised_levels_are_passable_oracle(oracle, W, H, seed, plateaus, lo):
+    """The same invariant on seeded grids through the pinned restatement,
+    with lake plateaus and with relief starting at 0 (burned streams at 0)."""
+    from cases import make_case, gaussian_noise
+    from cageo_gb300 import api
+    dem, streams = make_case(W, H, seed=seed, plateaus=plateaus, lo=lo)
+    r = api.filter_radius(60.0, 10.0)
+    taps = api.filter_build(1, 60.0, 10.0, r)
+    conv = oracle.convolve(gaussian_noise(W, H, seed + 1, 1.5), taps, r, 1)
+    burned = oracle.stream_burn(oracle.realistic_dem(dem, conv), streams)
+    q, filled = oracle.pitfill(burned)
+    raised = filled > q
+    assert raised.sum() > 0
+    assert np.all(_passable(filled[raised], q.min()))
