@@ -374,8 +374,58 @@ __device__ bool process_tile(WarpSmem<MODE>& s, const FloodArgs& a, int t, int l
       else *dq = 0.0f;
     }
   }
+  // Flood A on a tile whose 32 columns lie inside the grid, with 16-byte
+  // aligned rows: its columns' levels and flags by 16-byte and 4-byte loads
+  // (8 chunks of 4 cells per staged row, 8.5 per lane, all in flight at
+  // once), the two halo columns by scalar loads: about 21 loads per lane
+  // instead of 72.  Every load lies inside the grid.
+  const bool vec = MODE != 1 && x0 + kTile <= W && (W & 3) == 0 &&
+                   ((reinterpret_cast<uintptr_t>(a.Wg) | reinterpret_cast<uintptr_t>(w.flags)) &
+                    15u) == 0;
+  if (vec) {
+    constexpr int kChunks = 34 * (kTile / 4);  // 272
+#pragma unroll
+    for (int it = 0; it < (kChunks + 31) / 32; it++) {
+      const int k = lane + 32 * it;
+      if (k < kChunks) {
+        const int hy = k >> 3, c = k & 7;
+        const int gy = y0 - 1 + hy;
+        float4 wv = make_float4(kInf, kInf, kInf, kInf);
+        unsigned int f4 = 0x01010101u * FNODATA;
+        if (gy >= 0 && gy < H) {
+          const int64_t i = (int64_t)gy * W + x0 + 4 * c;
+          wv = __ldcg(reinterpret_cast<const float4*>(a.Wg + i));
+          f4 = __ldcg(reinterpret_cast<const unsigned int*>(w.flags + i));
+        }
+        float* r = &s.R[hy * kRS + 1 + 4 * c];
+        r[0] = relay<MODE>(wv.x, (uint8_t)f4, wv.x);
+        r[1] = relay<MODE>(wv.y, (uint8_t)(f4 >> 8), wv.y);
+        r[2] = relay<MODE>(wv.z, (uint8_t)(f4 >> 16), wv.z);
+        r[3] = relay<MODE>(wv.w, (uint8_t)(f4 >> 24), wv.w);
+        if (hy >= 1 && hy <= kTile)
+          *reinterpret_cast<unsigned int*>(&s.F[(hy - 1) * kFS + 4 * c]) = f4;
+      }
+    }
+#pragma unroll
+    for (int it = 0; it < 3; it++) {
+      const int k = lane + 32 * it;
+      if (k < 2 * 34) {
+        const int side = k >= 34 ? 1 : 0, hy = k - 34 * side;
+        const int hx = side ? kTile + 1 : 0;
+        const int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
+        float wv = kInf;
+        uint8_t fv = FNODATA;
+        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+          const int64_t i = (int64_t)gy * W + gx;
+          wv = __ldcg(a.Wg + i);
+          fv = __ldcg(w.flags + i);
+        }
+        s.R[hy * kRS + hx] = relay<MODE>(wv, fv, wv);
+      }
+    }
+  }
 #pragma unroll 12
-  for (int idx = lane; idx < 34 * 34; idx += 32) {
+  for (int idx = vec ? 34 * 34 : lane; idx < 34 * 34; idx += 32) {
     int hy = idx / 34, hx = idx - hy * 34;
     int gx = x0 - 1 + hx, gy = y0 - 1 + hy;
     float wv = kInf, qv = 0.0f;
