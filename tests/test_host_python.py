@@ -44,3 +44,23 @@ def test_warmstart_parameter_layout():
     assert trained.shape == p.shape and np.isfinite(trained).all()
     meta = learned.load_meta()
     assert meta["steps"] > 0 and "evaluation" in meta
+
+
+def test_plateaus_cover_their_share():
+    """Lake plateaus: discs flattened to their centre elevation until the
+    requested share of the area is flat (the stress workload asks 20% in
+    discs of radius 50-400 cells at 16384^2, Gaussian 90 m: radius 23)."""
+    dem = synth.fbm_dem(600, 500, 0.8, 3, 0.0, 300.0)
+    flat = synth.add_plateaus(dem, 0.2, seed=3, radius=(5, 40))
+    assert np.array_equal(synth.add_plateaus(dem, 0.2, seed=3, radius=(5, 40)), flat)
+    changed = np.count_nonzero(flat != dem) / dem.size
+    # Each disc keeps its centre's value; the last disc may overshoot by its area.
+    assert 0.2 - 0.01 <= changed <= 0.2 + np.pi * 40 ** 2 / dem.size
+    # Flattened cells equal a neighbour exactly (the fBm surface alone almost never does).
+    eq = np.zeros(dem.shape, bool)
+    for dy, dx in ((0, 1), (0, -1), (1, 0), (-1, 0)):
+        eq |= flat == np.roll(flat, (dy, dx), axis=(0, 1))
+    assert np.count_nonzero(eq) / dem.size >= 0.19
+    p = synth.WORKLOADS["stress-16384"]
+    assert (p["width"], p["height"], p["plateaus"], p["range_m"]) == (16384, 16384, 0.2, 90.0)
+    assert api.filter_radius(p["range_m"], p["cell"]) == 23
