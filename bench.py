@@ -374,7 +374,11 @@ def main():
     progress("autotuned: %s" % tuned)
     batch_ms = {}
     for b in args.batch_candidates:
-        pipe.set_batch(b)
+        try:
+            pipe.set_batch(b)
+        except api.CageoError as e:  # a stack of b grids at 2^31 cells or more, or no memory
+            progress("batch size %d refused: %s" % (b, e))
+            continue
         pipe.run(base + 800_000, b)
         batch_ms[b] = timed(base + 800_000 + 100 * b, 3 * b) / (3 * b)
     batch = min(batch_ms, key=batch_ms.get)
